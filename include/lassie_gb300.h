@@ -1,0 +1,176 @@
+/*
+ * lassie_gb300.h -- C ABI of the GB300-native LASSIE integrator.
+ *
+ * The reference (aresio/LASSIE) has no library interface: its boundary is the
+ * command line `LASSIE input_folder output_folder` (src/c++/simulator.cu:29)
+ * and the files of those folders.  Behind its CLI the engine is one class,
+ * Simulation<T>::run (src/c++/header/Simulation.cuh:230-981), which parses the
+ * folder, compiles the network, integrates on the GPU and writes the outputs.
+ * The entry points below are that engine split at the natural seams, with
+ * plain pointers and sizes so any host (the bundled C++ CLI, Python ctypes,
+ * cgo, JNI) can bind them.  Each cites the reference code it replaces.
+ *
+ * Conventions: every function returns LASSIE_OK (0) or a negative status;
+ * host buffers are caller-owned; device memory is owned by the library and
+ * released by the matching destroy call.  A model handle may be shared by
+ * concurrent solves; a batch handle is not thread-safe.  `stream` arguments
+ * are cudaStream_t values passed as void* (NULL = the legacy stream).
+ */
+#ifndef LASSIE_GB300_H
+#define LASSIE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- statuses */
+#define LASSIE_OK 0
+/* -1 .. -13 are the reference's process exit codes (simulator.cu:66-335,
+   Simulation.cuh:43-1010); the CLI exits with them. */
+#define LASSIE_ERR_INPUT_FOLDER (-1)
+#define LASSIE_ERR_MANDATORY (-4)
+#define LASSIE_ERR_MODELKIND (-7)
+#define LASSIE_ERR_VOLUME (-8)
+#define LASSIE_ERR_ORDER (-12)
+#define LASSIE_ERR_CUDA (-13)
+/* new statuses of the library */
+#define LASSIE_ERR_ARGS (-20)        /* invalid argument */
+#define LASSIE_ERR_MAX_STEPS (-21)   /* opts.max_steps loop iterations reached */
+#define LASSIE_ERR_ALLOC (-22)       /* host or device allocation failed */
+#define LASSIE_ERR_TOO_LARGE (-23)   /* network does not fit the engine */
+#define LASSIE_ERR_DEADLINE (-24)    /* opts.deadline_s elapsed on the device */
+#define LASSIE_ERR_NO_DEVICE (-25)   /* no CUDA device / not sm_103 */
+
+/* precision of the Newton matrix factorisation */
+#define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */
+#define LASSIE_PREC_MIXED 1 /* FP32 LU + FP64 iterative refinement */
+
+typedef struct lassie_model lassie_model;
+typedef struct lassie_batch lassie_batch;
+
+/* Integration options.  Defaults (lassie_opts_default) are the reference's
+   optional-file defaults, Simulation.cuh:272-354. */
+typedef struct {
+    double rkf_step;      /* initial RKF45 step, file rkf_step (1e-3) */
+    double be_step;       /* backward-Euler step, file be_step (0.01) */
+    double newton_tol;    /* Newton ||dx||_2 tolerance, file newton_tol (1e-6) */
+    double stiffness_tol; /* stiffness switch threshold, file stiffness_tol (1e-6) */
+    int64_t newton_iter;  /* Newton iteration cap, file newton_iter (10000) */
+    int64_t max_steps;    /* loop-iteration cap per instance, 0 = none */
+    double deadline_s;    /* device wall-clock limit per launch, 0 = none */
+    int32_t precision;    /* LASSIE_PREC_* */
+    int32_t refine_max;   /* refinement sweeps per linear solve (mixed), 0 = 8 */
+} lassie_opts;
+
+/* Per-instance counters; status is the instance's LASSIE_* result. */
+typedef struct {
+    int64_t outer_iters;
+    int64_t rkf_accepts;
+    int64_t rkf_retries;
+    int64_t be_steps;
+    int64_t newton_iters;
+    int64_t lu_factorisations;
+    int64_t lu_failures;
+    int64_t nan_reverts;
+    int64_t refine_sweeps;
+    double t_final;
+    double dt_be_final;
+    int32_t status;
+    int32_t pad;
+} lassie_stats;
+
+/* One instance of a batch: a network, its parameterisation and its outputs.
+   feed, atol and cs may be NULL (no feed, atol 1e-12, all species). */
+typedef struct {
+    const lassie_model *model;
+    const double *k;    /* [R] rate constants */
+    const double *x0;   /* [N] initial state */
+    const double *feed; /* [N] fed (constant) species, 0 = not fed */
+    const double *atol; /* [N] RKF45 absolute tolerance per unit time */
+    const double *t;    /* [nt] sampling times */
+    int32_t nt;
+    int32_t ncs;
+    const int32_t *cs;  /* [ncs] sampled species */
+    double *out;        /* [nt * ncs] host output, row per sample */
+} lassie_instance;
+
+void lassie_opts_default(lassie_opts *opts);
+const char *lassie_status_string(int status);
+/* Text of the last CUDA or argument error on the calling thread. */
+const char *lassie_last_error(void);
+/* 1 if an sm_103 device is visible and the kernels load, else 0 */
+int lassie_device_ok(void);
+
+/* Model compiler: replaces Simulation.cuh:397-418 (createTransposte,
+   create_sparse, create_sparse2) with int32 CSR (no int16 cap).
+   left/right: dense R x N row-major reactant/product stoichiometries, the
+   contents of the left_side / right_side files (Reader.h:104-124). */
+int lassie_model_create_dense(int32_t n_species, int32_t n_reactions,
+                              const int32_t *left, const int32_t *right,
+                              lassie_model **out);
+/* Same network given by reaction: reactants react_ptr[R+1] / react_species /
+   react_stoich and products prod_ptr[R+1] / prod_species / prod_stoich
+   (repeated species are summed). */
+int lassie_model_create_csr(int32_t n_species, int32_t n_reactions,
+                            const int32_t *react_ptr, const int32_t *react_species,
+                            const int32_t *react_stoich, const int32_t *prod_ptr,
+                            const int32_t *prod_species, const int32_t *prod_stoich,
+                            lassie_model **out);
+void lassie_model_destroy(lassie_model *model);
+int lassie_model_info(const lassie_model *model, int32_t *n_species,
+                      int32_t *n_reactions, int32_t *nnz_reactants,
+                      int32_t *nnz_net);
+
+/* One integration, host buffers in and out: the time loop of
+   Simulation.cuh:632-925 plus the sampling of :674-690 and the D2H copy of
+   :942.  out has nt*ncs doubles (cs NULL: ncs = N). */
+int lassie_solve(const lassie_model *model, const double *k, const double *x0,
+                 const double *feed, const double *atol, const double *t,
+                 int32_t nt, const int32_t *cs, int32_t ncs,
+                 const lassie_opts *opts, double *out, lassie_stats *stats);
+
+/* Many independent instances of possibly different networks and sizes in
+   one persistent launch (no reference counterpart: the reference runs one
+   model per process).  Host buffers in and out; stats may be NULL. */
+int lassie_solve_batch(const lassie_instance *inst, int32_t n,
+                       const lassie_opts *opts, lassie_stats *stats);
+
+/* Device-resident batch: upload once, run many times (inputs stay in HBM),
+   read back on demand.  lassie_batch_run only launches on `stream`;
+   lassie_batch_sync waits and returns the first failing instance status. */
+int lassie_batch_create(const lassie_instance *inst, int32_t n,
+                        const lassie_opts *opts, lassie_batch **out);
+int lassie_batch_run(lassie_batch *batch, void *stream);
+int lassie_batch_sync(lassie_batch *batch);
+int lassie_batch_read(lassie_batch *batch, const lassie_instance *inst,
+                      lassie_stats *stats);
+/* kernel launches one lassie_batch_run issues (for launch accounting) */
+int lassie_batch_launches(const lassie_batch *batch);
+void lassie_batch_destroy(lassie_batch *batch);
+
+/* ---------------------------------------------------- single evaluations */
+/* dx = f(x) for n_inst parameterisations of one network, device buffers,
+   instance-major: k [n_inst][R], x and dx [n_inst][N].  Replaces
+   generate_ode (kernels.cuh:5-50). */
+int lassie_rhs_device(const lassie_model *model, int32_t n_inst, const double *k,
+                      const double *x, double *dx, void *stream);
+/* Host-buffer wrappers (one instance) used by parity tests. */
+int lassie_rhs(const lassie_model *model, const double *k, const double *x,
+               double *dx);
+/* M = I - h*J(x), dense row-major N x N FP64, J with the reference's
+   createJac semantics (kernels.cuh:205-271, 393-402). */
+int lassie_newton_matrix(const lassie_model *model, const double *k,
+                         const double *x, double h, double *M);
+/* Factor a row-major n x n matrix with the engine's LU (precision as in
+   lassie_opts) and solve A x = b; returns 1 + column of the first exactly
+   zero pivot when singular.  Replaces linearSolverLU (Simulation.cuh:1280). */
+int lassie_lu_solve(int32_t n, const double *a, const double *b, double *x,
+                    int32_t precision);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

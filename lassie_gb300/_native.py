@@ -1,0 +1,128 @@
+"""ctypes binding of ``liblassie_gb300.so`` (the C ABI in
+``include/lassie_gb300.h``).  Loading fails loudly when the library is
+missing: there is no CPU fallback."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_native", "liblassie_gb300.so")
+
+OK = 0
+ERR_ARGS = -20
+ERR_MAX_STEPS = -21
+ERR_ALLOC = -22
+ERR_TOO_LARGE = -23
+ERR_DEADLINE = -24
+ERR_NO_DEVICE = -25
+ERR_CUDA = -13
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# every function the header declares (checked by the CPU test suite)
+EXPORTS = (
+    "lassie_opts_default", "lassie_status_string", "lassie_last_error", "lassie_device_ok",
+    "lassie_model_create_dense", "lassie_model_create_csr", "lassie_model_destroy",
+    "lassie_model_info", "lassie_solve", "lassie_solve_batch", "lassie_batch_create",
+    "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
+    "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
+    "lassie_lu_solve",
+)
+
+
+class Opts(C.Structure):
+    _fields_ = [("rkf_step", C.c_double), ("be_step", C.c_double),
+                ("newton_tol", C.c_double), ("stiffness_tol", C.c_double),
+                ("newton_iter", C.c_int64), ("max_steps", C.c_int64),
+                ("deadline_s", C.c_double), ("precision", C.c_int32),
+                ("refine_max", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("outer_iters", C.c_int64), ("rkf_accepts", C.c_int64),
+                ("rkf_retries", C.c_int64), ("be_steps", C.c_int64),
+                ("newton_iters", C.c_int64), ("lu_factorisations", C.c_int64),
+                ("lu_failures", C.c_int64), ("nan_reverts", C.c_int64),
+                ("refine_sweeps", C.c_int64), ("t_final", C.c_double),
+                ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
+class Instance(C.Structure):
+    _fields_ = [("model", C.c_void_p), ("k", C.c_void_p), ("x0", C.c_void_p),
+                ("feed", C.c_void_p), ("atol", C.c_void_p), ("t", C.c_void_p),
+                ("nt", C.c_int32), ("ncs", C.c_int32), ("cs", C.c_void_p),
+                ("out", C.c_void_p)]
+
+
+class LassieError(RuntimeError):
+    def __init__(self, status: int, where: str = ""):
+        lib_ = _lib
+        msg = ""
+        if lib_ is not None:
+            msg = lib_.lassie_status_string(status).decode()
+            last = lib_.lassie_last_error().decode()
+            if last:
+                msg += f" ({last})"
+        super().__init__(f"{where}: status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load():
+    """Load the library (building it first if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            from . import build as _build
+            _build.build()
+        L = C.CDLL(LIB_PATH)
+        vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+        L.lassie_opts_default.argtypes = [C.POINTER(Opts)]
+        L.lassie_opts_default.restype = None
+        L.lassie_status_string.argtypes = [C.c_int]
+        L.lassie_status_string.restype = C.c_char_p
+        L.lassie_last_error.argtypes = []
+        L.lassie_last_error.restype = C.c_char_p
+        L.lassie_device_ok.argtypes = []
+        L.lassie_device_ok.restype = C.c_int
+        L.lassie_model_create_dense.argtypes = [i32, i32, vp, vp, C.POINTER(vp)]
+        L.lassie_model_create_csr.argtypes = [i32, i32, vp, vp, vp, vp, vp, vp, C.POINTER(vp)]
+        L.lassie_model_destroy.argtypes = [vp]
+        L.lassie_model_destroy.restype = None
+        L.lassie_model_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32),
+                                        C.POINTER(i32)]
+        L.lassie_solve.argtypes = [vp, vp, vp, vp, vp, vp, i32, vp, i32, C.POINTER(Opts), vp,
+                                   C.POINTER(Stats)]
+        L.lassie_solve_batch.argtypes = [vp, i32, C.POINTER(Opts), vp]
+        L.lassie_batch_create.argtypes = [vp, i32, C.POINTER(Opts), C.POINTER(vp)]
+        L.lassie_batch_run.argtypes = [vp, vp]
+        L.lassie_batch_sync.argtypes = [vp]
+        L.lassie_batch_read.argtypes = [vp, vp, vp]
+        L.lassie_batch_launches.argtypes = [vp]
+        L.lassie_batch_destroy.argtypes = [vp]
+        L.lassie_batch_destroy.restype = None
+        L.lassie_rhs_device.argtypes = [vp, i32, vp, vp, vp, vp]
+        L.lassie_rhs.argtypes = [vp, vp, vp, vp]
+        L.lassie_newton_matrix.argtypes = [vp, vp, vp, dbl, vp]
+        L.lassie_lu_solve.argtypes = [i32, vp, vp, vp, i32]
+        for name in EXPORTS:
+            f = getattr(L, name)
+            if f.restype is C.c_int and name not in ("lassie_device_ok",):
+                f.restype = C.c_int
+        _lib = L
+        return L
+
+
+def check(status: int, where: str) -> None:
+    if status != OK:
+        raise LassieError(status, where)

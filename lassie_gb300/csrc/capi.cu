@@ -1,0 +1,647 @@
+// C ABI of the LASSIE GB300 engine: model compiler, batch packing, device
+// memory, launches.  Host code only; the kernels are in compat_engine.cu.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "lassie_gb300.h"
+
+namespace lassie {
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int precision);
+cudaError_t compat_configure(int precision, int64_t smem);
+cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
+cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, const int *rptr,
+                             const int *rent, const int *sptr, const int *sent,
+                             const double *k, const double *x, double *dx, int sm_count,
+                             cudaStream_t stream);
+cudaError_t newton_matrix_launch(int N, int R, int nnz_a, const int *rptr, const int *rent,
+                                 const int *sptr, const int *sent, const double *k,
+                                 const double *x, double h, double *M, cudaStream_t stream);
+cudaError_t lu_solve_launch(int N, void *A, int ld, const double *b, double *x, int *info,
+                            int precision, cudaStream_t stream);
+int64_t lu_solve_smem(int N, int precision);
+}  // namespace lassie
+
+using namespace lassie;
+
+// ----------------------------------------------------------- error state
+
+static thread_local std::string g_last_error;
+
+static int set_error(int status, const std::string &msg) {
+    g_last_error = msg;
+    return status;
+}
+
+#define CU(call)                                                                     \
+    do {                                                                             \
+        cudaError_t _e = (call);                                                     \
+        if (_e != cudaSuccess)                                                       \
+            return set_error(LASSIE_ERR_CUDA, std::string(#call) + ": " +           \
+                                                  cudaGetErrorString(_e));           \
+    } while (0)
+
+// ----------------------------------------------------------------- model
+
+struct lassie_model {
+    int32_t N = 0, R = 0;
+    std::vector<int32_t> rxn_ptr, rxn_ent, sp_ptr, sp_ent;
+    std::mutex mu;
+    int dev = -1;
+    int32_t *d_struct = nullptr;  // [rxn_ptr | rxn_ent | sp_ptr | sp_ent]
+
+    int64_t off_rent() const { return R + 1; }
+    int64_t off_sptr() const { return off_rent() + (int64_t)rxn_ent.size(); }
+    int64_t off_sent() const { return off_sptr() + N + 1; }
+    int64_t struct_len() const { return off_sent() + (int64_t)sp_ent.size(); }
+};
+
+static const int kMaxIndex = (1 << 23) - 1;
+
+// Simulation.cuh:397-418, 1061-1130: reactants by reaction (species
+// ascending), net stoichiometry H = (B-A)^T by species (reactions ascending).
+static int build_model(int32_t N, int32_t R, const std::vector<std::vector<std::pair<int, int>>> &A,
+                       const std::vector<std::vector<std::pair<int, int>>> &H, lassie_model **out) {
+    lassie_model *m = new (std::nothrow) lassie_model;
+    if (!m) return set_error(LASSIE_ERR_ALLOC, "model allocation");
+    m->N = N;
+    m->R = R;
+    m->rxn_ptr.resize(R + 1);
+    for (int j = 0; j < R; j++) {
+        m->rxn_ptr[j] = (int32_t)m->rxn_ent.size();
+        for (auto &e : A[j]) {
+            if (e.second < -128 || e.second > 127) {
+                delete m;
+                return set_error(LASSIE_ERR_TOO_LARGE, "stoichiometry outside [-128,127]");
+            }
+            m->rxn_ent.push_back(make_ent(e.first, e.second));
+        }
+    }
+    m->rxn_ptr[R] = (int32_t)m->rxn_ent.size();
+    std::vector<std::vector<std::pair<int, int>>> bys(N);
+    for (int j = 0; j < R; j++)
+        for (auto &e : H[j]) bys[e.first].push_back({j, e.second});
+    m->sp_ptr.resize(N + 1);
+    for (int s = 0; s < N; s++) {
+        m->sp_ptr[s] = (int32_t)m->sp_ent.size();
+        for (auto &e : bys[s]) {
+            if (e.second < -128 || e.second > 127) {
+                delete m;
+                return set_error(LASSIE_ERR_TOO_LARGE, "net stoichiometry outside [-128,127]");
+            }
+            m->sp_ent.push_back(make_ent(e.first, e.second));
+        }
+    }
+    m->sp_ptr[N] = (int32_t)m->sp_ent.size();
+    *out = m;
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_model_create_dense(int32_t N, int32_t R, const int32_t *left,
+                                         const int32_t *right, lassie_model **out) {
+    if (!out || !left || !right || N <= 0 || R <= 0 || N > kMaxIndex || R > kMaxIndex)
+        return set_error(LASSIE_ERR_ARGS, "model_create_dense: bad arguments");
+    std::vector<std::vector<std::pair<int, int>>> A(R), H(R);
+    for (int j = 0; j < R; j++) {
+        const int32_t *l = left + (int64_t)j * N, *r = right + (int64_t)j * N;
+        for (int s = 0; s < N; s++) {
+            if (l[s] != 0) A[j].push_back({s, l[s]});
+            const int h = r[s] - l[s];
+            if (h != 0) H[j].push_back({s, h});
+        }
+    }
+    return build_model(N, R, A, H, out);
+}
+
+extern "C" int lassie_model_create_csr(int32_t N, int32_t R, const int32_t *rp,
+                                       const int32_t *rs, const int32_t *rc, const int32_t *pp,
+                                       const int32_t *ps, const int32_t *pc, lassie_model **out) {
+    if (!out || !rp || !pp || N <= 0 || R <= 0 || N > kMaxIndex || R > kMaxIndex)
+        return set_error(LASSIE_ERR_ARGS, "model_create_csr: bad arguments");
+    std::vector<std::vector<std::pair<int, int>>> A(R), H(R);
+    for (int j = 0; j < R; j++) {
+        std::map<int, int> a, b;
+        for (int q = rp[j]; q < rp[j + 1]; q++) {
+            if (rs[q] < 0 || rs[q] >= N) return set_error(LASSIE_ERR_ARGS, "species index");
+            a[rs[q]] += rc[q];
+        }
+        for (int q = pp[j]; q < pp[j + 1]; q++) {
+            if (ps[q] < 0 || ps[q] >= N) return set_error(LASSIE_ERR_ARGS, "species index");
+            b[ps[q]] += pc[q];
+        }
+        std::map<int, int> h;
+        for (auto &e : a)
+            if (e.second != 0) A[j].push_back(e);
+        for (auto &e : a) h[e.first] -= e.second;
+        for (auto &e : b) h[e.first] += e.second;
+        for (auto &e : h)
+            if (e.second != 0) H[j].push_back(e);
+    }
+    return build_model(N, R, A, H, out);
+}
+
+extern "C" void lassie_model_destroy(lassie_model *m) {
+    if (!m) return;
+    if (m->d_struct) {
+        int cur = 0;
+        cudaGetDevice(&cur);
+        cudaSetDevice(m->dev);
+        cudaFree(m->d_struct);
+        cudaSetDevice(cur);
+    }
+    delete m;
+}
+
+extern "C" int lassie_model_info(const lassie_model *m, int32_t *n, int32_t *r, int32_t *na,
+                                 int32_t *nh) {
+    if (!m) return set_error(LASSIE_ERR_ARGS, "null model");
+    if (n) *n = m->N;
+    if (r) *r = m->R;
+    if (na) *na = (int32_t)m->rxn_ent.size();
+    if (nh) *nh = (int32_t)m->sp_ent.size();
+    return LASSIE_OK;
+}
+
+// Device copy of a model's structure (for the single-evaluation entry points).
+static int model_device(lassie_model *m, const int32_t **d) {
+    std::lock_guard<std::mutex> g(m->mu);
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (m->d_struct && m->dev == dev) {
+        *d = m->d_struct;
+        return LASSIE_OK;
+    }
+    if (m->d_struct) {
+        return set_error(LASSIE_ERR_ARGS, "model already bound to another device");
+    }
+    std::vector<int32_t> h((size_t)m->struct_len());
+    std::copy(m->rxn_ptr.begin(), m->rxn_ptr.end(), h.begin());
+    std::copy(m->rxn_ent.begin(), m->rxn_ent.end(), h.begin() + m->off_rent());
+    std::copy(m->sp_ptr.begin(), m->sp_ptr.end(), h.begin() + m->off_sptr());
+    std::copy(m->sp_ent.begin(), m->sp_ent.end(), h.begin() + m->off_sent());
+    CU(cudaMalloc(&m->d_struct, h.size() * sizeof(int32_t)));
+    CU(cudaMemcpy(m->d_struct, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    m->dev = dev;
+    *d = m->d_struct;
+    return LASSIE_OK;
+}
+
+// ------------------------------------------------------------- utilities
+
+extern "C" void lassie_opts_default(lassie_opts *o) {
+    if (!o) return;
+    o->rkf_step = 1e-3;
+    o->be_step = 0.01;
+    o->newton_tol = 1e-6;
+    o->stiffness_tol = 1e-6;
+    o->newton_iter = 10000;
+    o->max_steps = 0;
+    o->deadline_s = 0.0;
+    o->precision = LASSIE_PREC_MIXED;
+    o->refine_max = 0;
+}
+
+extern "C" const char *lassie_status_string(int s) {
+    switch (s) {
+    case LASSIE_OK: return "ok";
+    case LASSIE_ERR_INPUT_FOLDER: return "the input folder does not exist";
+    case LASSIE_ERR_MANDATORY: return "a mandatory input file is missing or inconsistent";
+    case LASSIE_ERR_MODELKIND: return "modelkind must be deterministic/concentration or stochastic/number";
+    case LASSIE_ERR_VOLUME: return "stochastic model without a volume";
+    case LASSIE_ERR_ORDER: return "a reaction has order higher than two";
+    case LASSIE_ERR_CUDA: return "CUDA error";
+    case LASSIE_ERR_ARGS: return "invalid argument";
+    case LASSIE_ERR_MAX_STEPS: return "maximum number of steps reached";
+    case LASSIE_ERR_ALLOC: return "allocation failed";
+    case LASSIE_ERR_TOO_LARGE: return "network too large for the engine";
+    case LASSIE_ERR_DEADLINE: return "device deadline elapsed";
+    case LASSIE_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char *lassie_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int lassie_device_ok(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return 0;
+    }
+    int dev = 0;
+    cudaDeviceProp p;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&p, dev) != cudaSuccess)
+        return 0;
+    return (p.major == 10 && p.minor == 3) ? 1 : 0;
+}
+
+// Grow-only device buffer.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int grow(size_t n) {
+        if (n <= cap) return LASSIE_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = std::max<size_t>(n, 256);
+        if (cudaMalloc(&p, want) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error(LASSIE_ERR_ALLOC, "cudaMalloc of " + std::to_string(want) + " bytes");
+        }
+        cap = want;
+        return LASSIE_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// ----------------------------------------------------------------- batch
+
+struct lassie_batch {
+    int dev = 0;
+    int n = 0;
+    int sm_count = 0;
+    lassie_opts opts{};
+    std::vector<InstDesc> desc;
+    std::vector<int32_t> order;
+    int64_t n_int = 0, n_dbl = 0, n_out = 0;
+    int32_t nmax = 0, rmax = 0, amax = 0;
+    int64_t smem = 0;
+    int grid = 0;
+    DevBuf d_int, d_dbl, d_out, d_desc, d_order, d_res, d_queue, d_ws;
+    cudaStream_t stream = nullptr;
+    LaunchParams P{};
+    ~lassie_batch() {
+        d_int.release();
+        d_dbl.release();
+        d_out.release();
+        d_desc.release();
+        d_order.release();
+        d_res.release();
+        d_queue.release();
+        d_ws.release();
+    }
+};
+
+static int validate_instance(const lassie_instance &q) {
+    if (!q.model || !q.k || !q.x0 || (q.nt > 0 && (!q.t || !q.out)) || q.nt < 0)
+        return set_error(LASSIE_ERR_ARGS, "instance: missing buffer");
+    const int N = q.model->N;
+    if (q.cs) {
+        if (q.ncs < 0) return set_error(LASSIE_ERR_ARGS, "instance: ncs");
+        for (int j = 0; j < q.ncs; j++)
+            if (q.cs[j] < 0 || q.cs[j] >= N)
+                return set_error(LASSIE_ERR_ARGS, "instance: cs out of range");
+    }
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const lassie_opts *opts,
+                                   lassie_batch **out) {
+    if (!out || (n > 0 && !inst) || n < 0) return set_error(LASSIE_ERR_ARGS, "batch_create");
+    lassie_opts o;
+    if (opts) o = *opts;
+    else lassie_opts_default(&o);
+    if (o.precision != LASSIE_PREC_FP64 && o.precision != LASSIE_PREC_MIXED)
+        return set_error(LASSIE_ERR_ARGS, "precision");
+    for (int q = 0; q < n; q++) {
+        int rc = validate_instance(inst[q]);
+        if (rc) return rc;
+    }
+    lassie_batch *b = new (std::nothrow) lassie_batch;
+    if (!b) return set_error(LASSIE_ERR_ALLOC, "batch allocation");
+    b->n = n;
+    b->opts = o;
+    int rc;
+    if (cudaGetDevice(&b->dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->dev) !=
+            cudaSuccess) {
+        delete b;
+        cudaGetLastError();
+        return set_error(LASSIE_ERR_NO_DEVICE, "no CUDA device");
+    }
+    // pack arenas: one copy of each distinct network
+    std::map<const lassie_model *, int64_t> model_off;
+    std::vector<int32_t> hint;
+    std::vector<double> hdbl;
+    b->desc.resize(n);
+    int64_t outpos = 0;
+    for (int q = 0; q < n; q++) {
+        const lassie_instance &I = inst[q];
+        const lassie_model *m = I.model;
+        auto it = model_off.find(m);
+        int64_t base;
+        if (it == model_off.end()) {
+            base = (int64_t)hint.size();
+            model_off[m] = base;
+            hint.insert(hint.end(), m->rxn_ptr.begin(), m->rxn_ptr.end());
+            hint.insert(hint.end(), m->rxn_ent.begin(), m->rxn_ent.end());
+            hint.insert(hint.end(), m->sp_ptr.begin(), m->sp_ptr.end());
+            hint.insert(hint.end(), m->sp_ent.begin(), m->sp_ent.end());
+        } else {
+            base = it->second;
+        }
+        InstDesc &D = b->desc[q];
+        D.n = m->N;
+        D.r = m->R;
+        D.nt = I.nt;
+        D.ncs = I.cs ? I.ncs : m->N;
+        D.nnz_a = (int32_t)m->rxn_ent.size();
+        D.nnz_h = (int32_t)m->sp_ent.size();
+        D.rxn_ptr = base;
+        D.rxn_ent = base + m->off_rent();
+        D.sp_ptr = base + m->off_sptr();
+        D.sp_ent = base + m->off_sent();
+        if (I.cs) {
+            D.cs = (int64_t)hint.size();
+            hint.insert(hint.end(), I.cs, I.cs + I.ncs);
+        } else {
+            D.cs = -1;
+        }
+        auto put = [&](const double *src, int64_t len) -> int64_t {
+            if (!src) return -1;
+            int64_t o = (int64_t)hdbl.size();
+            hdbl.insert(hdbl.end(), src, src + len);
+            return o;
+        };
+        D.k = put(I.k, m->R);
+        D.x0 = put(I.x0, m->N);
+        D.feed = put(I.feed, m->N);
+        D.atol = put(I.atol, m->N);
+        D.t = I.nt > 0 ? put(I.t, I.nt) : 0;
+        D.out = outpos;
+        outpos += (int64_t)I.nt * D.ncs;
+        D.rkf_step = o.rkf_step;
+        D.be_step = o.be_step;
+        D.newton_tol = o.newton_tol;
+        D.stiffness_tol = o.stiffness_tol;
+        D.newton_iter = o.newton_iter;
+        D.max_steps = o.max_steps;
+        b->nmax = std::max(b->nmax, m->N);
+        b->rmax = std::max(b->rmax, m->R);
+        b->amax = std::max(b->amax, (int32_t)m->rxn_ent.size());
+    }
+    if (hdbl.empty()) hdbl.push_back(0.0);
+    if (hint.empty()) hint.push_back(0);
+    b->n_int = (int64_t)hint.size();
+    b->n_dbl = (int64_t)hdbl.size();
+    b->n_out = std::max<int64_t>(outpos, 1);
+    // largest networks first: the dense LU cost grows as N^3
+    b->order.resize(n);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    std::stable_sort(b->order.begin(), b->order.end(),
+                     [&](int a, int c) { return b->desc[a].n > b->desc[c].n; });
+    b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, o.precision);
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
+    if (n > 0 && b->smem > max_optin - 1024) {
+        delete b;
+        return set_error(LASSIE_ERR_TOO_LARGE, "network needs " + std::to_string(b->smem) +
+                                                   " bytes of shared memory per CTA");
+    }
+    b->grid = std::max(1, std::min(n, b->sm_count));
+    const int lt = o.precision == LASSIE_PREC_FP64 ? 8 : 4;
+    const int64_t ws_stride =
+        ((int64_t)b->nmax * round_up4(b->nmax) * lt + 255) / 256 * 256;
+    if ((rc = b->d_int.grow(b->n_int * 4)) || (rc = b->d_dbl.grow(b->n_dbl * 8)) ||
+        (rc = b->d_out.grow(b->n_out * 8)) ||
+        (rc = b->d_desc.grow(std::max<size_t>(1, b->desc.size()) * sizeof(InstDesc))) ||
+        (rc = b->d_order.grow(std::max<size_t>(1, b->order.size()) * 4)) ||
+        (rc = b->d_res.grow(std::max<size_t>(1, b->desc.size()) * sizeof(InstResult))) ||
+        (rc = b->d_queue.grow(16)) || (rc = b->d_ws.grow((size_t)ws_stride * b->grid))) {
+        delete b;
+        return rc;
+    }
+    auto cpy = [&](DevBuf &d, const void *h, size_t bytes) {
+        return cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice);
+    };
+    if (cpy(b->d_int, hint.data(), hint.size() * 4) != cudaSuccess ||
+        cpy(b->d_dbl, hdbl.data(), hdbl.size() * 8) != cudaSuccess ||
+        (n > 0 && cpy(b->d_desc, b->desc.data(), b->desc.size() * sizeof(InstDesc)) != cudaSuccess) ||
+        (n > 0 && cpy(b->d_order, b->order.data(), b->order.size() * 4) != cudaSuccess) ||
+        cudaMemset(b->d_out.p, 0, b->n_out * 8) != cudaSuccess) {
+        delete b;
+        return set_error(LASSIE_ERR_CUDA, std::string("batch upload: ") +
+                                              cudaGetErrorString(cudaGetLastError()));
+    }
+    if (compat_configure(o.precision, b->smem) != cudaSuccess) {
+        delete b;
+        return set_error(LASSIE_ERR_CUDA, std::string("kernel configure: ") +
+                                              cudaGetErrorString(cudaGetLastError()));
+    }
+    LaunchParams &P = b->P;
+    P.inst = (const InstDesc *)b->d_desc.p;
+    P.n_inst = n;
+    P.order = (const int32_t *)b->d_order.p;
+    P.queue = (int32_t *)b->d_queue.p;
+    P.iarena = (const int32_t *)b->d_int.p;
+    P.darena = (const double *)b->d_dbl.p;
+    P.out = (double *)b->d_out.p;
+    P.res = (InstResult *)b->d_res.p;
+    P.workspace = (unsigned char *)b->d_ws.p;
+    P.ws_stride = ws_stride;
+    P.nmax = b->nmax;
+    P.rmax = b->rmax;
+    P.amax = b->amax;
+    P.precision = o.precision;
+    P.refine_max = o.refine_max;
+    P.deadline_ns = o.deadline_s > 0 ? (uint64_t)(o.deadline_s * 1e9) : 0;
+    *out = b;
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_batch_run(lassie_batch *b, void *stream) {
+    if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
+    if (b->n == 0) return LASSIE_OK;
+    b->stream = (cudaStream_t)stream;
+    CU(cudaMemsetAsync(b->d_queue.p, 0, 16, b->stream));
+    CU(compat_launch(b->P, b->grid, b->smem, b->stream));
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_batch_launches(const lassie_batch *b) { return (b && b->n > 0) ? 1 : 0; }
+
+extern "C" int lassie_batch_sync(lassie_batch *b) {
+    if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
+    CU(cudaStreamSynchronize(b->stream));
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_batch_read(lassie_batch *b, const lassie_instance *inst,
+                                 lassie_stats *stats) {
+    if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
+    if (b->n == 0) return LASSIE_OK;
+    std::vector<double> hout((size_t)b->n_out);
+    std::vector<InstResult> hres(b->n);
+    CU(cudaMemcpyAsync(hout.data(), b->d_out.p, hout.size() * 8, cudaMemcpyDeviceToHost,
+                       b->stream));
+    CU(cudaMemcpyAsync(hres.data(), b->d_res.p, hres.size() * sizeof(InstResult),
+                       cudaMemcpyDeviceToHost, b->stream));
+    CU(cudaStreamSynchronize(b->stream));
+    int first_bad = LASSIE_OK;
+    for (int q = 0; q < b->n; q++) {
+        const InstDesc &D = b->desc[q];
+        if (inst && inst[q].out)
+            std::memcpy(inst[q].out, hout.data() + D.out, sizeof(double) * (size_t)D.nt * D.ncs);
+        if (stats) std::memcpy(&stats[q], &hres[q], sizeof(lassie_stats));
+        if (hres[q].status != LASSIE_OK && first_bad == LASSIE_OK) first_bad = hres[q].status;
+    }
+    return first_bad;
+}
+
+extern "C" void lassie_batch_destroy(lassie_batch *b) { delete b; }
+
+extern "C" int lassie_solve_batch(const lassie_instance *inst, int32_t n, const lassie_opts *opts,
+                                  lassie_stats *stats) {
+    lassie_batch *b = nullptr;
+    int rc = lassie_batch_create(inst, n, opts, &b);
+    if (rc) return rc;
+    rc = lassie_batch_run(b, nullptr);
+    if (!rc) rc = lassie_batch_sync(b);
+    if (!rc) rc = lassie_batch_read(b, inst, stats);
+    lassie_batch_destroy(b);
+    return rc;
+}
+
+extern "C" int lassie_solve(const lassie_model *model, const double *k, const double *x0,
+                            const double *feed, const double *atol, const double *t, int32_t nt,
+                            const int32_t *cs, int32_t ncs, const lassie_opts *opts, double *out,
+                            lassie_stats *stats) {
+    lassie_instance I;
+    I.model = model;
+    I.k = k;
+    I.x0 = x0;
+    I.feed = feed;
+    I.atol = atol;
+    I.t = t;
+    I.nt = nt;
+    I.ncs = ncs;
+    I.cs = cs;
+    I.out = out;
+    return lassie_solve_batch(&I, 1, opts, stats);
+}
+
+// ---------------------------------------------------- single evaluations
+
+extern "C" int lassie_rhs_device(const lassie_model *cm, int32_t n_inst, const double *k,
+                                 const double *x, double *dx, void *stream) {
+    lassie_model *m = const_cast<lassie_model *>(cm);
+    if (!m || n_inst < 0 || (n_inst > 0 && (!k || !x || !dx)))
+        return set_error(LASSIE_ERR_ARGS, "rhs_device");
+    if (n_inst == 0) return LASSIE_OK;
+    const int32_t *d = nullptr;
+    int rc = model_device(m, &d);
+    if (rc) return rc;
+    int dev = 0, sms = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CU(rhs_batch_launch(n_inst, m->N, m->R, (int)m->rxn_ent.size(), d, d + m->off_rent(),
+                        d + m->off_sptr(), d + m->off_sent(), k, x, dx, sms,
+                        (cudaStream_t)stream));
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_rhs(const lassie_model *m, const double *k, const double *x, double *dx) {
+    if (!m || !k || !x || !dx) return set_error(LASSIE_ERR_ARGS, "rhs");
+    double *dk = nullptr, *dxv = nullptr, *ddx = nullptr;
+    CU(cudaMalloc(&dk, sizeof(double) * m->R));
+    CU(cudaMalloc(&dxv, sizeof(double) * m->N));
+    CU(cudaMalloc(&ddx, sizeof(double) * m->N));
+    int rc = LASSIE_OK;
+    if (cudaMemcpy(dk, k, sizeof(double) * m->R, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dxv, x, sizeof(double) * m->N, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = set_error(LASSIE_ERR_CUDA, "rhs upload");
+    if (!rc) rc = lassie_rhs_device(m, 1, dk, dxv, ddx, nullptr);
+    if (!rc && cudaMemcpy(dx, ddx, sizeof(double) * m->N, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = set_error(LASSIE_ERR_CUDA, "rhs download");
+    cudaFree(dk);
+    cudaFree(dxv);
+    cudaFree(ddx);
+    return rc;
+}
+
+extern "C" int lassie_newton_matrix(const lassie_model *cm, const double *k, const double *x,
+                                    double h, double *M) {
+    lassie_model *m = const_cast<lassie_model *>(cm);
+    if (!m || !k || !x || !M) return set_error(LASSIE_ERR_ARGS, "newton_matrix");
+    const int32_t *d = nullptr;
+    int rc = model_device(m, &d);
+    if (rc) return rc;
+    const size_t nn = (size_t)m->N * m->N;
+    double *dk = nullptr, *dxv = nullptr, *dM = nullptr;
+    CU(cudaMalloc(&dk, sizeof(double) * m->R));
+    CU(cudaMalloc(&dxv, sizeof(double) * m->N));
+    CU(cudaMalloc(&dM, sizeof(double) * nn));
+    if (cudaMemcpy(dk, k, sizeof(double) * m->R, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dxv, x, sizeof(double) * m->N, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = set_error(LASSIE_ERR_CUDA, "newton_matrix upload");
+    cudaError_t e = cudaSuccess;
+    if (!rc)
+        e = newton_matrix_launch(m->N, m->R, (int)m->rxn_ent.size(), d, d + m->off_rent(),
+                                 d + m->off_sptr(), d + m->off_sent(), dk, dxv, h, dM, nullptr);
+    if (!rc && e != cudaSuccess) rc = set_error(LASSIE_ERR_CUDA, cudaGetErrorString(e));
+    if (!rc && cudaMemcpy(M, dM, sizeof(double) * nn, cudaMemcpyDeviceToHost) != cudaSuccess)
+        rc = set_error(LASSIE_ERR_CUDA, "newton_matrix download");
+    cudaFree(dk);
+    cudaFree(dxv);
+    cudaFree(dM);
+    return rc;
+}
+
+extern "C" int lassie_lu_solve(int32_t n, const double *a, const double *b, double *x,
+                               int32_t precision) {
+    if (n <= 0 || !a || !b || !x ||
+        (precision != LASSIE_PREC_FP64 && precision != LASSIE_PREC_MIXED))
+        return set_error(LASSIE_ERR_ARGS, "lu_solve");
+    int dev = 0, max_optin = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (lu_solve_smem(n, precision) > max_optin - 1024)
+        return set_error(LASSIE_ERR_TOO_LARGE, "lu_solve: n too large for one CTA");
+    const int ld = round_up4(n);
+    const int lt = precision == LASSIE_PREC_FP64 ? 8 : 4;
+    std::vector<unsigned char> h((size_t)n * ld * lt, 0);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            const double v = a[(size_t)i * n + j];
+            if (lt == 8) ((double *)h.data())[(size_t)i * ld + j] = v;
+            else ((float *)h.data())[(size_t)i * ld + j] = (float)v;
+        }
+    void *dA = nullptr;
+    double *db = nullptr, *dx = nullptr;
+    int *dinfo = nullptr;
+    CU(cudaMalloc(&dA, h.size()));
+    CU(cudaMalloc(&db, sizeof(double) * n));
+    CU(cudaMalloc(&dx, sizeof(double) * n));
+    CU(cudaMalloc(&dinfo, sizeof(int)));
+    int rc = LASSIE_OK, info = 0;
+    if (cudaMemcpy(dA, h.data(), h.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(db, b, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+        rc = set_error(LASSIE_ERR_CUDA, "lu_solve upload");
+    cudaError_t e = cudaSuccess;
+    if (!rc) e = lu_solve_launch(n, dA, ld, db, dx, dinfo, precision, nullptr);
+    if (!rc && e != cudaSuccess) rc = set_error(LASSIE_ERR_CUDA, cudaGetErrorString(e));
+    if (!rc && (cudaMemcpy(&info, dinfo, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                cudaMemcpy(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost) != cudaSuccess))
+        rc = set_error(LASSIE_ERR_CUDA, "lu_solve download");
+    cudaFree(dA);
+    cudaFree(db);
+    cudaFree(dx);
+    cudaFree(dinfo);
+    if (!rc && info) return info;
+    return rc;
+}

@@ -1,0 +1,90 @@
+// Shared device/host definitions of the LASSIE GB300 engine.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lassie_gb300.h"
+
+namespace lassie {
+
+// One CTA integrates one instance at a time; 512 threads = 16 warps.
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+
+// Packed sparse entries: value = index * 256 + (int8 coefficient).
+__host__ __device__ __forceinline__ int ent_index(int e) { return e >> 8; }
+__host__ __device__ __forceinline__ int ent_coef(int e) {
+    return (int)(int8_t)(uint8_t)(e & 255);
+}
+__host__ __device__ __forceinline__ int make_ent(int index, int coef) {
+    return index * 256 + (coef & 255);
+}
+
+// Per-instance descriptor: offsets into the int / double / output arenas.
+struct InstDesc {
+    int32_t n, r, nt, ncs;
+    int32_t nnz_a, nnz_h, flags, pad;
+    int64_t rxn_ptr, rxn_ent, sp_ptr, sp_ent;  // int arena
+    int64_t cs;                                // int arena, -1 = all species
+    int64_t k, x0, feed, atol, t;              // double arena, feed/atol -1 = none
+    int64_t out;                               // output arena
+    double rkf_step, be_step, newton_tol, stiffness_tol;
+    int64_t newton_iter, max_steps;
+};
+
+// Per-instance result; layout identical to lassie_stats.
+struct InstResult {
+    int64_t outer_iters, rkf_accepts, rkf_retries, be_steps, newton_iters,
+        lu_factorisations, lu_failures, nan_reverts, refine_sweeps;
+    double t_final, dt_be_final;
+    int32_t status, pad;
+};
+static_assert(sizeof(InstResult) == sizeof(lassie_stats), "stats layout");
+
+struct LaunchParams {
+    const InstDesc *inst;
+    int32_t n_inst;
+    const int32_t *order;  // processing order (largest first)
+    int32_t *queue;        // work-queue counter, zeroed before launch
+    const int32_t *iarena;
+    const double *darena;
+    double *out;
+    InstResult *res;
+    unsigned char *workspace;  // per-CTA Newton matrix
+    int64_t ws_stride;         // bytes per CTA
+    int32_t nmax, rmax, amax;  // largest N, R, nnz_A in the batch
+    int32_t precision, refine_max;
+    uint64_t deadline_ns;      // per-launch wall-clock limit (ns), 0 = none
+};
+
+// Dynamic shared-memory layout of the integrator (bytes), identical on host
+// and device.  Vectors are FP64 N-vectors; the LU panel and U tile are in the
+// factorisation type (PB = panel width).
+struct SmemLayout {
+    int64_t vec, kk, pw, qr, rptr, perm, bvec, panel, utile, total;
+    __host__ __device__ static int64_t align(int64_t v) { return (v + 15) & ~int64_t(15); }
+    __host__ __device__ SmemLayout(int nmax, int rmax, int amax, int lt_bytes, int pb,
+                                   int tn) {
+        int64_t o = 0;
+        vec = o;   o = align(o + int64_t(10) * nmax * 8);
+        kk = o;    o = align(o + int64_t(rmax) * 8);
+        pw = o;    o = align(o + int64_t(amax > 0 ? amax : 1) * 8);
+        qr = o;    o = align(o + int64_t(rmax) * 8);
+        rptr = o;  o = align(o + int64_t(rmax + 1) * 4);
+        perm = o;  o = align(o + int64_t(nmax) * 4);
+        bvec = o;  o = align(o + int64_t(nmax) * lt_bytes);
+        panel = o; o = align(o + int64_t(nmax) * (pb + 1) * lt_bytes);
+        utile = o; o = align(o + int64_t(pb) * tn * lt_bytes);
+        total = o;
+    }
+};
+
+// Panel width and trailing tile width of the per-CTA LU, per element type.
+template <typename LT> struct LuShape;
+template <> struct LuShape<float> { static constexpr int PB = 32, TN = 128; };
+template <> struct LuShape<double> { static constexpr int PB = 16, TN = 128; };
+
+__host__ __device__ __forceinline__ int round_up4(int n) { return (n + 3) & ~3; }
+
+}  // namespace lassie

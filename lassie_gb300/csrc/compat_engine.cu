@@ -1,0 +1,991 @@
+// Persistent batched integrator with LASSIE's step control.
+//
+// One CTA of 512 threads integrates one instance at a time, taking instances
+// from a work queue (largest first), and runs the reference's whole time loop
+// (Simulation.cuh:632-925) on the device: RKF45 attempt, accept/reject,
+// stiffness switch, backward-Euler modified Newton with a dense LU of
+// M = I - h*J factored once per step.  State, stage vectors, rate constants
+// and per-reaction partial products live in shared memory; the Newton matrix
+// lives in a per-CTA global workspace (L2-resident at these sizes).
+//
+// Arithmetic contract (FP64 form, LT = double): every expression is
+// evaluated in the reference source's order without contraction (this file
+// is compiled with --fmad=false); the LU and triangular solves use explicit
+// fma in pivot order.  The CPU oracle follows the same contract, so the two
+// agree bit for bit.  Mixed form (LT = float): FP32 LU, FP64 iterative
+// refinement against the matrix-free FP64 product M*v = v - h*J(x)*v.
+#include <cmath>
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace lassie {
+
+// ------------------------------------------------------------ utilities
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// kernels.cuh:52-63 (myPow): repeated multiplication, 1 for ex <= 0.
+__device__ __forceinline__ double mypow(double b, int e) {
+    double p = 1.0;
+    while (e > 0) {
+        p = p * b;
+        --e;
+    }
+    return p;
+}
+
+__device__ __forceinline__ bool bad_value(double v) {
+    return isnan(v) || isinf(v) || v < 0;
+}
+
+template <typename T> __device__ __forceinline__ T lt_fma(T a, T b, T c);
+template <> __device__ __forceinline__ float lt_fma(float a, float b, float c) {
+    return __fmaf_rn(a, b, c);
+}
+template <> __device__ __forceinline__ double lt_fma(double a, double b, double c) {
+    return __fma_rn(a, b, c);
+}
+
+// Block sum of doubles in a fixed order (deterministic run to run).
+__device__ double block_sum(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int q = 0; q < kWarps; q++) s += red[q];
+    return s;
+}
+
+// Block max of non-negative doubles (NaN propagates).
+__device__ double block_max(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) {
+        double u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (isnan(u) || u > v) ? u : v;
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = red[0];
+    for (int q = 1; q < kWarps; q++) s = (isnan(red[q]) || red[q] > s) ? red[q] : s;
+    return s;
+}
+
+// Block minimum of non-NaN values (+inf if none).
+__device__ double block_min_nonnan(double v, double *red) {
+    for (int o = 16; o > 0; o >>= 1) {
+        double u = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (u < v) ? u : v;
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = red[0];
+    for (int q = 1; q < kWarps; q++) s = (red[q] < s) ? red[q] : s;
+    return s;
+}
+
+// --------------------------------------------------------------- model
+
+struct Net {
+    int n, r, nnz_a;
+    const int *__restrict__ rent;  // reactant entries (global)
+    const int *__restrict__ sptr;  // species row pointers (global)
+    const int *__restrict__ sent;  // species entries (global)
+    const int *rptr;               // reaction pointers (shared)
+    const double *kk;              // rate constants (shared)
+};
+
+// RHS phase 1: pw[q] = x_s^a for every reactant entry q.
+__device__ __forceinline__ void rhs_phase1(const Net &m, const double *x, double *pw) {
+    for (int q = threadIdx.x; q < m.nnz_a; q += kThreads) {
+        const int e = __ldg(m.rent + q);
+        pw[q] = mypow(x[ent_index(e)], ent_coef(e));
+    }
+}
+
+// RHS phase 2 for species i (kernels.cuh:5-50): over the reactions of its H
+// row in ascending order, ((s*k)*pw0)*pw1..., or s*k for zero order, summed
+// left to right from 0.  The reference's `temp = 0; temp += ...` differs from
+// this only in the sign of a zero, which cannot change the sum.
+__device__ __forceinline__ double rhs_species(const Net &m, int i, const double *pw) {
+    double acc = 0.0;
+    const int e0 = __ldg(m.sptr + i), e1 = __ldg(m.sptr + i + 1);
+    for (int e = e0; e < e1; e++) {
+        const int ent = __ldg(m.sent + e);
+        const int y = ent_index(ent);
+        double v = (double)ent_coef(ent) * m.kk[y];
+        const int b = m.rptr[y], en = m.rptr[y + 1];
+        for (int q = b; q < en; q++) v = v * pw[q];
+        acc = acc + v;
+    }
+    return acc;
+}
+
+// (J v)_i for the reference's Jacobian (kernels.cuh:205-271) at x, without
+// forming J: per reaction the directional derivative of k*prod(x), with the
+// other reactants multiplied in once each as createJac does, then the same
+// species sums as the RHS.  Phase 1 writes qr[R].
+__device__ void jv_phase1(const Net &m, const double *x, const double *v, double *qr) {
+    for (int y = threadIdx.x; y < m.r; y += kThreads) {
+        const int b = m.rptr[y], en = m.rptr[y + 1];
+        double q = 0.0;
+        for (int j = b; j < en; j++) {
+            const int ej = __ldg(m.rent + j);
+            const int g = ent_index(ej), a = ent_coef(ej);
+            double d;
+            if (a == 1) d = m.kk[y];
+            else if (a > 1) d = m.kk[y] * (double)a * mypow(x[g], a - 1);
+            else continue;
+            for (int jj = b; jj < en; jj++) {
+                const int o = ent_index(__ldg(m.rent + jj));
+                if (o != g) d = d * x[o];
+            }
+            q = fma(d, v[g], q);
+        }
+        qr[y] = q;
+    }
+}
+
+__device__ __forceinline__ double jv_species(const Net &m, int i, const double *qr) {
+    double acc = 0.0;
+    const int e0 = __ldg(m.sptr + i), e1 = __ldg(m.sptr + i + 1);
+    for (int e = e0; e < e1; e++) {
+        const int ent = __ldg(m.sent + e);
+        acc = fma((double)ent_coef(ent), qr[ent_index(ent)], acc);
+    }
+    return acc;
+}
+
+// M = I - h*J(x) into M (row-major, leading dimension ld), J with the
+// semantics of createJac + aggiorna_Jacobiano1 (kernels.cuh:205-271,393-402).
+// Entry (i,g) accumulates, over the reactions of H row i in ascending order,
+// temp = s*k [*a*x_g^(a-1)] * (each other reactant once).
+template <typename LT>
+__device__ void assemble_newton_matrix(const Net &m, const double *x, double h, LT *M,
+                                       int ld) {
+    const int N = m.n;
+    const int64_t total = (int64_t)N * ld;
+    for (int64_t idx = threadIdx.x; idx < total; idx += kThreads) {
+        const int row = (int)(idx / ld), col = (int)(idx - (int64_t)row * ld);
+        M[idx] = (row == col) ? LT(1) : LT(0);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < N; i += kThreads) {
+        const int e0 = __ldg(m.sptr + i), e1 = __ldg(m.sptr + i + 1);
+        for (int e = e0; e < e1; e++) {
+            const int y = ent_index(__ldg(m.sent + e));
+            const int b = m.rptr[y], en = m.rptr[y + 1];
+            for (int q = b; q < en; q++) {
+                const int g = ent_index(__ldg(m.rent + q));
+                // skip columns already produced by an earlier reaction of row i
+                bool seen = false;
+                for (int ep = e0; ep < e && !seen; ep++) {
+                    const int yp = ent_index(__ldg(m.sent + ep));
+                    for (int qp = m.rptr[yp]; qp < m.rptr[yp + 1]; qp++)
+                        if (ent_index(__ldg(m.rent + qp)) == g) { seen = true; break; }
+                }
+                if (seen) continue;
+                double J = 0.0;
+                for (int e2 = e; e2 < e1; e2++) {
+                    const int ent2 = __ldg(m.sent + e2);
+                    const int y2 = ent_index(ent2), s2 = ent_coef(ent2);
+                    const int b2 = m.rptr[y2], en2 = m.rptr[y2 + 1];
+                    int a = 0;
+                    bool has = false;
+                    for (int q2 = b2; q2 < en2; q2++) {
+                        const int ee = __ldg(m.rent + q2);
+                        if (ent_index(ee) == g) { a = ent_coef(ee); has = true; break; }
+                    }
+                    if (!has) continue;
+                    double temp = 0.0;
+                    if (a == 1) temp = temp + (double)s2 * m.kk[y2];
+                    else if (a > 1)
+                        temp = temp + (double)s2 * m.kk[y2] * (double)a * mypow(x[g], a - 1);
+                    else continue;
+                    for (int q2 = b2; q2 < en2; q2++) {
+                        const int o = ent_index(__ldg(m.rent + q2));
+                        if (o != g) temp = temp * x[o];
+                    }
+                    J = J + temp;
+                }
+                const double I = (i == g) ? 1.0 : 0.0;
+                M[(int64_t)i * ld + g] = (LT)(I - h * J);
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------ LU
+
+// Arg-max of |v| with the oracle's tie and NaN rules, combined over lanes.
+struct Piv {
+    double v;
+    int i;
+};
+__device__ __forceinline__ Piv piv_better(Piv a, Piv b) {
+    // larger |value| wins, ties to the smaller index; NaN values never win
+    if (b.v > a.v || (b.v == a.v && b.i < a.i)) return b;
+    return a;
+}
+
+// In-place blocked right-looking LU with partial pivoting on M (row-major,
+// leading dimension ld).  Every element receives a = fma(-l, u, a) once per
+// pivot in pivot order, as in the unblocked algorithm, so the factors equal
+// the oracle's bit for bit.  perm[i] = source row of row i of P*A.
+// Returns 0, or j+1 if the pivot of column j is exactly zero (uniform).
+template <typename LT>
+__device__ int lu_factor(LT *M, int ld, int N, int *perm, LT *panel, LT *utile,
+                         double *red, int *ired) {
+    constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN, PS = PB + 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < N; i += kThreads) perm[i] = i;
+    __syncthreads();
+    int fail = 0;
+    for (int j0 = 0; j0 < N; j0 += PB) {
+        const int pb = min(PB, N - j0);
+        const int m = N - j0;
+        // load panel rows j0..N-1, columns j0..j0+pb-1
+        for (int idx = tid; idx < m * PB; idx += kThreads) {
+            const int r = idx / PB, c = idx - r * PB;
+            panel[r * PS + c] = (c < pb) ? M[(int64_t)(j0 + r) * ld + j0 + c] : LT(0);
+        }
+        __syncthreads();
+        // arg-max of column 0 of the panel
+        Piv best{-1.0, 1 << 30};
+        for (int r = tid; r < m; r += kThreads) {
+            double v = fabs((double)panel[r * PS]);
+            if (!isnan(v)) best = piv_better(best, Piv{v, r});
+        }
+        for (int jj = 0; jj < pb; jj++) {
+            // combine partial arg-max for column jj
+            for (int o = 16; o > 0; o >>= 1) {
+                Piv other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                          __shfl_xor_sync(0xffffffffu, best.i, o)};
+                best = piv_better(best, other);
+            }
+            if (lane == 0) {
+                red[warp] = best.v;
+                ired[warp] = best.i;
+            }
+            __syncthreads();
+            Piv all{red[0], ired[0]};
+            for (int q = 1; q < kWarps; q++) all = piv_better(all, Piv{red[q], ired[q]});
+            int p = all.i;
+            // a NaN in the diagonal position keeps its own row (oracle rule)
+            if (isnan((double)panel[jj * PS + jj]) || p >= m) p = jj;
+            const LT pv = panel[p * PS + jj];
+            if (pv == LT(0)) {
+                fail = j0 + jj + 1;
+                break;
+            }
+            __syncthreads();  // everyone has read red/ired and the pivot
+            if (p != jj) {
+                for (int c = tid; c < PB; c += kThreads) {
+                    LT tmp = panel[jj * PS + c];
+                    panel[jj * PS + c] = panel[p * PS + c];
+                    panel[p * PS + c] = tmp;
+                }
+                if (tid == 0) {
+                    int tmp = perm[j0 + jj];
+                    perm[j0 + jj] = perm[j0 + p];
+                    perm[j0 + p] = tmp;
+                }
+            }
+            if (tid == 0) ired[kWarps] = p;  // pivot row for the column swaps
+            if (tid == 0) ired[kWarps + 1 + jj] = p;
+            __syncthreads();
+            // eliminate below the pivot; fused arg-max for column jj+1
+            const LT d = panel[jj * PS + jj];
+            best = Piv{-1.0, 1 << 30};
+            for (int r = jj + 1 + tid; r < m; r += kThreads) {
+                const LT l = panel[r * PS + jj] / d;
+                panel[r * PS + jj] = l;
+                for (int c = jj + 1; c < pb; c++)
+                    panel[r * PS + c] = lt_fma(-l, panel[jj * PS + c], panel[r * PS + c]);
+                if (jj + 1 < pb) {
+                    double v = fabs((double)panel[r * PS + jj + 1]);
+                    if (!isnan(v)) best = piv_better(best, Piv{v, r});
+                }
+            }
+            __syncthreads();
+        }
+        if (fail) break;
+        // write the panel back
+        for (int idx = tid; idx < m * PB; idx += kThreads) {
+            const int r = idx / PB, c = idx - r * PB;
+            if (c < pb) M[(int64_t)(j0 + r) * ld + j0 + c] = panel[r * PS + c];
+        }
+        // columns outside the panel: row swaps in pivot order, then the
+        // unit-lower triangular solve for the U12 block rows.
+        const int* pivrows = ired + kWarps + 1;
+        for (int c = tid; c < N; c += kThreads) {
+            if (c >= j0 && c < j0 + pb) continue;
+            for (int jj = 0; jj < pb; jj++) {
+                const int p = pivrows[jj];
+                if (p != jj) {
+                    LT *a = M + (int64_t)(j0 + jj) * ld + c;
+                    LT *b = M + (int64_t)(j0 + p) * ld + c;
+                    LT tmp = *a;
+                    *a = *b;
+                    *b = tmp;
+                }
+            }
+            if (c >= j0 + pb) {
+                LT v[PB];
+#pragma unroll
+                for (int r = 0; r < PB; r++)
+                    v[r] = (r < pb) ? M[(int64_t)(j0 + r) * ld + c] : LT(0);
+#pragma unroll
+                for (int r = 1; r < PB; r++) {
+                    LT acc = v[r];
+#pragma unroll
+                    for (int q = 0; q < r; q++) acc = lt_fma(-panel[r * PS + q], v[q], acc);
+                    v[r] = acc;
+                }
+#pragma unroll
+                for (int r = 1; r < PB; r++)
+                    if (r < pb) M[(int64_t)(j0 + r) * ld + c] = v[r];
+            }
+        }
+        __syncthreads();
+        // trailing update A22 -= L21 * U12, tiles of 64 x TN
+        const int c0 = j0 + pb;
+        const int m2 = N - c0;
+        if (m2 > 0) {
+            const int tx = tid & 31, ty = tid >> 5;
+            for (int tn0 = 0; tn0 < m2; tn0 += TN) {
+                for (int idx = tid; idx < pb * TN; idx += kThreads) {
+                    const int r = idx / TN, c = idx - r * TN;
+                    const int col = c0 + tn0 + c;
+                    utile[idx] = (col < N) ? M[(int64_t)(j0 + r) * ld + col] : LT(0);
+                }
+                __syncthreads();
+                for (int tm0 = 0; tm0 < m2; tm0 += 64) {
+                    const int rowb = c0 + tm0 + ty * 4;
+                    const int colb = c0 + tn0 + tx * 4;
+                    LT acc[4][4];
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+#pragma unroll
+                        for (int b = 0; b < 4; b++) {
+                            const int row = rowb + a, col = colb + b;
+                            acc[a][b] = (row < N && col < N) ? M[(int64_t)row * ld + col] : LT(0);
+                        }
+#pragma unroll 4
+                    for (int q = 0; q < PB; q++) {
+                        if (q < pb) {
+                            LT lv[4], uv[4];
+#pragma unroll
+                            for (int a = 0; a < 4; a++) {
+                                const int pr = rowb + a - j0;
+                                lv[a] = (pr < m) ? panel[pr * PS + q] : LT(0);
+                            }
+#pragma unroll
+                            for (int b = 0; b < 4; b++) uv[b] = utile[q * TN + tx * 4 + b];
+#pragma unroll
+                            for (int a = 0; a < 4; a++)
+#pragma unroll
+                                for (int b = 0; b < 4; b++)
+                                    acc[a][b] = lt_fma(-lv[a], uv[b], acc[a][b]);
+                        }
+                    }
+#pragma unroll
+                    for (int a = 0; a < 4; a++)
+#pragma unroll
+                        for (int b = 0; b < 4; b++) {
+                            const int row = rowb + a, col = colb + b;
+                            if (row < N && col < N) M[(int64_t)row * ld + col] = acc[a][b];
+                        }
+                }
+                __syncthreads();
+            }
+        }
+    }
+    __syncthreads();
+    return fail;
+}
+
+// Solve (P A) x = P b with the factors in M; b is in bvec (already permuted),
+// overwritten by x.  Forward: ascending accumulation; backward: descending
+// accumulation then one division (the oracle's order).
+template <typename LT>
+__device__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // forward substitution, unit lower
+    for (int r0 = 0; r0 < N; r0 += 32) {
+        const int nb = min(32, N - r0);
+        if (warp == 0) {
+            LT v = (lane < nb) ? bvec[r0 + lane] : LT(0);
+            LT row[32];
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                row[q] = (lane < nb && q < lane) ? M[(int64_t)(r0 + lane) * ld + r0 + q] : LT(0);
+#pragma unroll
+            for (int q = 0; q < 32; q++) {
+                const LT bq = __shfl_sync(0xffffffffu, v, q);
+                if (q < nb && lane > q && lane < nb) v = lt_fma(-row[q], bq, v);
+            }
+            if (lane < nb) bvec[r0 + lane] = v;
+        }
+        __syncthreads();
+        for (int i = r0 + nb + tid; i < N; i += kThreads) {
+            LT acc = bvec[i];
+            const LT *ri = M + (int64_t)i * ld + r0;
+            for (int q = 0; q < nb; q++) acc = lt_fma(-ri[q], bvec[r0 + q], acc);
+            bvec[i] = acc;
+        }
+        __syncthreads();
+    }
+    // backward substitution, upper
+    const int nblk = (N + 31) / 32;
+    for (int bk = nblk - 1; bk >= 0; bk--) {
+        const int r0 = bk * 32;
+        const int nb = min(32, N - r0);
+        if (warp == 0) {
+            LT v = (lane < nb) ? bvec[r0 + lane] : LT(0);
+            LT row[32];
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                row[q] = (lane < nb && q >= lane && q < nb) ? M[(int64_t)(r0 + lane) * ld + r0 + q]
+                                                            : LT(1);
+#pragma unroll
+            for (int q = 31; q >= 0; q--) {
+                if (q < nb) {
+                    LT xq = v / row[q];  // meaningful on lane q only
+                    xq = __shfl_sync(0xffffffffu, xq, q);
+                    if (lane == q) v = xq;
+                    else if (lane < q) v = lt_fma(-row[q], xq, v);
+                }
+            }
+            if (lane < nb) bvec[r0 + lane] = v;
+        }
+        __syncthreads();
+        for (int i = tid; i < r0; i += kThreads) {
+            LT acc = bvec[i];
+            const LT *ri = M + (int64_t)i * ld + r0;
+            for (int q = nb - 1; q >= 0; q--) acc = lt_fma(-ri[q], bvec[r0 + q], acc);
+            bvec[i] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// ----------------------------------------------------------- integrator
+
+struct Vecs {
+    double *y1, *u, *k1, *k2, *k3, *k4, *k5, *k6, *fd, *tol;
+};
+
+template <typename LT>
+__device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, double *red,
+                          int *ired, uint64_t deadline) {
+    constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN;
+    const InstDesc D = P.inst[id];
+    const int N = D.n, R = D.r, tid = threadIdx.x;
+    const SmemLayout L(P.nmax, P.rmax, P.amax, (int)sizeof(LT), PB, TN);
+    double *vbase = reinterpret_cast<double *>(smem + L.vec);
+    Vecs V;
+    V.y1 = vbase;
+    V.u = vbase + 1 * P.nmax;
+    V.k1 = vbase + 2 * P.nmax;
+    V.k2 = vbase + 3 * P.nmax;
+    V.k3 = vbase + 4 * P.nmax;
+    V.k4 = vbase + 5 * P.nmax;
+    V.k5 = vbase + 6 * P.nmax;
+    V.k6 = vbase + 7 * P.nmax;
+    V.fd = vbase + 8 * P.nmax;
+    V.tol = vbase + 9 * P.nmax;
+    double *kk = reinterpret_cast<double *>(smem + L.kk);
+    double *pw = reinterpret_cast<double *>(smem + L.pw);
+    double *qr = reinterpret_cast<double *>(smem + L.qr);
+    int *rptr = reinterpret_cast<int *>(smem + L.rptr);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    LT *bvec = reinterpret_cast<LT *>(smem + L.bvec);
+    LT *panel = reinterpret_cast<LT *>(smem + L.panel);
+    LT *utile = reinterpret_cast<LT *>(smem + L.utile);
+
+    const int *ia = P.iarena;
+    const double *da = P.darena;
+    Net m;
+    m.n = N;
+    m.r = R;
+    m.nnz_a = D.nnz_a;
+    m.rent = ia + D.rxn_ent;
+    m.sptr = ia + D.sp_ptr;
+    m.sent = ia + D.sp_ent;
+    m.rptr = rptr;
+    m.kk = kk;
+
+    for (int s = tid; s < N; s += kThreads) {
+        V.y1[s] = da[D.x0 + s];
+        V.u[s] = 0.0;  // the reference's stage vector is never written for fed species
+        V.fd[s] = D.feed >= 0 ? da[D.feed + s] : 0.0;
+        V.tol[s] = D.atol >= 0 ? da[D.atol + s] : 1e-12;
+    }
+    for (int j = tid; j < R; j += kThreads) kk[j] = da[D.k + j];
+    for (int j = tid; j <= R; j += kThreads) rptr[j] = ia[D.rxn_ptr + j];
+    __syncthreads();
+
+    const double *tv = da + D.t;
+    const int *cs = D.cs >= 0 ? ia + D.cs : nullptr;
+    double *out = P.out + D.out;
+    LT *M = reinterpret_cast<LT *>(P.workspace + (int64_t)blockIdx.x * P.ws_stride);
+    const int ld = round_up4(N);
+    const bool mixed = P.precision == LASSIE_PREC_MIXED;
+    const int refine_max = P.refine_max > 0 ? P.refine_max : 8;
+
+    InstResult st{};
+    int status = LASSIE_OK;
+    int i = 0;
+    double t1 = D.nt > 0 ? tv[0] : 0.0;
+    double t = 0.0;
+    double dt = D.rkf_step;
+    double newDt = D.be_step;
+    const int nt = D.nt, ncs = D.ncs;
+
+    while (i < nt) {
+        if (D.max_steps > 0 && st.outer_iters >= D.max_steps) {
+            status = LASSIE_ERR_MAX_STEPS;
+            break;
+        }
+        if (deadline && (st.outer_iters & 63) == 0) {
+            if (tid == 0) ired[0] = global_ns() > deadline;
+            __syncthreads();
+            const int expired = ired[0];
+            __syncthreads();
+            if (expired) {
+                status = LASSIE_ERR_DEADLINE;
+                break;
+            }
+        }
+        st.outer_iters++;
+        // sampling (Simulation.cuh:674-690)
+        if (fabs(t1 - t) < 1e-5) {
+            for (int j = tid; j < ncs; j += kThreads)
+                out[(int64_t)i * ncs + j] = V.y1[cs ? cs[j] : j];
+            i++;
+            if (i >= nt) break;
+            t1 = tv[i];
+        }
+        // ---- RKF45 attempt (Simulation.cuh:692-735, kernels.cuh:68-199)
+        rhs_phase1(m, V.y1, pw);
+        __syncthreads();
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            if (V.fd[s] != 0.0) V.k1[s] = V.fd[s];
+            else {
+                V.k1[s] = f * dt;
+                V.u[s] = V.y1[s] + V.k1[s] / 4.0;
+            }
+        }
+        __syncthreads();
+        rhs_phase1(m, V.u, pw);
+        __syncthreads();
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            if (V.fd[s] != 0.0) V.k2[s] = V.fd[s];
+            else {
+                V.k2[s] = f * dt;
+                V.u[s] = V.y1[s] + (3.0 * V.k1[s]) / 32.0 + (9.0 * V.k2[s]) / 32.0;
+            }
+        }
+        __syncthreads();
+        rhs_phase1(m, V.u, pw);
+        __syncthreads();
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            if (V.fd[s] != 0.0) V.k3[s] = V.fd[s];
+            else {
+                V.k3[s] = f * dt;
+                V.u[s] = V.y1[s] + (1932.0 * V.k1[s]) / 2197.0 - (7200.0 * V.k2[s]) / 2197.0 +
+                         (7296.0 * V.k3[s]) / 2197.0;
+            }
+        }
+        __syncthreads();
+        rhs_phase1(m, V.u, pw);
+        __syncthreads();
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            if (V.fd[s] != 0.0) V.k4[s] = V.fd[s];
+            else {
+                V.k4[s] = f * dt;
+                V.u[s] = V.y1[s] + (439.0 * V.k1[s]) / 216.0 - (8.0 * V.k2[s]) +
+                         (3680.0 * V.k3[s]) / 513.0 - (845.0 * V.k4[s]) / 4104.0;
+            }
+        }
+        __syncthreads();
+        rhs_phase1(m, V.u, pw);
+        __syncthreads();
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            if (V.fd[s] != 0.0) V.k5[s] = V.fd[s];
+            else {
+                V.k5[s] = f * dt;
+                V.u[s] = V.y1[s] - (8.0 * V.k1[s]) / 27.0 + (2.0 * V.k2[s]) -
+                         (3544.0 * V.k3[s]) / 2565.0 + (1859.0 * V.k4[s]) / 4104.0 -
+                         (11.0 * V.k5[s]) / 40.0;
+            }
+        }
+        __syncthreads();
+        rhs_phase1(m, V.u, pw);
+        __syncthreads();
+        bool ok = true;
+        double dloc = INFINITY;
+        bool d0nan = false;
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            const double fdv = V.fd[s];
+            double k6 = (fdv != 0.0) ? fdv : f * dt;
+            V.k6[s] = k6;
+            double w1, w2;
+            if (fdv != 0.0) {
+                w1 = fdv;
+                w2 = fdv;
+            } else {
+                w1 = V.y1[s] + (25.0 * V.k1[s]) / 216.0 + (1408.0 * V.k3[s]) / 2565.0 +
+                     (2197.0 * V.k4[s]) / 4104.0 - V.k5[s] / 5.0;
+                w2 = V.y1[s] + (16.0 * V.k1[s]) / 135.0 + (6656.0 * V.k3[s]) / 12825.0 +
+                     (28561.0 * V.k4[s]) / 56430.0 - (9.0 * V.k5[s] / 50.0) +
+                     (2.0 * k6) / 55.0;
+            }
+            V.k1[s] = w1;  // the 4th-order solution, kept on accept (u untouched)
+            const double Rv = fabs(w1 - w2) / dt;
+            const double delta = 0.84 * sqrt(sqrt(V.tol[s] / Rv));
+            if (!(Rv <= V.tol[s] && !isnan(Rv) && !isinf(Rv) && w1 > 0)) ok = false;
+            if (s == 0) d0nan = isnan(delta);
+            if (delta < dloc) dloc = delta;
+        }
+        const int all_ok = __syncthreads_and(ok);
+        const int dnan = __syncthreads_or(d0nan);
+        double dmin = block_min_nonnan(dloc, red);
+        if (dnan) dmin = NAN;  // thrust::min_element keeps a leading NaN
+        if (all_ok) {
+            // accept (Simulation.cuh:742-768)
+            for (int s = tid; s < N; s += kThreads) V.y1[s] = V.k1[s];
+            __syncthreads();
+            const double d_temp = dt * dmin;
+            if ((t + d_temp) > t1) dt = fabs(t1 - t);
+            else dt = d_temp;
+            t = t + dt;
+            st.rkf_accepts++;
+            continue;
+        }
+        // reject (Simulation.cuh:769-921)
+        const double dt_old = dt;
+        dt = dt * dmin;
+        if (!((dt < D.stiffness_tol) | isnan(dt) | isinf(dt) | (fabs(dt_old - dt) < 1e-3))) {
+            st.rkf_retries++;
+            continue;
+        }
+        dt = newDt;
+        if ((t + dt) > t1) dt = fabs(t1 - t);
+        double *yv = V.k2, *xr = V.k3, *dx = V.k4, *xf = V.k5, *res = V.k6;
+        for (int s = tid; s < N; s += kThreads) yv[s] = V.y1[s];
+        __syncthreads();
+        int64_t itN = 0;
+        double errN = 1000;
+        bool luFail = false;
+        st.be_steps++;
+        while ((itN < D.newton_iter) & (errN > D.newton_tol)) {
+            // x = f(y_v); x = -(y_v - y1 - h*x)   (kernels.cuh:289-300)
+            rhs_phase1(m, yv, pw);
+            __syncthreads();
+            for (int s = tid; s < N; s += kThreads) {
+                const double f = rhs_species(m, s, pw);
+                xr[s] = -(yv[s] - V.y1[s] - dt * f);
+                if (itN == 0) xf[s] = yv[s];
+            }
+            __syncthreads();
+            if (itN == 0) {
+                assemble_newton_matrix<LT>(m, yv, dt, M, ld);
+                st.lu_factorisations++;
+                if (lu_factor<LT>(M, ld, N, perm, panel, utile, red, ired) != 0) luFail = true;
+            }
+            if (luFail) {
+                // Simulation.cuh:869-875, kernels.cuh:512-521
+                for (int s = tid; s < N; s += kThreads)
+                    if (bad_value(yv[s])) yv[s] = V.y1[s];
+                __syncthreads();
+                newDt = dt * 0.1;
+                st.lu_failures++;
+                break;
+            }
+            if (!mixed) {
+                for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)xr[perm[s]];
+                __syncthreads();
+                lu_solve<LT>(M, ld, N, bvec);
+                for (int s = tid; s < N; s += kThreads) dx[s] = (double)bvec[s];
+                __syncthreads();
+            } else {
+                // FP32 solves, FP64 residuals: dx converges to the FP64 solve
+                for (int s = tid; s < N; s += kThreads) {
+                    dx[s] = 0.0;
+                    res[s] = xr[s];
+                }
+                __syncthreads();
+                double prev = INFINITY;
+                for (int sweep = 0; sweep < refine_max; sweep++) {
+                    for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)res[perm[s]];
+                    __syncthreads();
+                    lu_solve<LT>(M, ld, N, bvec);
+                    double cmax = 0.0, xmax = 0.0;
+                    for (int s = tid; s < N; s += kThreads) {
+                        const double c = (double)bvec[s];
+                        const double nx = dx[s] + c;
+                        dx[s] = nx;
+                        cmax = fmax(cmax, fabs(c));
+                        xmax = fmax(xmax, fabs(nx));
+                    }
+                    st.refine_sweeps++;
+                    cmax = block_max(cmax, red);
+                    xmax = block_max(xmax, red);
+                    if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) ||
+                        sweep + 1 == refine_max)
+                        break;
+                    prev = cmax;
+                    // res = xr - (dx - h*J(xf)*dx)
+                    jv_phase1(m, xf, dx, qr);
+                    __syncthreads();
+                    for (int s = tid; s < N; s += kThreads) {
+                        const double jv = jv_species(m, s, qr);
+                        res[s] = xr[s] - (dx[s] - dt * jv);
+                    }
+                    __syncthreads();
+                }
+            }
+            // y_v += dx; dx = y_v - y_v_old (kernels.cuh:462-477); ||dx|| with
+            // FP32-rounded squares (Simulation.cuh:58-64, 883-890)
+            double sq = 0.0;
+            for (int s = tid; s < N; s += kThreads) {
+                const double old = yv[s];
+                const double nv = (V.fd[s] == 0) ? yv[s] + dx[s] : V.fd[s];
+                yv[s] = nv;
+                const double d = nv - old;
+                dx[s] = d;
+                sq = sq + (double)(float)(d * d);
+            }
+            errN = sqrt(block_sum(sq, red));
+            itN = itN + 1;
+            st.newton_iters++;
+        }
+        if (!luFail) {
+            // Simulation.cuh:894-909
+            bool anybad = false;
+            for (int s = tid; s < N; s += kThreads) anybad |= bad_value(yv[s]);
+            if (__syncthreads_or(anybad)) {
+                for (int s = tid; s < N; s += kThreads)
+                    if (bad_value(yv[s])) yv[s] = V.y1[s];
+                newDt = dt * 0.1;
+                st.nan_reverts++;
+            }
+        }
+        __syncthreads();
+        double *tmp = V.y1;
+        V.y1 = V.k2;
+        V.k2 = tmp;
+        t = t + dt;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        st.t_final = t;
+        st.dt_be_final = newDt;
+        st.status = status;
+        P.res[id] = st;
+    }
+    __syncthreads();
+}
+
+template <typename LT>
+__global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[kWarps + 1];
+    __shared__ int ired[kWarps + 2 + LuShape<LT>::PB];
+    __shared__ int next;
+    __shared__ uint64_t start;
+    if (threadIdx.x == 0) start = global_ns();
+    __syncthreads();
+    const uint64_t deadline = P.deadline_ns ? start + P.deadline_ns : 0;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(P.queue, 1);
+        __syncthreads();
+        const int q = next;
+        __syncthreads();
+        if (q >= P.n_inst) break;
+        integrate<LT>(P, P.order[q], smem, red, ired, deadline);
+    }
+}
+
+// ------------------------------------------------------------- launch
+
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int precision) {
+    if (precision == LASSIE_PREC_FP64)
+        return SmemLayout(nmax, rmax, amax, 8, LuShape<double>::PB, LuShape<double>::TN).total;
+    return SmemLayout(nmax, rmax, amax, 4, LuShape<float>::PB, LuShape<float>::TN).total;
+}
+
+cudaError_t compat_configure(int precision, int64_t smem) {
+    if (precision == LASSIE_PREC_FP64)
+        return cudaFuncSetAttribute(compat_kernel<double>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaFuncSetAttribute(compat_kernel<float>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream) {
+    if (P.precision == LASSIE_PREC_FP64)
+        compat_kernel<double><<<grid, kThreads, smem, stream>>>(P);
+    else
+        compat_kernel<float><<<grid, kThreads, smem, stream>>>(P);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------ single-evaluation kernels
+
+// dx = f(x) for a batch of parameterisations of one network; one CTA per
+// instance chunk, x/k staged through shared memory with coalesced loads.
+__global__ void __launch_bounds__(kThreads) rhs_batch_kernel(
+    int n_inst, int N, int R, int nnz_a, const int *__restrict__ rptr_g,
+    const int *__restrict__ rent, const int *__restrict__ sptr, const int *__restrict__ sent,
+    const double *__restrict__ k, const double *__restrict__ x, double *__restrict__ dx) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *xs = reinterpret_cast<double *>(smem);
+    double *kk = xs + N;
+    double *pw = kk + R;
+    int *rptr = reinterpret_cast<int *>(pw + (nnz_a > 0 ? nnz_a : 1));
+    for (int j = threadIdx.x; j <= R; j += kThreads) rptr[j] = rptr_g[j];
+    Net m;
+    m.n = N;
+    m.r = R;
+    m.nnz_a = nnz_a;
+    m.rent = rent;
+    m.sptr = sptr;
+    m.sent = sent;
+    m.rptr = rptr;
+    m.kk = kk;
+    for (int b = blockIdx.x; b < n_inst; b += gridDim.x) {
+        __syncthreads();
+        const double *xb = x + (int64_t)b * N;
+        const double *kb = k + (int64_t)b * R;
+        for (int s = threadIdx.x; s < N; s += kThreads) xs[s] = xb[s];
+        for (int j = threadIdx.x; j < R; j += kThreads) kk[j] = kb[j];
+        __syncthreads();
+        rhs_phase1(m, xs, pw);
+        __syncthreads();
+        double *db = dx + (int64_t)b * N;
+        for (int s = threadIdx.x; s < N; s += kThreads) db[s] = rhs_species(m, s, pw);
+    }
+}
+
+cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, const int *rptr,
+                             const int *rent, const int *sptr, const int *sent,
+                             const double *k, const double *x, double *dx, int sm_count,
+                             cudaStream_t stream) {
+    const int64_t smem = int64_t(N + R + (nnz_a > 0 ? nnz_a : 1)) * 8 + int64_t(R + 1) * 4;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(rhs_batch_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = n_inst < sm_count * 4 ? n_inst : sm_count * 4;
+    rhs_batch_kernel<<<grid, kThreads, smem, stream>>>(n_inst, N, R, nnz_a, rptr, rent, sptr,
+                                                       sent, k, x, dx);
+    return cudaGetLastError();
+}
+
+// M = I - h*J(x) in FP64 for one instance (one CTA).
+__global__ void __launch_bounds__(kThreads) newton_matrix_kernel(
+    int N, int R, int nnz_a, const int *__restrict__ rptr_g, const int *__restrict__ rent,
+    const int *__restrict__ sptr, const int *__restrict__ sent, const double *__restrict__ k,
+    const double *__restrict__ x, double h, double *M) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *xs = reinterpret_cast<double *>(smem);
+    double *kk = xs + N;
+    int *rptr = reinterpret_cast<int *>(kk + R);
+    for (int j = threadIdx.x; j <= R; j += kThreads) rptr[j] = rptr_g[j];
+    for (int s = threadIdx.x; s < N; s += kThreads) xs[s] = x[s];
+    for (int j = threadIdx.x; j < R; j += kThreads) kk[j] = k[j];
+    __syncthreads();
+    Net m;
+    m.n = N;
+    m.r = R;
+    m.nnz_a = nnz_a;
+    m.rent = rent;
+    m.sptr = sptr;
+    m.sent = sent;
+    m.rptr = rptr;
+    m.kk = kk;
+    assemble_newton_matrix<double>(m, xs, h, M, N);
+}
+
+cudaError_t newton_matrix_launch(int N, int R, int nnz_a, const int *rptr, const int *rent,
+                                 const int *sptr, const int *sent, const double *k,
+                                 const double *x, double h, double *M, cudaStream_t stream) {
+    const int64_t smem = int64_t(N + R) * 8 + int64_t(R + 1) * 4;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(newton_matrix_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    newton_matrix_kernel<<<1, kThreads, smem, stream>>>(N, R, nnz_a, rptr, rent, sptr, sent, k,
+                                                       x, h, M);
+    return cudaGetLastError();
+}
+
+// Factor + solve one dense system with the engine's LU (tests).
+template <typename LT>
+__global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int ld,
+                                                               const double *b, double *x,
+                                                               int *info) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int PB = LuShape<LT>::PB;
+    __shared__ double red[kWarps + 1];
+    __shared__ int ired[kWarps + 2 + PB];
+    int *perm = reinterpret_cast<int *>(smem);
+    LT *bvec = reinterpret_cast<LT *>(smem + SmemLayout::align(int64_t(N) * 4));
+    LT *panel = bvec + round_up4(N);
+    LT *utile = panel + (int64_t)N * (PB + 1);
+    const int fail = lu_factor<LT>(A, ld, N, perm, panel, utile, red, ired);
+    if (threadIdx.x == 0) *info = fail;
+    if (fail) return;
+    for (int s = threadIdx.x; s < N; s += kThreads) bvec[s] = (LT)b[perm[s]];
+    __syncthreads();
+    lu_solve<LT>(A, ld, N, bvec);
+    for (int s = threadIdx.x; s < N; s += kThreads) x[s] = (double)bvec[s];
+}
+
+int64_t lu_solve_smem(int N, int precision) {
+    const int lt = precision == LASSIE_PREC_FP64 ? 8 : 4;
+    const int PB = precision == LASSIE_PREC_FP64 ? LuShape<double>::PB : LuShape<float>::PB;
+    const int TN = 128;
+    return SmemLayout::align(int64_t(N) * 4) + int64_t(round_up4(N)) * lt +
+           int64_t(N) * (PB + 1) * lt + int64_t(PB) * TN * lt + 64;
+}
+
+cudaError_t lu_solve_launch(int N, void *A, int ld, const double *b, double *x, int *info,
+                            int precision, cudaStream_t stream) {
+    const int64_t smem = lu_solve_smem(N, precision);
+    if (smem > 220 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e;
+    if (precision == LASSIE_PREC_FP64) {
+        e = cudaFuncSetAttribute(lu_solve_kernel<double>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        lu_solve_kernel<double><<<1, kThreads, smem, stream>>>(N, (double *)A, ld, b, x, info);
+    } else {
+        e = cudaFuncSetAttribute(lu_solve_kernel<float>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        lu_solve_kernel<float><<<1, kThreads, smem, stream>>>(N, (float *)A, ld, b, x, info);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace lassie

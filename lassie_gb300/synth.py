@@ -1,0 +1,153 @@
+"""Seeded synthetic mass-action workloads.
+
+Five workload shapes, each generated from ``numpy.random.default_rng(seed)``
+with ``seed = 1000 * config + instance``:
+
+* ``c1``: 64 species x 64 reactions; 1-2 distinct reactants (stoichiometry 1),
+  0-2 products; k = 10^U(-3,0); x0 ~ U(0,1); t = linspace(0, 10, 100).
+* ``c2``: 512 x 512 stiff; order 0/1/2 (order 2 is A+B or 2A), 1-2 products
+  of stoichiometry 1-2; k = 10^U(-6,6); x0 = 10^U(-3,1); t = linspace(0,100,200).
+* ``c3``: 4096 x 4096; exactly 2 reactants and 2 products (stoichiometry 1);
+  k = 10^U(-4,2); x0 ~ U(0,1); t = linspace(0, 50, 100).
+* ``c4``: batch of 2048 instances; N_i ~ U{32..512}, R_i = N_i, the c1
+  structure; k = 10^U(-4,4) per instance; x0 ~ U(0,1); t = linspace(0,20,50).
+* ``c5``: one 256 x 256 c1-structured model with k = 10^U(-3,3), 64 copies;
+  targets from k * exp(N(0, 0.3^2)); 40 samples in (0, 10].
+
+Products are drawn independently of the reactants, so a species may be both
+consumed and produced by one reaction (its net coefficient is then B - A).
+"""
+from __future__ import annotations
+
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+from .model import Model
+
+
+def _structure(rng: np.random.Generator, N: int, R: int, kind: str
+               ) -> Tuple[np.ndarray, np.ndarray]:
+    left = np.zeros((R, N), np.int32)
+    right = np.zeros((R, N), np.int32)
+    for j in range(R):
+        if kind == "c1":
+            nr = int(rng.integers(1, 3))
+            sp = rng.choice(N, size=nr, replace=False)
+            left[j, sp] = 1
+            npd = int(rng.integers(0, 3))
+            if npd:
+                right[j, rng.choice(N, size=npd, replace=False)] = 1
+        elif kind == "c2":
+            order = int(rng.integers(0, 3))
+            if order == 1:
+                left[j, int(rng.integers(0, N))] = 1
+            elif order == 2:
+                if rng.random() < 0.5:
+                    left[j, rng.choice(N, size=2, replace=False)] = 1
+                else:
+                    left[j, int(rng.integers(0, N))] = 2
+            npd = int(rng.integers(1, 3))
+            sp = rng.choice(N, size=npd, replace=False)
+            right[j, sp] = rng.integers(1, 3, size=npd)
+        elif kind == "c3":
+            left[j, rng.choice(N, size=2, replace=False)] = 1
+            right[j, rng.choice(N, size=2, replace=False)] = 1
+        else:
+            raise ValueError(kind)
+    return left, right
+
+
+def make_c1(instance: int = 0) -> Model:
+    rng = np.random.default_rng(1000 * 1 + instance)
+    N = R = 64
+    left, right = _structure(rng, N, R, "c1")
+    k = 10.0 ** rng.uniform(-3.0, 0.0, R)
+    x0 = rng.uniform(0.0, 1.0, N)
+    return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 10.0, 100))
+
+
+def make_c2(instance: int = 0) -> Model:
+    rng = np.random.default_rng(1000 * 2 + instance)
+    N = R = 512
+    left, right = _structure(rng, N, R, "c2")
+    k = 10.0 ** rng.uniform(-6.0, 6.0, R)
+    x0 = 10.0 ** rng.uniform(-3.0, 1.0, N)
+    return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 100.0, 200))
+
+
+def make_c3(instance: int = 0) -> Model:
+    rng = np.random.default_rng(1000 * 3 + instance)
+    N = R = 4096
+    left, right = _structure(rng, N, R, "c3")
+    k = 10.0 ** rng.uniform(-4.0, 2.0, R)
+    x0 = rng.uniform(0.0, 1.0, N)
+    return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 50.0, 100))
+
+
+def make_c4_instance(instance: int) -> Model:
+    rng = np.random.default_rng(1000 * 4 + instance)
+    N = int(rng.integers(32, 513))
+    left, right = _structure(rng, N, N, "c1")
+    k = 10.0 ** rng.uniform(-4.0, 4.0, N)
+    x0 = rng.uniform(0.0, 1.0, N)
+    return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 20.0, 50))
+
+
+def make_c4(n_instances: int = 2048, first: int = 0) -> List[Model]:
+    return [make_c4_instance(first + q) for q in range(n_instances)]
+
+
+def make_c5(n_copies: int = 64) -> Tuple[List[Model], np.ndarray]:
+    """Base model copies and the perturbed rate constants of each copy's
+    target trajectory (``k * exp(N(0, 0.3^2))``)."""
+    rng = np.random.default_rng(1000 * 5)
+    N = R = 256
+    left, right = _structure(rng, N, R, "c1")
+    k = 10.0 ** rng.uniform(-3.0, 3.0, R)
+    x0 = rng.uniform(0.0, 1.0, N)
+    t = np.linspace(0.0, 10.0, 41)[1:]
+    base = [Model(left=left, right=right, k=k.copy(), x0=x0.copy(), t=t.copy())
+            for _ in range(n_copies)]
+    k_target = np.stack([k * np.exp(rng.normal(0.0, 0.3, R)) for _ in range(n_copies)])
+    return base, k_target
+
+
+def shorten(m: Model, t_end: float, n_samples: int) -> Model:
+    """Same network and parameters on a shorter horizon (parity tests at sizes
+    the CPU oracle finishes in seconds)."""
+    import dataclasses
+    return dataclasses.replace(m, t=np.linspace(0.0, t_end, n_samples))
+
+
+def make(config: str, instance: int = 0) -> Model:
+    return {"c1": make_c1, "c2": make_c2, "c3": make_c3,
+            "c4": make_c4_instance}[config](instance)
+
+
+def tiny_network(kind: str, k: Optional[np.ndarray] = None) -> Model:
+    """Closed-form known-answer networks (N <= 3)."""
+    t = np.linspace(0.0, 2.0, 21)
+    if kind == "decay":            # A -> 0,    x = x0 exp(-k t)
+        left = np.array([[1]]); right = np.array([[0]])
+        kk = np.array([0.7]); x0 = np.array([1.5])
+    elif kind == "conversion":     # A -> B
+        left = np.array([[1, 0]]); right = np.array([[0, 1]])
+        kk = np.array([1.3]); x0 = np.array([1.0, 0.25])
+    elif kind == "dimer":          # 2A -> B,   x_A = x0 / (1 + 2 k x0 t)
+        left = np.array([[2, 0]]); right = np.array([[0, 1]])
+        kk = np.array([0.5]); x0 = np.array([1.0, 0.0])
+    elif kind == "bimolecular":    # A + B -> C
+        left = np.array([[1, 1, 0]]); right = np.array([[0, 0, 1]])
+        kk = np.array([0.8]); x0 = np.array([1.0, 0.6, 0.0])
+    elif kind == "source":         # 0 -> A,    x = x0 + k t
+        left = np.array([[0]]); right = np.array([[1]])
+        kk = np.array([0.3]); x0 = np.array([0.2])
+    elif kind == "reversible":     # A + B <-> C, conserves A+C and B+C
+        left = np.array([[1, 1, 0], [0, 0, 1]])
+        right = np.array([[0, 0, 1], [1, 1, 0]])
+        kk = np.array([2.0, 0.5]); x0 = np.array([1.0, 0.8, 0.1])
+    else:
+        raise ValueError(kind)
+    return Model(left=left.astype(np.int32), right=right.astype(np.int32),
+                 k=kk if k is None else np.asarray(k, np.float64), x0=x0.astype(np.float64), t=t)

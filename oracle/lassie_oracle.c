@@ -1,0 +1,508 @@
+/*
+ * lassie_oracle.c -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
+ *
+ * CPU restatement of the LASSIE deterministic integrator.  Each function cites
+ * the reference file:line it follows (paths inside the LASSIE project).
+ * Build with -ffp-contract=off (see oracle/Makefile): the arithmetic order is
+ * part of the contract with the FP64 CUDA form.
+ */
+#include "lassie_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ model */
+
+/* Simulation.cuh:1061-1130: H = (B-A)^T stored by species with reactions in
+   ascending order; A stored by reaction with species in ascending order.
+   int32 indices instead of the reference's int16 (no 32767 cap). */
+int lo_model_build(int R, int N, const int32_t *left, const int32_t *right,
+                   lo_model *m) {
+    memset(m, 0, sizeof(*m));
+    if (R <= 0 || N <= 0 || !left || !right) return LO_ERR_ARGS;
+    m->n_species = N;
+    m->n_reactions = R;
+    int nnz_a = 0, nnz_h = 0;
+    for (int64_t q = 0; q < (int64_t)R * N; q++) {
+        if (left[q] != 0) nnz_a++;
+        if (right[q] - left[q] != 0) nnz_h++;
+    }
+    m->nnz_a = nnz_a;
+    m->nnz_h = nnz_h;
+    m->rxn_ptr = (int *)malloc(sizeof(int) * (R + 1));
+    m->rxn_species = (int *)malloc(sizeof(int) * (nnz_a ? nnz_a : 1));
+    m->rxn_stoich = (int *)malloc(sizeof(int) * (nnz_a ? nnz_a : 1));
+    m->sp_ptr = (int *)malloc(sizeof(int) * (N + 1));
+    m->sp_rxn = (int *)malloc(sizeof(int) * (nnz_h ? nnz_h : 1));
+    m->sp_coef = (int *)malloc(sizeof(int) * (nnz_h ? nnz_h : 1));
+    if (!m->rxn_ptr || !m->rxn_species || !m->rxn_stoich || !m->sp_ptr ||
+        !m->sp_rxn || !m->sp_coef) {
+        lo_model_free(m);
+        return LO_ERR_ALLOC;
+    }
+    int c = 0;
+    for (int j = 0; j < R; j++) {
+        m->rxn_ptr[j] = c;
+        for (int s = 0; s < N; s++) {
+            int a = left[(int64_t)j * N + s];
+            if (a != 0) {
+                m->rxn_species[c] = s;
+                m->rxn_stoich[c] = a;
+                c++;
+            }
+        }
+    }
+    m->rxn_ptr[R] = c;
+    c = 0;
+    for (int s = 0; s < N; s++) {
+        m->sp_ptr[s] = c;
+        for (int j = 0; j < R; j++) {
+            int h = right[(int64_t)j * N + s] - left[(int64_t)j * N + s];
+            if (h != 0) {
+                m->sp_rxn[c] = j;
+                m->sp_coef[c] = h;
+                c++;
+            }
+        }
+    }
+    m->sp_ptr[N] = c;
+    return LO_OK;
+}
+
+void lo_model_free(lo_model *m) {
+    free(m->rxn_ptr);
+    free(m->rxn_species);
+    free(m->rxn_stoich);
+    free(m->sp_ptr);
+    free(m->sp_rxn);
+    free(m->sp_coef);
+    memset(m, 0, sizeof(*m));
+}
+
+/* kernels.cuh:52-63 (myPow): repeated multiplication, 1 for ex <= 0 */
+static inline double lo_pow(double base, int ex) {
+    double p = 1.0;
+    while (ex > 0) {
+        p = p * base;
+        ex--;
+    }
+    return p;
+}
+
+/* kernels.cuh:5-50 (generate_ode).  For species i, each reaction of its H row
+   in ascending order contributes ((s*k)*x_a^ea)*x_b^eb..., or s*k for a
+   zero-order reaction, added left to right onto 0. */
+void lo_rhs(const lo_model *m, const double *k, const double *x, double *dx) {
+    const int N = m->n_species;
+    for (int i = 0; i < N; i++) {
+        double acc = 0.0;
+        for (int e = m->sp_ptr[i]; e < m->sp_ptr[i + 1]; e++) {
+            const int y = m->sp_rxn[e];
+            const int s = m->sp_coef[e];
+            const int b = m->rxn_ptr[y], en = m->rxn_ptr[y + 1];
+            if (en > b) {
+                double temp = 0.0;
+                for (int j = b; j < en; j++) {
+                    if (j == b)
+                        temp += (double)s * k[y] *
+                                lo_pow(x[m->rxn_species[j]], m->rxn_stoich[j]);
+                    else
+                        temp *= lo_pow(x[m->rxn_species[j]], m->rxn_stoich[j]);
+                }
+                acc = acc + temp;
+            } else {
+                acc = acc + (double)s * k[y];
+            }
+        }
+        dx[i] = acc;
+    }
+}
+
+/* kernels.cuh:205-271 (createJac/createJac_).  Entry (i, g) sums, over the
+   reactions of H row i in ascending order, the partial derivative of that
+   reaction's term with respect to x_g; the other reactants are multiplied in
+   once each, whatever their stoichiometry (exact for total order <= 2). */
+void lo_jacobian(const lo_model *m, const double *k, const double *x,
+                 double *J) {
+    const int N = m->n_species;
+    memset(J, 0, sizeof(double) * (size_t)N * N);
+    for (int i = 0; i < N; i++) {
+        double *row = J + (size_t)i * N;
+        for (int e = m->sp_ptr[i]; e < m->sp_ptr[i + 1]; e++) {
+            const int y = m->sp_rxn[e];
+            const int s = m->sp_coef[e];
+            const int b = m->rxn_ptr[y], en = m->rxn_ptr[y + 1];
+            for (int j = b; j < en; j++) {
+                const int g = m->rxn_species[j];
+                const int a = m->rxn_stoich[j];
+                double temp = 0.0;
+                if (a == 1) {
+                    temp = temp + (double)s * k[y];
+                } else if (a > 1) {
+                    temp = temp + (double)s * k[y] * (double)a * lo_pow(x[g], a - 1);
+                } else {
+                    continue; /* neither branch of kernels.cuh:241/254 */
+                }
+                for (int jj = b; jj < en; jj++)
+                    if (m->rxn_species[jj] != g) temp = temp * x[m->rxn_species[jj]];
+                row[g] = row[g] + temp;
+            }
+        }
+    }
+}
+
+/* Dense LU with partial pivoting (replaces cusolverDnDgetrf,
+   Simulation.cuh:1280-1326).  Pivot = first index of max |a|; failure when the
+   pivot is exactly zero (getrf's info > 0).  Right-looking: every trailing
+   element is updated as a = fma(-l, u, a) once per pivot, in pivot order. */
+int lo_lu_factor(int n, double *a, int *piv) {
+    for (int j = 0; j < n; j++) {
+        int p = j;
+        double best = fabs(a[(size_t)j * n + j]);
+        for (int i = j + 1; i < n; i++) {
+            double v = fabs(a[(size_t)i * n + j]);
+            if (v > best) {
+                best = v;
+                p = i;
+            }
+        }
+        piv[j] = p;
+        if (a[(size_t)p * n + j] == 0.0) return j + 1;
+        if (p != j) {
+            double *rj = a + (size_t)j * n, *rp = a + (size_t)p * n;
+            for (int c = 0; c < n; c++) {
+                double tmp = rj[c];
+                rj[c] = rp[c];
+                rp[c] = tmp;
+            }
+        }
+        const double d = a[(size_t)j * n + j];
+        const double *uj = a + (size_t)j * n;
+        for (int i = j + 1; i < n; i++) {
+            double *ri = a + (size_t)i * n;
+            const double l = ri[j] / d;
+            ri[j] = l;
+            for (int c = j + 1; c < n; c++) ri[c] = fma(-l, uj[c], ri[c]);
+        }
+    }
+    return 0;
+}
+
+/* getrs with one right-hand side: row interchanges in pivot order, unit-lower
+   forward substitution (ascending), upper backward substitution (descending
+   accumulation, then one division by the diagonal). */
+void lo_lu_solve(int n, const double *lu, const int *piv, double *b) {
+    for (int j = 0; j < n; j++) {
+        int p = piv[j];
+        if (p != j) {
+            double tmp = b[j];
+            b[j] = b[p];
+            b[p] = tmp;
+        }
+    }
+    for (int i = 0; i < n; i++) {
+        double acc = b[i];
+        const double *ri = lu + (size_t)i * n;
+        for (int j = 0; j < i; j++) acc = fma(-ri[j], b[j], acc);
+        b[i] = acc;
+    }
+    for (int i = n - 1; i >= 0; i--) {
+        double acc = b[i];
+        const double *ri = lu + (size_t)i * n;
+        for (int j = n - 1; j > i; j--) acc = fma(-ri[j], b[j], acc);
+        b[i] = acc / ri[i];
+    }
+}
+
+/* ------------------------------------------------------------- integrator */
+
+/* Simulation.cuh:632-925 with kernels.cuh:68-199, 289-300, 393-402, 462-477,
+   512-521.  Differences, all documented in the design notes:
+   - the stage vector u starts at 0 (the reference never writes u for feed
+     species and leaves it uninitialised);
+   - the loop stops right after the last sample instead of taking one more
+     step with t1 read past the end of t_vector (Simulation.cuh:689);
+   - the LU is factored once per backward-Euler step: the reference refactors
+     the identical matrix at every Newton iteration, with identical results;
+   - the Newton norm sums in index order (thrust's order in the reference);
+     only its comparison with newton_tol is used. */
+int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
+                    const double *feed, const double *atol, const double *tv,
+                    int nt, const int *cs, int ncs, const lo_opts *opts_in,
+                    double *out, lo_stats *st_out) {
+    lo_opts o;
+    if (opts_in)
+        o = *opts_in;
+    else {
+        o.rkf_step = 1e-3;
+        o.be_step = 0.01;
+        o.newton_tol = 1e-6;
+        o.stiffness_tol = 1e-6;
+        o.newton_iter = 10000;
+        o.max_steps = 0;
+    }
+    lo_stats st;
+    memset(&st, 0, sizeof(st));
+    const int N = m->n_species;
+    if (nt < 0 || (nt > 0 && (!tv || !out))) return LO_ERR_ARGS;
+    if (!cs) ncs = N;
+    for (int j = 0; cs && j < ncs; j++)
+        if (cs[j] < 0 || cs[j] >= N) return LO_ERR_ARGS;
+
+    double *buf = (double *)calloc((size_t)N * 16, sizeof(double));
+    double *M = (double *)malloc(sizeof(double) * (size_t)N * N);
+    int *piv = (int *)malloc(sizeof(int) * (size_t)N);
+    if (!buf || !M || !piv) {
+        free(buf);
+        free(M);
+        free(piv);
+        return LO_ERR_ALLOC;
+    }
+    double *y1 = buf, *u = buf + N, *k1 = buf + 2 * N, *k2 = buf + 3 * N,
+           *k3 = buf + 4 * N, *k4 = buf + 5 * N, *k5 = buf + 6 * N,
+           *k6 = buf + 7 * N, *w1 = buf + 8 * N, *w2 = buf + 9 * N,
+           *delta = buf + 10 * N, *yv = buf + 11 * N, *xr = buf + 12 * N,
+           *fd = buf + 13 * N, *tol = buf + 14 * N, *dx = buf + 15 * N;
+    for (int s = 0; s < N; s++) {
+        y1[s] = x0[s];
+        fd[s] = feed ? feed[s] : 0.0;
+        tol[s] = atol ? atol[s] : 1e-12;
+    }
+
+    int status = LO_OK;
+    int i = 0;
+    double t1 = nt > 0 ? tv[0] : 0.0;
+    double t = 0.0;
+    double dt = o.rkf_step;
+    double newDtBDF = o.be_step;
+
+    while (i < nt) {
+        if (o.max_steps > 0 && st.outer_iters >= o.max_steps) {
+            status = LO_ERR_MAX_STEPS;
+            break;
+        }
+        st.outer_iters++;
+        /* Simulation.cuh:674-690 */
+        if (fabs(t1 - t) < 1e-5) {
+            for (int j = 0; j < ncs; j++) out[(size_t)i * ncs + j] = y1[cs ? cs[j] : j];
+            i++;
+            if (i >= nt) break;
+            t1 = tv[i];
+        }
+        /* RKF45 attempt: Simulation.cuh:692-735, kernels.cuh:68-199 */
+        lo_rhs(m, k, y1, k1);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k1[s] = fd[s];
+            else {
+                k1[s] = k1[s] * dt;
+                u[s] = y1[s] + k1[s] / 4.0;
+            }
+        }
+        lo_rhs(m, k, u, k2);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k2[s] = fd[s];
+            else {
+                k2[s] = k2[s] * dt;
+                u[s] = y1[s] + (3.0 * k1[s]) / 32.0 + (9.0 * k2[s]) / 32.0;
+            }
+        }
+        lo_rhs(m, k, u, k3);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k3[s] = fd[s];
+            else {
+                k3[s] = k3[s] * dt;
+                u[s] = y1[s] + (1932.0 * k1[s]) / 2197.0 - (7200.0 * k2[s]) / 2197.0 +
+                       (7296.0 * k3[s]) / 2197.0;
+            }
+        }
+        lo_rhs(m, k, u, k4);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k4[s] = fd[s];
+            else {
+                k4[s] = k4[s] * dt;
+                u[s] = y1[s] + (439.0 * k1[s]) / 216.0 - (8.0 * k2[s]) +
+                       (3680.0 * k3[s]) / 513.0 - (845.0 * k4[s]) / 4104.0;
+            }
+        }
+        lo_rhs(m, k, u, k5);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k5[s] = fd[s];
+            else {
+                k5[s] = k5[s] * dt;
+                u[s] = y1[s] - (8.0 * k1[s]) / 27.0 + (2.0 * k2[s]) -
+                       (3544.0 * k3[s]) / 2565.0 + (1859.0 * k4[s]) / 4104.0 -
+                       (11.0 * k5[s]) / 40.0;
+            }
+        }
+        lo_rhs(m, k, u, k6);
+        int count = 0;
+        double dmin = 0.0;
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k6[s] = fd[s];
+            else k6[s] = k6[s] * dt;
+            if (fd[s] != 0.0) {
+                w1[s] = fd[s];
+                w2[s] = fd[s];
+            } else {
+                w1[s] = y1[s] + (25.0 * k1[s]) / 216.0 + (1408.0 * k3[s]) / 2565.0 +
+                        (2197.0 * k4[s]) / 4104.0 - k5[s] / 5.0;
+                w2[s] = y1[s] + (16.0 * k1[s]) / 135.0 + (6656.0 * k3[s]) / 12825.0 +
+                        (28561.0 * k4[s]) / 56430.0 - (9.0 * k5[s] / 50.0) +
+                        (2.0 * k6[s]) / 55.0;
+            }
+            /* kernels.cuh:184-199 */
+            double R = fabs(w1[s] - w2[s]) / dt;
+            delta[s] = 0.84 * sqrt(sqrt(tol[s] / R));
+            if (R <= tol[s] && !isnan(R) && !isinf(R) && w1[s] > 0) count++;
+            /* thrust::min_element: first element, replaced only by a strictly
+               smaller one (a leading NaN therefore sticks) */
+            if (s == 0 || delta[s] < dmin) dmin = delta[s];
+        }
+        if (count == N) {
+            /* accept: Simulation.cuh:742-768 */
+            memcpy(y1, w1, sizeof(double) * N);
+            double d_temp = dt * dmin;
+            if ((t + d_temp) > t1) dt = fabs(t1 - t);
+            else dt = d_temp;
+            t = t + dt;
+            st.rkf_accepts++;
+        } else {
+            /* reject: Simulation.cuh:769-921 */
+            double dt_old = dt;
+            dt = dt * dmin;
+            if ((dt < o.stiffness_tol) | isnan(dt) | isinf(dt) |
+                (fabs(dt_old - dt) < 1e-3)) {
+                dt = newDtBDF;
+                if ((t + dt) > t1) dt = fabs(t1 - t);
+                memcpy(yv, y1, sizeof(double) * N);
+                int64_t itN = 0;
+                double errN = 1000;
+                int luFail = 0;
+                st.be_steps++;
+                while ((itN < o.newton_iter) & (errN > o.newton_tol)) {
+                    lo_rhs(m, k, yv, xr);
+                    /* kernels.cuh:289-300 */
+                    for (int s = 0; s < N; s++) xr[s] = -(yv[s] - y1[s] - dt * xr[s]);
+                    if (itN == 0) {
+                        /* kernels.cuh:205-271, 393-402: M = I - dt*J */
+                        lo_jacobian(m, k, yv, M);
+                        for (int r = 0; r < N; r++)
+                            for (int c = 0; c < N; c++) {
+                                double I = (r == c) ? 1.0 : 0.0;
+                                M[(size_t)r * N + c] = I - dt * M[(size_t)r * N + c];
+                            }
+                        st.lu_factorisations++;
+                        if (lo_lu_factor(N, M, piv) != 0) luFail = 1;
+                    }
+                    if (luFail) {
+                        /* Simulation.cuh:869-875, kernels.cuh:512-521 */
+                        for (int s = 0; s < N; s++)
+                            if (isnan(yv[s]) || isinf(yv[s]) || yv[s] < 0) yv[s] = y1[s];
+                        newDtBDF = dt * 0.1;
+                        st.lu_failures++;
+                        break;
+                    }
+                    memcpy(dx, xr, sizeof(double) * N);
+                    lo_lu_solve(N, M, piv, dx);
+                    /* kernels.cuh:462-477 and Simulation.cuh:883-890 */
+                    double sum = 0.0;
+                    for (int s = 0; s < N; s++) {
+                        double old = yv[s];
+                        if (fd[s] == 0) yv[s] = yv[s] + dx[s];
+                        else yv[s] = fd[s];
+                        dx[s] = yv[s] - old;
+                        sum = sum + (double)(float)(dx[s] * dx[s]);
+                    }
+                    errN = sqrt(sum);
+                    itN = itN + 1;
+                    st.newton_iters++;
+                }
+                if (!luFail) {
+                    /* Simulation.cuh:894-909 */
+                    int bad = 0;
+                    for (int s = 0; s < N; s++)
+                        if (isnan(yv[s]) || isinf(yv[s]) || yv[s] < 0) bad++;
+                    if (bad > 0) {
+                        for (int s = 0; s < N; s++)
+                            if (isnan(yv[s]) || isinf(yv[s]) || yv[s] < 0) yv[s] = y1[s];
+                        newDtBDF = dt * 0.1;
+                        st.nan_reverts++;
+                    }
+                }
+                memcpy(y1, yv, sizeof(double) * N);
+                t = t + dt;
+            } else {
+                st.rkf_retries++;
+            }
+        }
+    }
+    st.t_final = t;
+    st.dt_be_final = newDtBDF;
+    if (st_out) *st_out = st;
+    free(buf);
+    free(M);
+    free(piv);
+    return status;
+}
+
+/* ------------------------------------------------------------------ batch */
+
+typedef struct {
+    int n_inst;
+    const lo_model *const *models;
+    const double *const *k;
+    const double *const *x0;
+    const double *const *t;
+    const int *nt;
+    const lo_opts *opts;
+    double *const *out;
+    lo_stats *stats;
+    int *status;
+    int next;
+    pthread_mutex_t mu;
+} lo_batch_ctx;
+
+static void *lo_batch_worker(void *arg) {
+    lo_batch_ctx *c = (lo_batch_ctx *)arg;
+    for (;;) {
+        pthread_mutex_lock(&c->mu);
+        int q = c->next++;
+        pthread_mutex_unlock(&c->mu);
+        if (q >= c->n_inst) break;
+        c->status[q] = lo_solve_compat(c->models[q], c->k[q], c->x0[q], NULL, NULL,
+                                       c->t[q], c->nt[q], NULL, 0, c->opts,
+                                       c->out[q], c->stats ? &c->stats[q] : NULL);
+    }
+    return NULL;
+}
+
+int lo_solve_batch(int n_inst, const lo_model *const *models,
+                   const double *const *k, const double *const *x0,
+                   const double *const *t, const int *nt, const lo_opts *opts,
+                   double *const *out, lo_stats *stats, int *status,
+                   int threads) {
+    if (n_inst < 0 || threads < 1) return LO_ERR_ARGS;
+    lo_batch_ctx c;
+    c.n_inst = n_inst;
+    c.models = models;
+    c.k = k;
+    c.x0 = x0;
+    c.t = t;
+    c.nt = nt;
+    c.opts = opts;
+    c.out = out;
+    c.stats = stats;
+    c.status = status;
+    c.next = 0;
+    pthread_mutex_init(&c.mu, NULL);
+    if (threads > n_inst) threads = n_inst > 0 ? n_inst : 1;
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    if (!th) return LO_ERR_ALLOC;
+    for (int q = 0; q < threads; q++) pthread_create(&th[q], NULL, lo_batch_worker, &c);
+    for (int q = 0; q < threads; q++) pthread_join(th[q], NULL);
+    free(th);
+    pthread_mutex_destroy(&c.mu);
+    return LO_OK;
+}

@@ -1,0 +1,107 @@
+/*
+ * lassie_oracle.h -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
+ *
+ * CPU restatement (plain C, FP64) of the LASSIE deterministic integrator
+ * (mass-action RHS, analytic Jacobian, RKF45 with LASSIE's stiffness switch,
+ * backward-Euler modified Newton with a dense partial-pivot LU).  It is the
+ * checker for the CUDA path: only tests/, the smoke check and the CPU-baseline
+ * leg of bench.py may load it.  The product never links or calls it.
+ *
+ * Arithmetic contract shared with the FP64 CUDA form (so that the two agree
+ * bit for bit on the same inputs):
+ *   - every expression is evaluated in the order the reference source writes
+ *     it, with no contraction (compiled with -ffp-contract=off);
+ *   - the LU and the triangular solves accumulate with fma() in ascending
+ *     pivot order (forward) and descending order (backward);
+ *   - the RKF45 step-size factor (atol/R)^(1/4) is sqrt(sqrt(atol/R)), which
+ *     is correctly rounded on every IEEE platform (the reference calls pow());
+ *   - the Newton norm squares are rounded to float before summation, as the
+ *     reference's `square` functor does (Simulation.cuh:58-64).
+ */
+#ifndef LASSIE_ORACLE_H
+#define LASSIE_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+    int n_species;
+    int n_reactions;
+    /* reactant CSR by reaction (A), species ascending (Simulation.cuh:1107-1130) */
+    int *rxn_ptr;     /* R+1 */
+    int *rxn_species; /* nnzA */
+    int *rxn_stoich;  /* nnzA */
+    /* net-stoichiometry CSR by species (H = (B-A)^T), reaction ascending
+       (Simulation.cuh:1061-1105) */
+    int *sp_ptr;      /* N+1 */
+    int *sp_rxn;      /* nnzH */
+    int *sp_coef;     /* nnzH */
+    int nnz_a;
+    int nnz_h;
+} lo_model;
+
+typedef struct {
+    double rkf_step;       /* default 1e-3  (Simulation.cuh:281-288) */
+    double be_step;        /* default 0.01  (Simulation.cuh:272-279) */
+    double newton_tol;     /* default 1e-6  (Simulation.cuh:299-306) */
+    double stiffness_tol;  /* default 1e-6  (Simulation.cuh:308-315) */
+    int64_t newton_iter;   /* default 10000 (Simulation.cuh:290-297) */
+    int64_t max_steps;     /* loop-iteration cap; <=0 means unlimited */
+} lo_opts;
+
+typedef struct {
+    int64_t outer_iters;
+    int64_t rkf_accepts;
+    int64_t rkf_retries;
+    int64_t be_steps;
+    int64_t newton_iters;
+    int64_t lu_factorisations;
+    int64_t lu_failures;
+    int64_t nan_reverts;
+    double t_final;
+    double dt_be_final;
+} lo_stats;
+
+/* status codes (shared numbering with the CUDA C-ABI) */
+#define LO_OK 0
+#define LO_ERR_ARGS (-20)
+#define LO_ERR_MAX_STEPS (-21)
+#define LO_ERR_ALLOC (-22)
+
+int lo_model_build(int n_reactions, int n_species, const int32_t *left,
+                   const int32_t *right, lo_model *out);
+void lo_model_free(lo_model *m);
+
+/* dx = f(x) -- kernels.cuh:5-63 */
+void lo_rhs(const lo_model *m, const double *k, const double *x, double *dx);
+/* dense row-major Jacobian J[i*N+g] with the reference's stoichiometry
+   handling (kernels.cuh:205-271) */
+void lo_jacobian(const lo_model *m, const double *k, const double *x, double *J);
+/* in-place LU with partial pivoting on a row-major n x n matrix.
+   Returns 0, or j+1 when the pivot of column j is exactly zero. */
+int lo_lu_factor(int n, double *a, int *piv);
+void lo_lu_solve(int n, const double *lu, const int *piv, double *b);
+
+/* The full integration (Simulation.cuh:632-925).
+   k[R], x0[N], feed[N] (may be NULL), atol[N] (may be NULL -> 1e-12),
+   t[nt], cs[ncs] (may be NULL -> all species), out[nt*ncs]. */
+int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
+                    const double *feed, const double *atol, const double *t,
+                    int nt, const int *cs, int ncs, const lo_opts *opts,
+                    double *out, lo_stats *stats);
+
+/* Batch of independent instances solved on `threads` host threads
+   (the CPU baseline).  Arrays are per-instance pointers. */
+int lo_solve_batch(int n_inst, const lo_model *const *models,
+                   const double *const *k, const double *const *x0,
+                   const double *const *t, const int *nt,
+                   const lo_opts *opts, double *const *out, lo_stats *stats,
+                   int *status, int threads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,77 @@
+"""The C ABI library loads and exports every function include/ declares;
+host-only entry points (model compiler, options, statuses) work without a
+GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from lassie_gb300 import _native as nat
+from lassie_gb300 import synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            names |= set(re.findall(r"\b(lassie_\w+)\s*\(", text))
+    return names
+
+
+def test_exports_every_declared_symbol(native):
+    decl = declared_functions()
+    assert decl, "no declarations found"
+    assert decl <= set(nat.EXPORTS), decl - set(nat.EXPORTS)
+    for name in decl:
+        assert hasattr(native, name), name
+
+
+def test_defaults_match_reference(native):
+    o = nat.Opts()
+    native.lassie_opts_default(C.byref(o))
+    assert (o.rkf_step, o.be_step, o.newton_tol, o.stiffness_tol, o.newton_iter) == \
+        (1e-3, 0.01, 1e-6, 1e-6, 10000)
+
+
+def test_model_compiler_counts(native):
+    m = synth.make_c1()
+    left = np.ascontiguousarray(m.left, np.int32)
+    right = np.ascontiguousarray(m.right, np.int32)
+    h = C.c_void_p()
+    assert native.lassie_model_create_dense(64, 64, left.ctypes.data, right.ctypes.data,
+                                            C.byref(h)) == 0
+    v = [C.c_int32() for _ in range(4)]
+    assert native.lassie_model_info(h, *[C.byref(x) for x in v]) == 0
+    assert [x.value for x in v] == [64, 64, int(np.count_nonzero(left)),
+                                    int(np.count_nonzero(right - left))]
+    native.lassie_model_destroy(h)
+
+
+def test_csr_and_dense_agree(native):
+    # A + B -> C, 2C -> A (given as CSR by reaction)
+    rp = np.array([0, 2, 3], np.int32); rs = np.array([0, 1, 2], np.int32)
+    rc = np.array([1, 1, 2], np.int32)
+    pp = np.array([0, 1, 2], np.int32); ps = np.array([2, 0], np.int32)
+    pc = np.array([1, 1], np.int32)
+    h = C.c_void_p()
+    assert native.lassie_model_create_csr(3, 2, rp.ctypes.data, rs.ctypes.data, rc.ctypes.data,
+                                          pp.ctypes.data, ps.ctypes.data, pc.ctypes.data,
+                                          C.byref(h)) == 0
+    v = [C.c_int32() for _ in range(4)]
+    native.lassie_model_info(h, *[C.byref(x) for x in v])
+    assert [x.value for x in v] == [3, 2, 3, 5]
+    native.lassie_model_destroy(h)
+
+
+def test_bad_arguments_are_rejected(native):
+    h = C.c_void_p()
+    assert native.lassie_model_create_dense(0, 1, None, None, C.byref(h)) == nat.ERR_ARGS
+    assert native.lassie_status_string(nat.ERR_MAX_STEPS) == b"maximum number of steps reached"
+    # stoichiometry outside int8 is refused, not truncated
+    left = np.array([[300]], np.int32); right = np.zeros((1, 1), np.int32)
+    assert native.lassie_model_create_dense(1, 1, left.ctypes.data, right.ctypes.data,
+                                            C.byref(h)) == nat.ERR_TOO_LARGE

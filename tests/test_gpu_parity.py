@@ -1,0 +1,110 @@
+"""CUDA path vs the CPU oracle, through the C ABI.
+
+The FP64 engine follows the oracle's arithmetic contract (same evaluation
+order, explicit fma in the LU and solves, no contraction), so its outputs are
+compared for exact equality.  The mixed engine (FP32 LU + FP64 refinement) is
+compared at rtol 1e-6 / atol 1e-9, the spec parity tolerance.
+"""
+import numpy as np
+import pytest
+
+from lassie_gb300 import synth, solver
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 1e-6, 1e-9
+
+
+def within(a, b, rtol=RTOL, atol=ATOL):
+    return bool(np.all(np.abs(a - b) <= atol + rtol * np.abs(b)))
+
+
+def small_cases():
+    yield "c1", synth.make_c1()
+    yield "c4-2-short", synth.shorten(synth.make_c4_instance(2), 1.0, 11)
+    yield "c4-5-short", synth.shorten(synth.make_c4_instance(5), 0.3, 4)
+    yield "c2-short", synth.shorten(synth.make_c2(), 0.012, 3)
+    for kind in ("decay", "conversion", "dimer", "bimolecular", "source", "reversible"):
+        yield kind, synth.tiny_network(kind)
+
+
+@pytest.mark.parametrize("name,m", list(small_cases()), ids=[c[0] for c in small_cases()])
+def test_rhs_bit_exact(gpu, name, m):
+    om = O.OracleModel(m.left, m.right)
+    rng = np.random.default_rng(7)
+    for _ in range(3):
+        x = rng.uniform(0, 2, m.n_species)
+        assert np.array_equal(solver.rhs(m, x), om.rhs(m.k, x))
+
+
+@pytest.mark.parametrize("name,m", list(small_cases()), ids=[c[0] for c in small_cases()])
+def test_newton_matrix_bit_exact(gpu, name, m):
+    om = O.OracleModel(m.left, m.right)
+    x = np.random.default_rng(3).uniform(0, 2, m.n_species)
+    h = 0.01
+    J = om.jacobian(m.k, x)
+    M_ref = np.eye(m.n_species) - h * J
+    assert np.array_equal(solver.newton_matrix(m, x, h), M_ref)
+
+
+@pytest.mark.parametrize("n", [1, 5, 31, 32, 33, 64, 100, 257, 512])
+def test_lu_fp64_bit_exact(gpu, n):
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=(n, n)) + np.eye(n) * 0.1
+    b = rng.normal(size=n)
+    lu, piv, rc = O.lu_factor(a)
+    assert rc == 0
+    ref = O.lu_solve(lu, piv, b)
+    x, info = solver.lu_solve(a, b, "fp64")
+    assert info == 0
+    assert np.array_equal(x, ref)
+
+
+@pytest.mark.parametrize("n", [8, 64, 300])
+def test_lu_mixed_close(gpu, n):
+    rng = np.random.default_rng(n + 1)
+    a = rng.normal(size=(n, n)) + np.eye(n) * n
+    b = rng.normal(size=n)
+    x, info = solver.lu_solve(a, b, "mixed")
+    assert info == 0
+    ref = np.linalg.solve(a, b)
+    assert np.allclose(x, ref, rtol=1e-4, atol=1e-5)
+
+
+def test_lu_singular_reports_column(gpu):
+    a = np.eye(6)
+    a[:, 3] = 0.0
+    x, info = solver.lu_solve(a, np.ones(6), "fp64")
+    assert info == 4
+    _, _, rc = O.lu_factor(a)
+    assert rc == 4
+
+
+@pytest.mark.parametrize("name,m", list(small_cases()), ids=[c[0] for c in small_cases()])
+def test_solve_fp64_bit_exact(gpu, name, m):
+    ref, st_ref, rc = O.solve(m, max_steps=2_000_000)
+    assert rc == 0
+    out, st = solver.simulate(m, engine="fp64", deadline_s=120)
+    assert st["status"] == 0
+    assert st["be_steps"] == st_ref["be_steps"]
+    assert st["rkf_accepts"] == st_ref["rkf_accepts"]
+    assert st["newton_iters"] == st_ref["newton_iters"]
+    assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
+
+
+@pytest.mark.parametrize("name,m", list(small_cases()), ids=[c[0] for c in small_cases()])
+def test_solve_mixed_within_tolerance(gpu, name, m):
+    ref, st_ref, rc = O.solve(m, max_steps=2_000_000)
+    out, st = solver.simulate(m, engine="mixed", deadline_s=120)
+    assert st["status"] == 0
+    assert within(out, ref), float(np.max(np.abs(out - ref) - RTOL * np.abs(ref)))
+
+
+def test_batch_equals_single(gpu):
+    models = [synth.shorten(synth.make_c4_instance(q), 0.2, 3) for q in range(6)]
+    outs, stats = solver.simulate_batch(models, engine="fp64", deadline_s=120)
+    for m, o, s in zip(models, outs, stats):
+        ref, _, _ = O.solve(m)
+        assert s["status"] == 0
+        assert np.array_equal(o, ref)

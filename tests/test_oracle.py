@@ -1,0 +1,167 @@
+"""The CPU oracle against closed forms, finite differences and LAPACK.
+
+Pins the restatement of the reference's RHS (kernels.cuh:5-50), Jacobian
+(kernels.cuh:205-271), LU solve (replacing cuSOLVER getrf/getrs,
+Simulation.cuh:1280-1326) and integrator (Simulation.cuh:632-925).
+"""
+import numpy as np
+import pytest
+
+from lassie_gb300 import synth
+from lassie_gb300.model import compile_model, rhs_numpy
+from oracle import oracle as O
+
+
+@pytest.mark.parametrize("cfg", ["c1", "c2"])
+def test_rhs_matches_vectorised_formula(cfg):
+    m = synth.make(cfg)
+    om = O.OracleModel(m.left, m.right)
+    cm = compile_model(m.left, m.right)
+    rng = np.random.default_rng(0)
+    for _ in range(3):
+        x = rng.uniform(0, 3, m.n_species)
+        a, b = om.rhs(m.k, x), rhs_numpy(cm, m.k, x)
+        assert np.allclose(a, b, rtol=1e-12, atol=1e-12 * np.abs(b).max())
+
+
+def test_rhs_summation_order_is_reaction_ascending():
+    # species 0 receives +1e16 (reaction 0), -1e16 (reaction 1), +1 (reaction 2):
+    # left-to-right in reaction order gives exactly 1.0
+    left = np.array([[0, 0], [0, 1], [0, 0]], np.int32)
+    right = np.array([[1, 0], [0, 1], [1, 0]], np.int32)
+    right[1, 0] = 0
+    left[1, 0] = 1
+    left[1, 1] = 0
+    k = np.array([1e16, 1e16, 1.0])
+    om = O.OracleModel(left, right)
+    dx = om.rhs(k, np.array([1.0, 1.0]))
+    assert dx[0] == 1.0
+
+
+@pytest.mark.parametrize("cfg", ["c1", "c2"])
+def test_jacobian_matches_central_differences(cfg):
+    m = synth.make(cfg)
+    om = O.OracleModel(m.left, m.right)
+    x = np.random.default_rng(1).uniform(0.5, 1.5, m.n_species)
+    J = om.jacobian(m.k, x)
+    h = 1e-6
+    cols = np.random.default_rng(2).choice(m.n_species, 8, replace=False)
+    for g in cols:
+        e = np.zeros(m.n_species); e[g] = h
+        fd = (om.rhs(m.k, x + e) - om.rhs(m.k, x - e)) / (2 * h)
+        scale = max(1.0, np.abs(fd).max())
+        assert np.allclose(J[:, g], fd, rtol=1e-5, atol=1e-6 * scale)
+
+
+def test_jacobian_quirk_ignores_other_stoichiometry():
+    # A + 2B -> 0 (order 3): d/dA of k*A*B^2 is k*B^2, the reference uses k*B
+    left = np.array([[1, 2]], np.int32)
+    right = np.zeros((1, 2), np.int32)
+    om = O.OracleModel(left, right)
+    J = om.jacobian(np.array([2.0]), np.array([3.0, 5.0]))
+    assert J[0, 0] == -2.0 * 5.0
+    assert J[1, 0] == -2.0 * 2.0 * 5.0
+    assert J[0, 1] == -2.0 * 2.0 * 5.0 * 3.0
+
+
+@pytest.mark.parametrize("n", [1, 7, 64, 200])
+def test_lu_solve_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=(n, n)) + np.eye(n)
+    b = rng.normal(size=n)
+    lu, piv, rc = O.lu_factor(a)
+    assert rc == 0
+    x = O.lu_solve(lu, piv, b)
+    assert np.allclose(x, np.linalg.solve(a, b), rtol=1e-9, atol=1e-9)
+
+
+def test_lu_pivot_ties_pick_first_row():
+    a = np.array([[1.0, 2.0], [-1.0, 1.0]])
+    lu, piv, rc = O.lu_factor(a)
+    assert rc == 0 and piv[0] == 0
+
+
+def test_lu_reports_zero_pivot():
+    a = np.array([[0.0, 1.0], [0.0, 2.0]])
+    _, _, rc = O.lu_factor(a)
+    assert rc == 1
+
+
+def _solve(m, **kw):
+    out, st, rc = O.solve(m, **kw)
+    assert rc == 0
+    return out, st
+
+
+def test_stiff_decay_is_exact_backward_euler():
+    # k*h = 10: every RKF45 attempt fails and the switch takes backward-Euler
+    # steps of be_step = 0.01, so x_n = x0 / (1 + k h)^n exactly (the linear
+    # Newton system converges in one correction)
+    m = synth.tiny_network("decay", k=np.array([1000.0]))
+    m.t = np.linspace(0.0, 0.1, 3)
+    m.atol = np.array([1e-300])  # no RKF45 attempt can pass the error test
+    out, st = _solve(m)
+    n = np.round(m.t / 0.01)
+    exact = m.x0[0] / (1.0 + 1000.0 * 0.01) ** n
+    assert st["rkf_accepts"] == 0 and st["be_steps"] == 10
+    assert np.allclose(out[:, 0], exact, rtol=1e-9, atol=0)
+
+
+def test_decay_rkf_path_lags_the_clock():
+    # Non-stiff decay: accepted RKF45 steps advance the clock by the next step
+    # size and the state by the previous one (Simulation.cuh:753-767), so the
+    # sampled state lies between the exact value and x0 and decreases.
+    m = synth.tiny_network("decay")
+    out, st = _solve(m)
+    exact = m.x0[0] * np.exp(-m.k[0] * m.t)
+    assert st["rkf_accepts"] > 0
+    assert np.all(np.diff(out[:, 0]) < 0)
+    assert np.all(out[:, 0] >= exact - 1e-12) and np.all(out[:, 0] <= m.x0[0])
+
+
+def test_source_is_bounded_by_linear_growth():
+    m = synth.tiny_network("source")
+    out, _ = _solve(m)
+    assert np.all(np.diff(out[:, 0]) > 0)
+    assert np.all(out[:, 0] <= m.x0[0] + m.k[0] * m.t + 1e-12)
+
+
+def test_reversible_conserves_moieties():
+    m = synth.tiny_network("reversible")
+    out, _ = _solve(m)
+    a, b, c = out[:, 0], out[:, 1], out[:, 2]
+    assert np.allclose(a + c, a[0] + c[0], rtol=1e-9)
+    assert np.allclose(b + c, b[0] + c[0], rtol=1e-9)
+
+
+def test_dimer_conserves_and_decreases():
+    # the clock can run ahead of or behind the state (Simulation.cuh:767), so
+    # only the invariants are exact: A decreases and A + 2B is conserved
+    m = synth.tiny_network("dimer")
+    out, _ = _solve(m)
+    assert np.all(np.diff(out[:, 0]) < 0)
+    # 2A -> B: A + 2B is conserved
+    assert np.allclose(out[:, 0] + 2 * out[:, 1], m.x0[0] + 2 * m.x0[1], rtol=1e-9)
+
+
+def test_c1_runs_and_samples_every_time():
+    m = synth.make_c1()
+    out, st = _solve(m)
+    assert out.shape == (100, 64)
+    assert st["t_final"] == pytest.approx(10.0)
+    assert np.all(np.isfinite(out)) and np.all(out >= 0)
+
+
+def test_max_steps_cap_returns_status():
+    m = synth.make_c1()
+    _, st, rc = O.solve(m, max_steps=10)
+    assert rc == -21
+    assert st["outer_iters"] == 10
+
+
+def test_batch_equals_single():
+    models = [synth.shorten(synth.make_c4_instance(q), 0.05, 2) for q in (2, 14, 47)]
+    outs, stats, status = O.solve_batch(models, threads=2)
+    for m, o, s in zip(models, outs, status):
+        ref, _, _ = O.solve(m)
+        assert s == 0 and np.array_equal(o, ref)
