@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark of the LASSIE GB300 integrator on the batched workload.
+
+Workload: 2048 independent mass-action instances (species N_i ~ U{32..512},
+R_i = N_i, 1-2 reactant structure, k ~ 10^U(-4,4), t in [0,20], 50 samples),
+integrated with the reference's step control (RKF45, stiffness switch,
+backward-Euler modified Newton) by the mixed-precision batched form (FP32 LU,
+FP64 refinement) in one persistent launch.  A step integrates the whole
+batch; ``value`` is instances per second with inputs resident in HBM,
+``e2e`` the same through the public host-buffer API (``lassie_solve_batch``).
+
+Extra keys: the plain FP64 GPU form and the max relative error against it on
+a sample, the batched RHS kernel's HBM bandwidth, the roofline of the
+integrator kernel, the CPU baseline (the oracle port on the host cores), the
+SM clocks sampled during the timed region.
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+oracle port, all host threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sims/s and adjoint grads/s at rtol 1e-6 vs plain FP64 GPU form; RHS HBM GB/s"
+WORKLOAD = "c4: 2048 instances, N_i~U{32..512}, R_i=N_i, k~10^U(-4,4), t in [0,20], 50 samples"
+RTOL, ATOL = 1e-6, 1e-9
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the integrator kernel from the committed ncu
+    summary (scaled to the full batch), or None."""
+    p = os.path.join(ROOT, "profiles", "compat_kernel_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f).get("dram_bytes_per_full_launch")
+    return None
+
+
+def lu_flops(stats, models, engine):
+    """Algorithmic FLOPs of the dense linear algebra the integration did:
+    (2/3)N^3 per factorisation + 2N^2 per triangular-solve pair."""
+    tot = 0.0
+    for s, m in zip(stats, models):
+        n = float(m.n_species)
+        pairs = s["refine_sweeps"] if engine == "mixed" else s["newton_iters"]
+        tot += s["lu_factorisations"] * (2.0 / 3.0) * n ** 3 + pairs * 2.0 * n * n
+    return tot
+
+
+def max_rel_err(a_list, b_list):
+    import numpy as np
+    worst, bad = 0.0, 0
+    for a, b in zip(a_list, b_list):
+        d = np.abs(a - b)
+        rel = d / np.maximum(np.abs(b), ATOL / RTOL)
+        worst = max(worst, float(rel.max()) if rel.size else 0.0)
+        bad += int(np.count_nonzero(d > ATOL + RTOL * np.abs(b)))
+    return worst, bad
+
+
+def cpu_baseline(n_total, threads=None, stride=64, t_frac=0.1):
+    """The oracle port on the host cores: every `stride`-th instance of the
+    workload on the first `t_frac` of its horizon, extrapolated to the
+    horizon (the backward-Euler step is fixed, so cost is uniform in time)."""
+    from lassie_gb300 import synth
+    from oracle import oracle as O
+    idx = list(range(0, n_total, stride))
+    models = [synth.shorten(synth.make_c4_instance(q), 20.0 * t_frac,
+                            max(2, int(round(50 * t_frac))))
+              for q in idx]
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    _, _, status = O.solve_batch(models, threads=threads)
+    dt = time.perf_counter() - t0
+    sims = len(models) / (dt / t_frac)
+    return {"value": sims, "unit": "sims/s", "cores": threads, "kind": "port",
+            "sample": f"{len(models)} of the {n_total} instances (every {stride}th), "
+                      f"t in [0,{20.0 * t_frac:g}] (= {t_frac:g} of the horizon), "
+                      f"time scaled by {1 / t_frac:g}; {dt:.2f} s wall",
+            "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from lassie_gb300 import synth  # noqa: F401
+    stride, t_frac = 128, 0.05
+    for _ in range(args.warmup):
+        cpu_baseline(args.instances, stride=stride, t_frac=t_frac)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        cb = cpu_baseline(args.instances, stride=stride, t_frac=t_frac)
+        vals.append(cb["value"])
+        secs.append(cb["seconds"])
+    v = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "sims/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * statistics.mean(secs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "reference algorithm, CPU (oracle port)",
+                   "l2": "n/a (host)"},
+        "cpu_baseline": {"value": v, "unit": "sims/s", "cores": cb["cores"], "kind": "port",
+                         "sample": cb["sample"]},
+        "e2e": {"value": v, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def rhs_bandwidth(torch, stream, n_inst=65536, reps=20):
+    """Batched RHS kernel on one 256-species network with n_inst
+    parameterisations (x, k, dx each n_inst*256 doubles, larger than L2)."""
+    import ctypes as C
+    import numpy as np
+    from lassie_gb300 import synth, _native as nat
+    from lassie_gb300.solver import NativeModel
+    base, _ = synth.make_c5(1)
+    m = base[0]
+    nm = NativeModel.of(m)
+    N, R = m.n_species, m.n_reactions
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(0)
+    x = torch.rand((n_inst, N), dtype=torch.float64, device=dev, generator=g)
+    k = torch.rand((n_inst, R), dtype=torch.float64, device=dev, generator=g)
+    dx = torch.empty_like(x)
+    L = nat.load()
+    launch = lambda: nat.check(L.lassie_rhs_device(nm.handle, n_inst, k.data_ptr(), x.data_ptr(),  # noqa: E731
+                                                   dx.data_ptr(), C.c_void_p(stream.cuda_stream)),
+                               "lassie_rhs_device")
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            launch()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            launch()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    n_a, n_h = nm.info()[2], nm.info()[3]
+    alg = n_inst * (8 * R + 8 * N + 8 * N) + 4 * (R + 1 + n_a + N + 1 + n_h)
+    return {"gbs": alg / (ms * 1e-3) / 1e9, "ms_per_launch": ms, "bytes_per_launch": alg,
+            "network": "256 species x 256 reactions", "instances": n_inst}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--instances", type=int, default=2048)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP64-form, RHS and CPU-baseline measurements")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    from lassie_gb300 import synth, solver, sharding
+    from lassie_gb300 import _native as nat
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    L = nat.load()
+    if not L.lassie_device_ok():
+        raise RuntimeError("no sm_103 device")
+
+    # weak scaling: every rank integrates its own 2048 instances
+    ids = sharding.weak_shard(args.instances, rank)
+    models = synth.make_c4(args.instances, first=ids.start)
+    stream = torch.cuda.Stream()
+    batch = solver.Batch(models, engine="mixed", deadline_s=600)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            batch.run(stream.cuda_stream)
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        with ClockSampler(local) as clocks:
+            barrier()
+            t0 = time.perf_counter()
+            for e0, e1 in evs:
+                flush.zero_()
+                e0.record(stream)
+                batch.run(stream.cuda_stream)
+                e1.record(stream)
+            barrier()
+            t1 = time.perf_counter()
+    kernel_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    outs, stats = batch.read()
+    bad = [s["status"] for s in stats if s["status"] != 0]
+    wall = sharding.max_over_ranks(t1 - t0)
+    value = args.instances * world * args.steps / wall
+    ms_per_step = 1000.0 * wall / args.steps
+
+    # end to end through the public host-buffer API
+    h2d, d2h = batch.transfer_bytes()
+    e2e_t = []
+    for _ in range(max(1, min(args.steps, 2))):
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        solver.simulate_batch(models, engine="mixed", deadline_s=600)
+        e2e_t.append(time.perf_counter() - s0)
+    e2e_val = args.instances / statistics.mean(e2e_t)
+
+    # roofline of the integrator kernel (FP32 LU + FP64 refinement)
+    peaks, peak_kind = load_peaks()
+    flops = lu_flops(stats, models, "mixed")
+    k_ms = statistics.mean(kernel_ms)
+    achieved = flops / (k_ms * 1e-3) / 1e12
+    peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": load_traffic(),
+                "kernel": "compat_kernel<float>", "kernel_ms": k_ms,
+                "algorithmic_flops_per_launch": flops,
+                "peak_kind": f"{peak_kind} bf16 sustained"}
+
+    line = {"metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, numpy default_rng(1000*4 + instance))",
+            "config": {"workload": WORKLOAD, "instances_per_gpu": args.instances,
+                       "form": "mixed (FP32 LU + FP64 refinement)",
+                       "parallelism": f"instances sharded over {world} GPU(s)",
+                       "l2": "flushed between steps (256 MB write)"},
+            "failed_instances": len(bad),
+            "e2e": {"value": e2e_val, "unit": "sims/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": batch.launches() * args.steps,
+            "roofline": roofline,
+            "clocks": clocks.summary()}
+
+    if rank == 0 and world == 1 and not args.no_extras:
+        # plain FP64 GPU form vs the mixed form on the same sample
+        sample = [synth.shorten(m, 2.0, 5) for m in models[::13][:152]]
+        res = {}
+        for eng in ("fp64", "mixed"):
+            b = solver.Batch(sample, engine=eng, deadline_s=600)
+            b.run(stream.cuda_stream)
+            b.sync()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                e0.record(stream)
+                b.run(stream.cuda_stream)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            o, st = b.read()
+            res[eng] = (e0.elapsed_time(e1), o, st)
+        worst, nbad = max_rel_err(res["mixed"][1], res["fp64"][1])
+        line["fp64_form"] = {
+            "sample": f"{len(sample)} instances (every 13th), t in [0,2] (0.1 of horizon)",
+            "fp64_ms": res["fp64"][0], "mixed_ms": res["mixed"][0],
+            "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
+            "max_rel_err_vs_fp64": worst, "points_outside_rtol1e-6_atol1e-9": nbad}
+        line["rhs_hbm"] = rhs_bandwidth(torch, stream)
+        line["rhs_hbm"]["frac"] = line["rhs_hbm"]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
+        line["cpu_baseline"] = cpu_baseline(args.instances)
+        line["cpu_baseline"].pop("seconds", None)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -76,6 +76,12 @@ typedef struct {
     int64_t lu_failures;
     int64_t nan_reverts;
     int64_t refine_sweeps;
+    /* SM clock cycles spent (thread 0 of the instance's CTA) in the RKF45
+       attempts, the Newton-matrix assembly, the LU, and the linear solves */
+    int64_t cycles_rkf;
+    int64_t cycles_matrix;
+    int64_t cycles_lu;
+    int64_t cycles_solve;
     double t_final;
     double dt_be_final;
     int32_t status;
@@ -149,6 +155,9 @@ int lassie_batch_read(lassie_batch *batch, const lassie_instance *inst,
                       lassie_stats *stats);
 /* kernel launches one lassie_batch_run issues (for launch accounting) */
 int lassie_batch_launches(const lassie_batch *batch);
+/* bytes lassie_solve_batch moves host->device (inputs) and device->host
+   (trajectories and stats) for this batch */
+int lassie_batch_bytes(const lassie_batch *batch, int64_t *h2d, int64_t *d2h);
 void lassie_batch_destroy(lassie_batch *batch);
 
 /* ---------------------------------------------------- single evaluations */

@@ -27,7 +27,7 @@ EXPORTS = (
     "lassie_model_create_dense", "lassie_model_create_csr", "lassie_model_destroy",
     "lassie_model_info", "lassie_solve", "lassie_solve_batch", "lassie_batch_create",
     "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
-    "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
+    "lassie_batch_bytes", "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
     "lassie_lu_solve",
 )
 
@@ -45,7 +45,9 @@ class Stats(C.Structure):
                 ("rkf_retries", C.c_int64), ("be_steps", C.c_int64),
                 ("newton_iters", C.c_int64), ("lu_factorisations", C.c_int64),
                 ("lu_failures", C.c_int64), ("nan_reverts", C.c_int64),
-                ("refine_sweeps", C.c_int64), ("t_final", C.c_double),
+                ("refine_sweeps", C.c_int64), ("cycles_rkf", C.c_int64),
+                ("cycles_matrix", C.c_int64), ("cycles_lu", C.c_int64),
+                ("cycles_solve", C.c_int64), ("t_final", C.c_double),
                 ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self):
@@ -82,9 +84,8 @@ def load():
     with _lock:
         if _lib is not None:
             return _lib
-        if not os.path.exists(LIB_PATH):
-            from . import build as _build
-            _build.build()
+        from . import build as _build
+        _build.build()  # incremental: a no-op when the library is up to date
         L = C.CDLL(LIB_PATH)
         vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
         L.lassie_opts_default.argtypes = [C.POINTER(Opts)]
@@ -109,6 +110,7 @@ def load():
         L.lassie_batch_sync.argtypes = [vp]
         L.lassie_batch_read.argtypes = [vp, vp, vp]
         L.lassie_batch_launches.argtypes = [vp]
+        L.lassie_batch_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
         L.lassie_batch_destroy.argtypes = [vp]
         L.lassie_batch_destroy.restype = None
         L.lassie_rhs_device.argtypes = [vp, i32, vp, vp, vp, vp]

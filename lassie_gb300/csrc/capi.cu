@@ -415,8 +415,10 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     }
     b->grid = std::max(1, std::min(n, b->sm_count));
     const int lt = o.precision == LASSIE_PREC_FP64 ? 8 : 4;
+    const int64_t dinv_bytes =
+        o.precision == LASSIE_PREC_MIXED ? (int64_t)((b->nmax + 31) / 32) * 2048 * 4 : 0;
     const int64_t ws_stride =
-        ((int64_t)b->nmax * round_up4(b->nmax) * lt + 255) / 256 * 256;
+        ((int64_t)b->nmax * round_up4(b->nmax) * lt + dinv_bytes + 255) / 256 * 256;
     if ((rc = b->d_int.grow(b->n_int * 4)) || (rc = b->d_dbl.grow(b->n_dbl * 8)) ||
         (rc = b->d_out.grow(b->n_out * 8)) ||
         (rc = b->d_desc.grow(std::max<size_t>(1, b->desc.size()) * sizeof(InstDesc))) ||
@@ -474,6 +476,15 @@ extern "C" int lassie_batch_run(lassie_batch *b, void *stream) {
 }
 
 extern "C" int lassie_batch_launches(const lassie_batch *b) { return (b && b->n > 0) ? 1 : 0; }
+
+extern "C" int lassie_batch_bytes(const lassie_batch *b, int64_t *h2d, int64_t *d2h) {
+    if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
+    if (h2d)
+        *h2d = b->n_int * 4 + b->n_dbl * 8 + (int64_t)b->desc.size() * sizeof(InstDesc) +
+               (int64_t)b->order.size() * 4;
+    if (d2h) *d2h = b->n_out * 8 + (int64_t)b->n * sizeof(InstResult);
+    return LASSIE_OK;
+}
 
 extern "C" int lassie_batch_sync(lassie_batch *b) {
     if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
@@ -614,7 +625,8 @@ extern "C" int lassie_lu_solve(int32_t n, const double *a, const double *b, doub
         return set_error(LASSIE_ERR_TOO_LARGE, "lu_solve: n too large for one CTA");
     const int ld = round_up4(n);
     const int lt = precision == LASSIE_PREC_FP64 ? 8 : 4;
-    std::vector<unsigned char> h((size_t)n * ld * lt, 0);
+    const size_t dinv_bytes = lt == 4 ? (size_t)((n + 31) / 32) * 2048 * 4 : 0;
+    std::vector<unsigned char> h((size_t)n * ld * lt + dinv_bytes, 0);
     for (int i = 0; i < n; i++)
         for (int j = 0; j < n; j++) {
             const double v = a[(size_t)i * n + j];

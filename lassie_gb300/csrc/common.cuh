@@ -37,6 +37,7 @@ struct InstDesc {
 struct InstResult {
     int64_t outer_iters, rkf_accepts, rkf_retries, be_steps, newton_iters,
         lu_factorisations, lu_failures, nan_reverts, refine_sweeps;
+    int64_t cycles_rkf, cycles_matrix, cycles_lu, cycles_solve;
     double t_final, dt_be_final;
     int32_t status, pad;
 };
@@ -62,7 +63,7 @@ struct LaunchParams {
 // and device.  Vectors are FP64 N-vectors; the LU panel and U tile are in the
 // factorisation type (PB = panel width).
 struct SmemLayout {
-    int64_t vec, kk, pw, qr, rptr, perm, bvec, panel, utile, total;
+    int64_t vec, kk, pw, qr, rptr, perm, slot, bvec, panel, utile, total;
     __host__ __device__ static int64_t align(int64_t v) { return (v + 15) & ~int64_t(15); }
     __host__ __device__ SmemLayout(int nmax, int rmax, int amax, int lt_bytes, int pb,
                                    int tn) {
@@ -73,6 +74,7 @@ struct SmemLayout {
         qr = o;    o = align(o + int64_t(rmax) * 8);
         rptr = o;  o = align(o + int64_t(rmax + 1) * 4);
         perm = o;  o = align(o + int64_t(nmax) * 4);
+        slot = o;  o = align(o + int64_t(nmax) * 4);
         bvec = o;  o = align(o + int64_t(nmax) * lt_bytes);
         panel = o; o = align(o + int64_t(nmax) * (pb + 1) * lt_bytes);
         utile = o; o = align(o + int64_t(pb) * tn * lt_bytes);

@@ -16,6 +16,7 @@
 // refinement against the matrix-free FP64 product M*v = v - h*J(x)*v.
 #include <cmath>
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -170,7 +171,7 @@ __device__ __forceinline__ double jv_species(const Net &m, int i, const double *
 // Entry (i,g) accumulates, over the reactions of H row i in ascending order,
 // temp = s*k [*a*x_g^(a-1)] * (each other reactant once).
 template <typename LT>
-__device__ void assemble_newton_matrix(const Net &m, const double *x, double h, LT *M,
+__device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *x, double h, LT *M,
                                        int ld) {
     const int N = m.n;
     const int64_t total = (int64_t)N * ld;
@@ -242,13 +243,19 @@ __device__ __forceinline__ Piv piv_better(Piv a, Piv b) {
 // leading dimension ld).  Every element receives a = fma(-l, u, a) once per
 // pivot in pivot order, as in the unblocked algorithm, so the factors equal
 // the oracle's bit for bit.  perm[i] = source row of row i of P*A.
+// slot[N] (shared, scratch) and mv[4*PB] (shared) record the panel's net row
+// moves so that the other columns apply them with independent loads.
 // Returns 0, or j+1 if the pivot of column j is exactly zero (uniform).
 template <typename LT>
-__device__ int lu_factor(LT *M, int ld, int N, int *perm, LT *panel, LT *utile,
-                         double *red, int *ired) {
+__device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot, LT *panel, LT *utile,
+                         double *red, int *ired, int *mv) {
     constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN, PS = PB + 1;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int i = tid; i < N; i += kThreads) perm[i] = i;
+    int *mv_dst = mv, *mv_src = mv + 2 * PB;
+    for (int i = tid; i < N; i += kThreads) {
+        perm[i] = i;
+        slot[i] = -1;
+    }
     __syncthreads();
     int fail = 0;
     for (int j0 = 0; j0 < N; j0 += PB) {
@@ -259,6 +266,7 @@ __device__ int lu_factor(LT *M, int ld, int N, int *perm, LT *panel, LT *utile,
             const int r = idx / PB, c = idx - r * PB;
             panel[r * PS + c] = (c < pb) ? M[(int64_t)(j0 + r) * ld + j0 + c] : LT(0);
         }
+        if (tid == 0) ired[kWarps] = 0;  // number of recorded row moves
         __syncthreads();
         // arg-max of column 0 of the panel
         Piv best{-1.0, 1 << 30};
@@ -299,10 +307,28 @@ __device__ int lu_factor(LT *M, int ld, int N, int *perm, LT *panel, LT *utile,
                     int tmp = perm[j0 + jj];
                     perm[j0 + jj] = perm[j0 + p];
                     perm[j0 + p] = tmp;
+                    // net move list: mv_src[k] = pre-panel row now at mv_dst[k]
+                    int n = ired[kWarps];
+                    int sa = slot[j0 + jj];
+                    if (sa < 0) {
+                        sa = n++;
+                        slot[j0 + jj] = sa;
+                        mv_dst[sa] = j0 + jj;
+                        mv_src[sa] = j0 + jj;
+                    }
+                    int sb = slot[j0 + p];
+                    if (sb < 0) {
+                        sb = n++;
+                        slot[j0 + p] = sb;
+                        mv_dst[sb] = j0 + p;
+                        mv_src[sb] = j0 + p;
+                    }
+                    int t2 = mv_src[sa];
+                    mv_src[sa] = mv_src[sb];
+                    mv_src[sb] = t2;
+                    ired[kWarps] = n;
                 }
             }
-            if (tid == 0) ired[kWarps] = p;  // pivot row for the column swaps
-            if (tid == 0) ired[kWarps + 1 + jj] = p;
             __syncthreads();
             // eliminate below the pivot; fused arg-max for column jj+1
             const LT d = panel[jj * PS + jj];
@@ -325,39 +351,38 @@ __device__ int lu_factor(LT *M, int ld, int N, int *perm, LT *panel, LT *utile,
             const int r = idx / PB, c = idx - r * PB;
             if (c < pb) M[(int64_t)(j0 + r) * ld + j0 + c] = panel[r * PS + c];
         }
-        // columns outside the panel: row swaps in pivot order, then the
-        // unit-lower triangular solve for the U12 block rows.
-        const int* pivrows = ired + kWarps + 1;
+        // columns outside the panel: the panel's row moves (all loads first,
+        // then all stores: the moves form a permutation), then the unit-lower
+        // triangular solve for the U12 block rows.
+        const int nmv = ired[kWarps];
         for (int c = tid; c < N; c += kThreads) {
             if (c >= j0 && c < j0 + pb) continue;
-            for (int jj = 0; jj < pb; jj++) {
-                const int p = pivrows[jj];
-                if (p != jj) {
-                    LT *a = M + (int64_t)(j0 + jj) * ld + c;
-                    LT *b = M + (int64_t)(j0 + p) * ld + c;
-                    LT tmp = *a;
-                    *a = *b;
-                    *b = tmp;
-                }
-            }
+            LT v[2 * PB];
+#pragma unroll
+            for (int k = 0; k < 2 * PB; k++)
+                if (k < nmv) v[k] = M[(int64_t)mv_src[k] * ld + c];
+#pragma unroll
+            for (int k = 0; k < 2 * PB; k++)
+                if (k < nmv) M[(int64_t)mv_dst[k] * ld + c] = v[k];
             if (c >= j0 + pb) {
-                LT v[PB];
+                LT u[PB];
 #pragma unroll
                 for (int r = 0; r < PB; r++)
-                    v[r] = (r < pb) ? M[(int64_t)(j0 + r) * ld + c] : LT(0);
+                    u[r] = (r < pb) ? M[(int64_t)(j0 + r) * ld + c] : LT(0);
 #pragma unroll
                 for (int r = 1; r < PB; r++) {
-                    LT acc = v[r];
+                    LT acc = u[r];
 #pragma unroll
-                    for (int q = 0; q < r; q++) acc = lt_fma(-panel[r * PS + q], v[q], acc);
-                    v[r] = acc;
+                    for (int q = 0; q < r; q++) acc = lt_fma(-panel[r * PS + q], u[q], acc);
+                    u[r] = acc;
                 }
 #pragma unroll
                 for (int r = 1; r < PB; r++)
-                    if (r < pb) M[(int64_t)(j0 + r) * ld + c] = v[r];
+                    if (r < pb) M[(int64_t)(j0 + r) * ld + c] = u[r];
             }
         }
         __syncthreads();
+        for (int k = tid; k < nmv; k += kThreads) slot[mv_dst[k]] = -1;
         // trailing update A22 -= L21 * U12, tiles of 64 x TN
         const int c0 = j0 + pb;
         const int m2 = N - c0;
@@ -417,9 +442,10 @@ __device__ int lu_factor(LT *M, int ld, int N, int *perm, LT *panel, LT *utile,
 
 // Solve (P A) x = P b with the factors in M; b is in bvec (already permuted),
 // overwritten by x.  Forward: ascending accumulation; backward: descending
-// accumulation then one division (the oracle's order).
+// accumulation then one division (the oracle's order).  Used by the FP64
+// form, whose results must equal the oracle's.
 template <typename LT>
-__device__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
+__device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // forward substitution, unit lower
     for (int r0 = 0; r0 < N; r0 += 32) {
@@ -439,9 +465,14 @@ __device__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
         }
         __syncthreads();
         for (int i = r0 + nb + tid; i < N; i += kThreads) {
-            LT acc = bvec[i];
             const LT *ri = M + (int64_t)i * ld + r0;
-            for (int q = 0; q < nb; q++) acc = lt_fma(-ri[q], bvec[r0 + q], acc);
+            LT seg[32];
+#pragma unroll
+            for (int q = 0; q < 32; q++) seg[q] = (q < nb) ? ri[q] : LT(0);
+            LT acc = bvec[i];
+#pragma unroll
+            for (int q = 0; q < 32; q++)
+                if (q < nb) acc = lt_fma(-seg[q], bvec[r0 + q], acc);
             bvec[i] = acc;
         }
         __syncthreads();
@@ -471,10 +502,159 @@ __device__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
         }
         __syncthreads();
         for (int i = tid; i < r0; i += kThreads) {
-            LT acc = bvec[i];
             const LT *ri = M + (int64_t)i * ld + r0;
-            for (int q = nb - 1; q >= 0; q--) acc = lt_fma(-ri[q], bvec[r0 + q], acc);
+            LT seg[32];
+#pragma unroll
+            for (int q = 0; q < 32; q++) seg[q] = (q < nb) ? ri[q] : LT(0);
+            LT acc = bvec[i];
+#pragma unroll
+            for (int q = 31; q >= 0; q--)
+                if (q < nb) acc = lt_fma(-seg[q], bvec[r0 + q], acc);
             bvec[i] = acc;
+        }
+        __syncthreads();
+    }
+}
+
+// FP32 form: inverses of the 32 x 32 diagonal blocks of L (unit lower) and U,
+// dinv[b*2048 + i*32 + j] (L^-1) and dinv[b*2048 + 1024 + i*32 + j] (U^-1);
+// rows/columns past N are identity.  One warp per block, lane j builds
+// column j by substitution on the block rows held in registers.
+__device__ __noinline__ void invert_diag_blocks(const float *M, int ld, int N, float *dinv) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nblk = (N + 31) / 32;
+    for (int b = warp; b < nblk; b += kWarps) {
+        const int r0 = b * 32;
+        const int nb = min(32, N - r0);
+        float row[32];  // row `lane` of the diagonal block (identity past nb)
+#pragma unroll
+        for (int k = 0; k < 32; k++)
+            row[k] = (lane < nb && k < nb) ? M[(int64_t)(r0 + lane) * ld + r0 + k]
+                                          : (lane == k ? 1.f : 0.f);
+        float x[32];
+        // L^-1 column `lane`: unit lower
+#pragma unroll
+        for (int i = 0; i < 32; i++) {
+            float acc = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+            for (int k = 0; k < i; k++)
+                acc = __fmaf_rn(-__shfl_sync(0xffffffffu, row[k], i), x[k], acc);
+            x[i] = acc;
+        }
+        float *Li = dinv + (int64_t)b * 2048;
+#pragma unroll
+        for (int i = 0; i < 32; i++) Li[i * 32 + lane] = x[i];
+        // U^-1 column `lane`: upper
+#pragma unroll
+        for (int i = 31; i >= 0; i--) {
+            float acc = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+            for (int k = i + 1; k < 32; k++)
+                acc = __fmaf_rn(-__shfl_sync(0xffffffffu, row[k], i), x[k], acc);
+            x[i] = acc / __shfl_sync(0xffffffffu, row[i], i);
+        }
+        float *Ui = Li + 1024;
+#pragma unroll
+        for (int i = 0; i < 32; i++) Ui[i * 32 + lane] = x[i];
+    }
+}
+
+// 32 consecutive floats of row r starting at column c0 (c0 % 4 == 0), zero
+// past the leading dimension.
+__device__ __forceinline__ void load_seg32(const float *M, int ld, int r, int c0, float *seg) {
+    const float4 *p = reinterpret_cast<const float4 *>(M + (int64_t)r * ld + c0);
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        float4 v = (c0 + 4 * q < ld) ? p[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+        seg[4 * q] = v.x;
+        seg[4 * q + 1] = v.y;
+        seg[4 * q + 2] = v.z;
+        seg[4 * q + 3] = v.w;
+    }
+}
+
+// FP32 form solve: 32-row block steps; the diagonal blocks are applied as
+// their inverses (one 32 x 32 matvec by warp 0), the off-diagonal rows update
+// with row segments loaded before the block step's barrier.
+__device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const float *dinv, float *bvec) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nblk = (N + 31) / 32;
+    for (int b = 0; b < nblk; b++) {
+        const int r0 = b * 32;
+        const int nb = min(32, N - r0);
+        const int r = r0 + nb + tid;
+        float seg[32];
+        if (r < N) load_seg32(M, ld, r, r0, seg);
+        if (warp == 0) {
+            float li[32];
+            const float4 *lp = reinterpret_cast<const float4 *>(dinv + (int64_t)b * 2048 + lane * 32);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                float4 v = lp[q];
+                li[4 * q] = v.x; li[4 * q + 1] = v.y; li[4 * q + 2] = v.z; li[4 * q + 3] = v.w;
+            }
+            const float bi = (lane < nb) ? bvec[r0 + lane] : 0.f;
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; k++) acc = __fmaf_rn(li[k], __shfl_sync(0xffffffffu, bi, k), acc);
+            if (lane < nb) bvec[r0 + lane] = acc;
+        }
+        __syncthreads();
+        if (r < N) {
+            float acc = bvec[r];
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k < nb) acc = __fmaf_rn(-seg[k], bvec[r0 + k], acc);
+            bvec[r] = acc;
+        }
+        for (int r2 = r + kThreads; r2 < N; r2 += kThreads) {
+            float s2[32];
+            load_seg32(M, ld, r2, r0, s2);
+            float acc = bvec[r2];
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k < nb) acc = __fmaf_rn(-s2[k], bvec[r0 + k], acc);
+            bvec[r2] = acc;
+        }
+        __syncthreads();
+    }
+    for (int b = nblk - 1; b >= 0; b--) {
+        const int r0 = b * 32;
+        const int nb = min(32, N - r0);
+        const int r = tid;
+        float seg[32];
+        if (r < r0) load_seg32(M, ld, r, r0, seg);
+        if (warp == 0) {
+            float ui[32];
+            const float4 *up =
+                reinterpret_cast<const float4 *>(dinv + (int64_t)b * 2048 + 1024 + lane * 32);
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                float4 v = up[q];
+                ui[4 * q] = v.x; ui[4 * q + 1] = v.y; ui[4 * q + 2] = v.z; ui[4 * q + 3] = v.w;
+            }
+            const float bi = (lane < nb) ? bvec[r0 + lane] : 0.f;
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; k++) acc = __fmaf_rn(ui[k], __shfl_sync(0xffffffffu, bi, k), acc);
+            if (lane < nb) bvec[r0 + lane] = acc;
+        }
+        __syncthreads();
+        if (r < r0) {
+            float acc = bvec[r];
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k < nb) acc = __fmaf_rn(-seg[k], bvec[r0 + k], acc);
+            bvec[r] = acc;
+        }
+        for (int r2 = r + kThreads; r2 < r0; r2 += kThreads) {
+            float s2[32];
+            load_seg32(M, ld, r2, r0, s2);
+            float acc = bvec[r2];
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k < nb) acc = __fmaf_rn(-s2[k], bvec[r0 + k], acc);
+            bvec[r2] = acc;
         }
         __syncthreads();
     }
@@ -488,10 +668,17 @@ struct Vecs {
 
 template <typename LT>
 __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, double *red,
-                          int *ired, uint64_t deadline) {
+                          int *ired, int *mv, InstDesc &D, InstResult &st,
+                          uint64_t deadline) {
     constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN;
-    const InstDesc D = P.inst[id];
-    const int N = D.n, R = D.r, tid = threadIdx.x;
+    constexpr bool kMixed = std::is_same<LT, float>::value;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        D = P.inst[id];
+        st = InstResult{};
+    }
+    __syncthreads();
+    const int N = D.n, R = D.r;
     const SmemLayout L(P.nmax, P.rmax, P.amax, (int)sizeof(LT), PB, TN);
     double *vbase = reinterpret_cast<double *>(smem + L.vec);
     Vecs V;
@@ -510,6 +697,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     double *qr = reinterpret_cast<double *>(smem + L.qr);
     int *rptr = reinterpret_cast<int *>(smem + L.rptr);
     int *perm = reinterpret_cast<int *>(smem + L.perm);
+    int *slot = reinterpret_cast<int *>(smem + L.slot);
     LT *bvec = reinterpret_cast<LT *>(smem + L.bvec);
     LT *panel = reinterpret_cast<LT *>(smem + L.panel);
     LT *utile = reinterpret_cast<LT *>(smem + L.utile);
@@ -541,10 +729,12 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     double *out = P.out + D.out;
     LT *M = reinterpret_cast<LT *>(P.workspace + (int64_t)blockIdx.x * P.ws_stride);
     const int ld = round_up4(N);
-    const bool mixed = P.precision == LASSIE_PREC_MIXED;
+    // FP32 form: inverted diagonal blocks of the factors follow the matrix
+    float *dinv = reinterpret_cast<float *>(M + (int64_t)N * ld);
     const int refine_max = P.refine_max > 0 ? P.refine_max : 8;
+    long long c_mark = 0;
 
-    InstResult st{};
+    int64_t outer = 0;  // every thread keeps the loop count (uniform control)
     int status = LASSIE_OK;
     int i = 0;
     double t1 = D.nt > 0 ? tv[0] : 0.0;
@@ -554,11 +744,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     const int nt = D.nt, ncs = D.ncs;
 
     while (i < nt) {
-        if (D.max_steps > 0 && st.outer_iters >= D.max_steps) {
+        if (D.max_steps > 0 && outer >= D.max_steps) {
             status = LASSIE_ERR_MAX_STEPS;
             break;
         }
-        if (deadline && (st.outer_iters & 63) == 0) {
+        if (deadline && (outer & 63) == 0) {
             if (tid == 0) ired[0] = global_ns() > deadline;
             __syncthreads();
             const int expired = ired[0];
@@ -568,7 +758,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 break;
             }
         }
-        st.outer_iters++;
+        outer++;
         // sampling (Simulation.cuh:674-690)
         if (fabs(t1 - t) < 1e-5) {
             for (int j = tid; j < ncs; j += kThreads)
@@ -578,6 +768,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             t1 = tv[i];
         }
         // ---- RKF45 attempt (Simulation.cuh:692-735, kernels.cuh:68-199)
+        c_mark = clock64();
         rhs_phase1(m, V.y1, pw);
         __syncthreads();
         for (int s = tid; s < N; s += kThreads) {
@@ -666,6 +857,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if (delta < dloc) dloc = delta;
         }
         const int all_ok = __syncthreads_and(ok);
+        if (tid == 0) st.cycles_rkf += clock64() - c_mark;
         const int dnan = __syncthreads_or(d0nan);
         double dmin = block_min_nonnan(dloc, red);
         if (dnan) dmin = NAN;  // thrust::min_element keeps a leading NaN
@@ -677,14 +869,14 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if ((t + d_temp) > t1) dt = fabs(t1 - t);
             else dt = d_temp;
             t = t + dt;
-            st.rkf_accepts++;
+            if (tid == 0) st.rkf_accepts++;
             continue;
         }
         // reject (Simulation.cuh:769-921)
         const double dt_old = dt;
         dt = dt * dmin;
         if (!((dt < D.stiffness_tol) | isnan(dt) | isinf(dt) | (fabs(dt_old - dt) < 1e-3))) {
-            st.rkf_retries++;
+            if (tid == 0) st.rkf_retries++;
             continue;
         }
         dt = newDt;
@@ -695,8 +887,16 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         int64_t itN = 0;
         double errN = 1000;
         bool luFail = false;
-        st.be_steps++;
+        if (tid == 0) st.be_steps++;
+        bool expired = false;
         while ((itN < D.newton_iter) & (errN > D.newton_tol)) {
+            if (deadline && (itN & 63) == 63) {
+                if (tid == 0) ired[0] = global_ns() > deadline;
+                __syncthreads();
+                expired = ired[0] != 0;
+                __syncthreads();
+                if (expired) break;
+            }
             // x = f(y_v); x = -(y_v - y1 - h*x)   (kernels.cuh:289-300)
             rhs_phase1(m, yv, pw);
             __syncthreads();
@@ -707,9 +907,18 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
             __syncthreads();
             if (itN == 0) {
+                c_mark = clock64();
                 assemble_newton_matrix<LT>(m, yv, dt, M, ld);
-                st.lu_factorisations++;
-                if (lu_factor<LT>(M, ld, N, perm, panel, utile, red, ired) != 0) luFail = true;
+                const long long c1 = clock64();
+                if (tid == 0) st.cycles_matrix += c1 - c_mark;
+                if (tid == 0) st.lu_factorisations++;
+                if (lu_factor<LT>(M, ld, N, perm, slot, panel, utile, red, ired, mv) != 0)
+                    luFail = true;
+                if constexpr (kMixed) {
+                    if (!luFail) invert_diag_blocks(M, ld, N, dinv);
+                    __syncthreads();
+                }
+                if (tid == 0) st.cycles_lu += clock64() - c1;
             }
             if (luFail) {
                 // Simulation.cuh:869-875, kernels.cuh:512-521
@@ -717,10 +926,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     if (bad_value(yv[s])) yv[s] = V.y1[s];
                 __syncthreads();
                 newDt = dt * 0.1;
-                st.lu_failures++;
+                if (tid == 0) st.lu_failures++;
                 break;
             }
-            if (!mixed) {
+            c_mark = clock64();
+            if constexpr (!kMixed) {
                 for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)xr[perm[s]];
                 __syncthreads();
                 lu_solve<LT>(M, ld, N, bvec);
@@ -737,7 +947,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 for (int sweep = 0; sweep < refine_max; sweep++) {
                     for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)res[perm[s]];
                     __syncthreads();
-                    lu_solve<LT>(M, ld, N, bvec);
+                    lu_solve_fast(M, ld, N, dinv, bvec);
                     double cmax = 0.0, xmax = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
                         const double c = (double)bvec[s];
@@ -746,11 +956,13 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                         cmax = fmax(cmax, fabs(c));
                         xmax = fmax(xmax, fabs(nx));
                     }
-                    st.refine_sweeps++;
+                    if (tid == 0) st.refine_sweeps++;
                     cmax = block_max(cmax, red);
                     xmax = block_max(xmax, red);
+                    // stop when this correction, or the next one predicted from
+                    // the contraction so far, is below FP64 resolution of dx
                     if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) ||
-                        sweep + 1 == refine_max)
+                        !(cmax * (cmax / prev) > 1e-16 * xmax) || sweep + 1 == refine_max)
                         break;
                     prev = cmax;
                     // res = xr - (dx - h*J(xf)*dx)
@@ -763,6 +975,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     __syncthreads();
                 }
             }
+            if (tid == 0) st.cycles_solve += clock64() - c_mark;
             // y_v += dx; dx = y_v - y_v_old (kernels.cuh:462-477); ||dx|| with
             // FP32-rounded squares (Simulation.cuh:58-64, 883-890)
             double sq = 0.0;
@@ -776,7 +989,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
             errN = sqrt(block_sum(sq, red));
             itN = itN + 1;
-            st.newton_iters++;
+            if (tid == 0) st.newton_iters++;
         }
         if (!luFail) {
             // Simulation.cuh:894-909
@@ -786,10 +999,14 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 for (int s = tid; s < N; s += kThreads)
                     if (bad_value(yv[s])) yv[s] = V.y1[s];
                 newDt = dt * 0.1;
-                st.nan_reverts++;
+                if (tid == 0) st.nan_reverts++;
             }
         }
         __syncthreads();
+        if (expired) {
+            status = LASSIE_ERR_DEADLINE;
+            break;
+        }
         double *tmp = V.y1;
         V.y1 = V.k2;
         V.k2 = tmp;
@@ -797,6 +1014,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     }
     __syncthreads();
     if (tid == 0) {
+        st.outer_iters = outer;
         st.t_final = t;
         st.dt_be_final = newDt;
         st.status = status;
@@ -810,6 +1028,9 @@ __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double red[kWarps + 1];
     __shared__ int ired[kWarps + 2 + LuShape<LT>::PB];
+    __shared__ int mv[4 * LuShape<LT>::PB];
+    __shared__ InstDesc D;
+    __shared__ InstResult st;
     __shared__ int next;
     __shared__ uint64_t start;
     if (threadIdx.x == 0) start = global_ns();
@@ -821,7 +1042,7 @@ __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
         const int q = next;
         __syncthreads();
         if (q >= P.n_inst) break;
-        integrate<LT>(P, P.order[q], smem, red, ired, deadline);
+        integrate<LT>(P, P.order[q], smem, red, ired, mv, D, st, deadline);
     }
 }
 
@@ -948,16 +1169,25 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
     constexpr int PB = LuShape<LT>::PB;
     __shared__ double red[kWarps + 1];
     __shared__ int ired[kWarps + 2 + PB];
+    __shared__ int mv[4 * PB];
     int *perm = reinterpret_cast<int *>(smem);
-    LT *bvec = reinterpret_cast<LT *>(smem + SmemLayout::align(int64_t(N) * 4));
+    int *slot = perm + round_up4(N);
+    LT *bvec = reinterpret_cast<LT *>(smem + SmemLayout::align(int64_t(round_up4(N)) * 8));
     LT *panel = bvec + round_up4(N);
     LT *utile = panel + (int64_t)N * (PB + 1);
-    const int fail = lu_factor<LT>(A, ld, N, perm, panel, utile, red, ired);
+    const int fail = lu_factor<LT>(A, ld, N, perm, slot, panel, utile, red, ired, mv);
     if (threadIdx.x == 0) *info = fail;
     if (fail) return;
     for (int s = threadIdx.x; s < N; s += kThreads) bvec[s] = (LT)b[perm[s]];
     __syncthreads();
-    lu_solve<LT>(A, ld, N, bvec);
+    if constexpr (std::is_same<LT, float>::value) {
+        float *dinv = A + (int64_t)N * ld;
+        invert_diag_blocks(A, ld, N, dinv);
+        __syncthreads();
+        lu_solve_fast(A, ld, N, dinv, bvec);
+    } else {
+        lu_solve<LT>(A, ld, N, bvec);
+    }
     for (int s = threadIdx.x; s < N; s += kThreads) x[s] = (double)bvec[s];
 }
 
@@ -965,7 +1195,7 @@ int64_t lu_solve_smem(int N, int precision) {
     const int lt = precision == LASSIE_PREC_FP64 ? 8 : 4;
     const int PB = precision == LASSIE_PREC_FP64 ? LuShape<double>::PB : LuShape<float>::PB;
     const int TN = 128;
-    return SmemLayout::align(int64_t(N) * 4) + int64_t(round_up4(N)) * lt +
+    return SmemLayout::align(int64_t(round_up4(N)) * 8) + int64_t(round_up4(N)) * lt +
            int64_t(N) * (PB + 1) * lt + int64_t(PB) * TN * lt + 64;
 }
 

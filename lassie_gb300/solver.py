@@ -156,6 +156,12 @@ class Batch:
     def launches(self) -> int:
         return int(nat.load().lassie_batch_launches(self.handle))
 
+    def transfer_bytes(self) -> Tuple[int, int]:
+        h2d, d2h = C.c_int64(), C.c_int64()
+        nat.check(nat.load().lassie_batch_bytes(self.handle, C.byref(h2d), C.byref(d2h)),
+                  "lassie_batch_bytes")
+        return int(h2d.value), int(d2h.value)
+
     def read(self) -> Tuple[List[np.ndarray], List[Dict]]:
         stats = (nat.Stats * max(self.n, 1))()
         rc = nat.load().lassie_batch_read(self.handle, C.cast(self._inst, C.c_void_p),

@@ -1,7 +1,8 @@
 /*
  * ref_prelude.h -- TEST INFRASTRUCTURE.  Force-included (nvcc -include) when
  * the unmodified LASSIE sources are compiled into oracle/_ref/lassie_ref.
- * It makes the sources compile with nvcc 13 / g++ 13 without editing them:
+ * It makes the sources compile with nvcc 13 / g++ 13, and run, without
+ * editing them:
  *   1. Simulation.cuh:79 takes the address of `ostringstream() << num`, an
  *      rvalue with the C++11 rvalue-stream operator; a stream type whose own
  *      member operator<<(int) returns an lvalue restores the C++03 meaning.
@@ -30,6 +31,30 @@ struct lassie_ref_oss : public std::ostringstream {
     }
 };
 #define ostringstream lassie_ref_oss
+
+/* 3. Simulation.cuh:739,753,773,883,898 construct thrust::device_vector from
+      raw device pointers.  Thrust takes a raw pointer for a host iterator, so
+      the host dereferences device memory (and converts int -> short element
+      by element on the host) and the process dies with SIGSEGV.  A
+      device_vector whose range constructor wraps the pointers with
+      device_pointer_cast gives the intended device-to-device copy. */
+#include <thrust/count.h>
+#include <thrust/device_ptr.h>
+#include <thrust/device_vector.h>
+#include <thrust/extrema.h>
+#include <thrust/functional.h>
+#include <thrust/host_vector.h>
+#include <thrust/transform_reduce.h>
+namespace thrust {
+template <class T>
+struct lassie_ref_device_vector : public thrust::device_vector<T> {
+    template <class U>
+    lassie_ref_device_vector(U *first, U *last)
+        : thrust::device_vector<T>(thrust::device_pointer_cast(first),
+                                   thrust::device_pointer_cast(last)) {}
+};
+}  // namespace thrust
+#define device_vector lassie_ref_device_vector
 
 #ifdef LASSIE_REF_FULL_DIGITS
 static inline int lassie_ref_fprintf(FILE *f, const char *fmt, ...) {
