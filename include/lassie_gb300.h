@@ -63,7 +63,15 @@ typedef struct {
     double deadline_s;    /* device wall-clock limit per launch, 0 = none */
     int32_t precision;    /* LASSIE_PREC_* */
     int32_t refine_max;   /* refinement sweeps per linear solve (mixed), 0 = 8 */
+    int32_t quarter_root; /* RKF45 step factor (atol/R)^(1/4): LASSIE_ROOT_POW
+                             = pow(x, 0.25) as kernels.cuh:193 (default);
+                             LASSIE_ROOT_SQRT = sqrt(sqrt(x)), correctly rounded
+                             on every platform (matches the CPU restatement) */
+    int32_t pad;
 } lassie_opts;
+
+#define LASSIE_ROOT_POW 0
+#define LASSIE_ROOT_SQRT 1
 
 /* Per-instance counters; status is the instance's LASSIE_* result. */
 typedef struct {

@@ -20,6 +20,8 @@ ERR_NO_DEVICE = -25
 ERR_CUDA = -13
 PREC_FP64 = 0
 PREC_MIXED = 1
+ROOT_POW = 0
+ROOT_SQRT = 1
 
 # every function the header declares (checked by the CPU test suite)
 EXPORTS = (
@@ -37,7 +39,7 @@ class Opts(C.Structure):
                 ("newton_tol", C.c_double), ("stiffness_tol", C.c_double),
                 ("newton_iter", C.c_int64), ("max_steps", C.c_int64),
                 ("deadline_s", C.c_double), ("precision", C.c_int32),
-                ("refine_max", C.c_int32)]
+                ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("pad", C.c_int32)]
 
 
 class Stats(C.Structure):

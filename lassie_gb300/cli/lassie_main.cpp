@@ -1,5 +1,5 @@
 // `lassie input_folder output_folder [-v1|-v2|-v3] [-p double|float]
-//        [-engine mixed|fp64] [-dump-f64] [-stats]`
+//        [-engine mixed|fp64] [-root pow|sqrt] [-dump-f64] [-stats]`
 //
 // Drop-in host for the reference CLI (src/c++/simulator.cu:29-319): the same
 // input-folder files and parsing (src/c++/header/Reader.h:23-134), defaults
@@ -174,7 +174,7 @@ int main(int argc, char *argv[]) {
     int verbose = 0;
     std::string prec = "double";
     std::string engine = "mixed";
-    bool dump_f64 = false, want_stats = false;
+    bool dump_f64 = false, want_stats = false, root_sqrt = false;
     for (int i = 3; i < argc; i++) {
         const std::string a = argv[i];
         if (a == "-v1") verbose = 1;
@@ -190,6 +190,11 @@ int main(int argc, char *argv[]) {
             engine = argv[i + 1];
             if (engine != "mixed" && engine != "fp64")
                 fail(-6, "Error: the engine must be mixed or fp64");
+        }
+        if (a == "-root" && i + 1 < argc) {
+            const std::string r = argv[i + 1];
+            if (r != "pow" && r != "sqrt") fail(-6, "Error: the root must be pow or sqrt");
+            root_sqrt = r == "sqrt";
         }
         if (a == "-dump-f64") dump_f64 = true;
         if (a == "-stats") want_stats = true;
@@ -207,6 +212,7 @@ int main(int argc, char *argv[]) {
     lassie_opts opts;
     lassie_opts_default(&opts);
     opts.precision = engine == "fp64" ? LASSIE_PREC_FP64 : LASSIE_PREC_MIXED;
+    opts.quarter_root = root_sqrt ? LASSIE_ROOT_SQRT : LASSIE_ROOT_POW;
     if (files.count("be_step")) opts.be_step = read_single(files["be_step"]);
     if (files.count("rkf_step")) opts.rkf_step = read_single(files["rkf_step"]);
     if (files.count("newton_iter")) opts.newton_iter = (int64_t)(int)read_single(files["newton_iter"]);

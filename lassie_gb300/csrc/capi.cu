@@ -17,7 +17,7 @@
 #include "lassie_gb300.h"
 
 namespace lassie {
-int64_t compat_smem_bytes(int nmax, int rmax, int amax, int precision);
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision);
 cudaError_t compat_configure(int precision, int64_t smem);
 cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
 cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, const int *rptr,
@@ -209,6 +209,8 @@ extern "C" void lassie_opts_default(lassie_opts *o) {
     o->deadline_s = 0.0;
     o->precision = LASSIE_PREC_MIXED;
     o->refine_max = 0;
+    o->quarter_root = LASSIE_ROOT_POW;
+    o->pad = 0;
 }
 
 extern "C" const char *lassie_status_string(int s) {
@@ -279,7 +281,7 @@ struct lassie_batch {
     std::vector<InstDesc> desc;
     std::vector<int32_t> order;
     int64_t n_int = 0, n_dbl = 0, n_out = 0;
-    int32_t nmax = 0, rmax = 0, amax = 0;
+    int32_t nmax = 0, rmax = 0, amax = 0, hmax = 0;
     int64_t smem = 0;
     int grid = 0;
     DevBuf d_int, d_dbl, d_out, d_desc, d_order, d_res, d_queue, d_ws;
@@ -391,9 +393,11 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         D.stiffness_tol = o.stiffness_tol;
         D.newton_iter = o.newton_iter;
         D.max_steps = o.max_steps;
+        D.flags = o.quarter_root == LASSIE_ROOT_SQRT ? 1 : 0;
         b->nmax = std::max(b->nmax, m->N);
         b->rmax = std::max(b->rmax, m->R);
         b->amax = std::max(b->amax, (int32_t)m->rxn_ent.size());
+        b->hmax = std::max(b->hmax, (int32_t)m->sp_ent.size());
     }
     if (hdbl.empty()) hdbl.push_back(0.0);
     if (hint.empty()) hint.push_back(0);
@@ -405,7 +409,12 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     std::iota(b->order.begin(), b->order.end(), 0);
     std::stable_sort(b->order.begin(), b->order.end(),
                      [&](int a, int c) { return b->desc[a].n > b->desc[c].n; });
-    b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, o.precision);
+    if (b->nmax > kThreads) {
+        delete b;
+        return set_error(LASSIE_ERR_TOO_LARGE, "the batched engine takes networks of at most " +
+                                                   std::to_string(kThreads) + " species");
+    }
+    b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax, o.precision);
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
     if (n > 0 && b->smem > max_optin - 1024) {
@@ -459,6 +468,7 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     P.nmax = b->nmax;
     P.rmax = b->rmax;
     P.amax = b->amax;
+    P.hmax = b->hmax;
     P.precision = o.precision;
     P.refine_max = o.refine_max;
     P.deadline_ns = o.deadline_s > 0 ? (uint64_t)(o.deadline_s * 1e9) : 0;
@@ -621,7 +631,7 @@ extern "C" int lassie_lu_solve(int32_t n, const double *a, const double *b, doub
     int dev = 0, max_optin = 0;
     CU(cudaGetDevice(&dev));
     CU(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    if (lu_solve_smem(n, precision) > max_optin - 1024)
+    if (n > kThreads || lu_solve_smem(n, precision) > max_optin - 1024)
         return set_error(LASSIE_ERR_TOO_LARGE, "lu_solve: n too large for one CTA");
     const int ld = round_up4(n);
     const int lt = precision == LASSIE_PREC_FP64 ? 8 : 4;

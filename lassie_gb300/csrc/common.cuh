@@ -54,30 +54,36 @@ struct LaunchParams {
     InstResult *res;
     unsigned char *workspace;  // per-CTA Newton matrix
     int64_t ws_stride;         // bytes per CTA
-    int32_t nmax, rmax, amax;  // largest N, R, nnz_A in the batch
+    int32_t nmax, rmax, amax, hmax;  // largest N, R, nnz_A, nnz_H in the batch
     int32_t precision, refine_max;
     uint64_t deadline_ns;      // per-launch wall-clock limit (ns), 0 = none
 };
 
 // Dynamic shared-memory layout of the integrator (bytes), identical on host
-// and device.  Vectors are FP64 N-vectors; the LU panel and U tile are in the
-// factorisation type (PB = panel width).
+// and device.  Vectors are FP64 N-vectors; the sparse structure of the
+// network is staged here too; lt holds the factor panel transposed
+// (PB x round_up4(N), plus slack for the 8-row tile reads past its end),
+// utile one PB x 128 tile of U12, rowbuf the pivot and swap rows.
 struct SmemLayout {
-    int64_t vec, kk, pw, qr, rptr, perm, slot, bvec, panel, utile, total;
+    int64_t vec, kk, pw, qr, rptr, sptr, sent, rent, perm, slot, bvec, lt, utile, rowbuf, total;
     __host__ __device__ static int64_t align(int64_t v) { return (v + 15) & ~int64_t(15); }
-    __host__ __device__ SmemLayout(int nmax, int rmax, int amax, int lt_bytes, int pb,
+    __host__ __device__ SmemLayout(int nmax, int rmax, int amax, int hmax, int lt_bytes, int pb,
                                    int tn) {
         int64_t o = 0;
-        vec = o;   o = align(o + int64_t(10) * nmax * 8);
-        kk = o;    o = align(o + int64_t(rmax) * 8);
-        pw = o;    o = align(o + int64_t(amax > 0 ? amax : 1) * 8);
-        qr = o;    o = align(o + int64_t(rmax) * 8);
-        rptr = o;  o = align(o + int64_t(rmax + 1) * 4);
-        perm = o;  o = align(o + int64_t(nmax) * 4);
-        slot = o;  o = align(o + int64_t(nmax) * 4);
-        bvec = o;  o = align(o + int64_t(nmax) * lt_bytes);
-        panel = o; o = align(o + int64_t(nmax) * (pb + 1) * lt_bytes);
-        utile = o; o = align(o + int64_t(pb) * tn * lt_bytes);
+        vec = o;    o = align(o + int64_t(10) * nmax * 8);
+        kk = o;     o = align(o + int64_t(rmax) * 8);
+        pw = o;     o = align(o + int64_t(amax > 0 ? amax : 1) * 8);
+        qr = o;     o = align(o + int64_t(rmax) * 8);
+        rptr = o;   o = align(o + int64_t(rmax + 1) * 4);
+        sptr = o;   o = align(o + int64_t(nmax + 1) * 4);
+        sent = o;   o = align(o + int64_t(hmax > 0 ? hmax : 1) * 4);
+        rent = o;   o = align(o + int64_t(amax > 0 ? amax : 1) * 4);
+        perm = o;   o = align(o + int64_t(nmax) * 4);
+        slot = o;   o = align(o + int64_t(nmax) * 4);
+        bvec = o;   o = align(o + int64_t(nmax) * lt_bytes);
+        lt = o;     o = align(o + (int64_t(pb) * ((nmax + 3) & ~3) + 160) * lt_bytes);
+        utile = o;  o = align(o + int64_t(pb) * tn * lt_bytes);
+        rowbuf = o; o = align(o + int64_t(2 * pb) * lt_bytes);
         total = o;
     }
 };

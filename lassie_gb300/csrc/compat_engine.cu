@@ -98,9 +98,9 @@ __device__ double block_min_nonnan(double v, double *red) {
 
 struct Net {
     int n, r, nnz_a;
-    const int *__restrict__ rent;  // reactant entries (global)
-    const int *__restrict__ sptr;  // species row pointers (global)
-    const int *__restrict__ sent;  // species entries (global)
+    const int *rent;  // reactant entries
+    const int *sptr;  // species row pointers
+    const int *sent;  // species entries
     const int *rptr;               // reaction pointers (shared)
     const double *kk;              // rate constants (shared)
 };
@@ -108,7 +108,7 @@ struct Net {
 // RHS phase 1: pw[q] = x_s^a for every reactant entry q.
 __device__ __forceinline__ void rhs_phase1(const Net &m, const double *x, double *pw) {
     for (int q = threadIdx.x; q < m.nnz_a; q += kThreads) {
-        const int e = __ldg(m.rent + q);
+        const int e = m.rent[q];
         pw[q] = mypow(x[ent_index(e)], ent_coef(e));
     }
 }
@@ -119,9 +119,9 @@ __device__ __forceinline__ void rhs_phase1(const Net &m, const double *x, double
 // this only in the sign of a zero, which cannot change the sum.
 __device__ __forceinline__ double rhs_species(const Net &m, int i, const double *pw) {
     double acc = 0.0;
-    const int e0 = __ldg(m.sptr + i), e1 = __ldg(m.sptr + i + 1);
+    const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
     for (int e = e0; e < e1; e++) {
-        const int ent = __ldg(m.sent + e);
+        const int ent = m.sent[e];
         const int y = ent_index(ent);
         double v = (double)ent_coef(ent) * m.kk[y];
         const int b = m.rptr[y], en = m.rptr[y + 1];
@@ -140,14 +140,14 @@ __device__ void jv_phase1(const Net &m, const double *x, const double *v, double
         const int b = m.rptr[y], en = m.rptr[y + 1];
         double q = 0.0;
         for (int j = b; j < en; j++) {
-            const int ej = __ldg(m.rent + j);
+            const int ej = m.rent[j];
             const int g = ent_index(ej), a = ent_coef(ej);
             double d;
             if (a == 1) d = m.kk[y];
             else if (a > 1) d = m.kk[y] * (double)a * mypow(x[g], a - 1);
             else continue;
             for (int jj = b; jj < en; jj++) {
-                const int o = ent_index(__ldg(m.rent + jj));
+                const int o = ent_index(m.rent[jj]);
                 if (o != g) d = d * x[o];
             }
             q = fma(d, v[g], q);
@@ -158,9 +158,9 @@ __device__ void jv_phase1(const Net &m, const double *x, const double *v, double
 
 __device__ __forceinline__ double jv_species(const Net &m, int i, const double *qr) {
     double acc = 0.0;
-    const int e0 = __ldg(m.sptr + i), e1 = __ldg(m.sptr + i + 1);
+    const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
     for (int e = e0; e < e1; e++) {
-        const int ent = __ldg(m.sent + e);
+        const int ent = m.sent[e];
         acc = fma((double)ent_coef(ent), qr[ent_index(ent)], acc);
     }
     return acc;
@@ -174,36 +174,36 @@ template <typename LT>
 __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *x, double h, LT *M,
                                        int ld) {
     const int N = m.n;
-    const int64_t total = (int64_t)N * ld;
-    for (int64_t idx = threadIdx.x; idx < total; idx += kThreads) {
-        const int row = (int)(idx / ld), col = (int)(idx - (int64_t)row * ld);
-        M[idx] = (row == col) ? LT(1) : LT(0);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int row = warp; row < N; row += kWarps) {
+        LT *Mr = M + (int64_t)row * ld;
+        for (int col = lane; col < ld; col += 32) Mr[col] = (row == col) ? LT(1) : LT(0);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += kThreads) {
-        const int e0 = __ldg(m.sptr + i), e1 = __ldg(m.sptr + i + 1);
+        const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
         for (int e = e0; e < e1; e++) {
-            const int y = ent_index(__ldg(m.sent + e));
+            const int y = ent_index(m.sent[e]);
             const int b = m.rptr[y], en = m.rptr[y + 1];
             for (int q = b; q < en; q++) {
-                const int g = ent_index(__ldg(m.rent + q));
+                const int g = ent_index(m.rent[q]);
                 // skip columns already produced by an earlier reaction of row i
                 bool seen = false;
                 for (int ep = e0; ep < e && !seen; ep++) {
-                    const int yp = ent_index(__ldg(m.sent + ep));
+                    const int yp = ent_index(m.sent[ep]);
                     for (int qp = m.rptr[yp]; qp < m.rptr[yp + 1]; qp++)
-                        if (ent_index(__ldg(m.rent + qp)) == g) { seen = true; break; }
+                        if (ent_index(m.rent[qp]) == g) { seen = true; break; }
                 }
                 if (seen) continue;
                 double J = 0.0;
                 for (int e2 = e; e2 < e1; e2++) {
-                    const int ent2 = __ldg(m.sent + e2);
+                    const int ent2 = m.sent[e2];
                     const int y2 = ent_index(ent2), s2 = ent_coef(ent2);
                     const int b2 = m.rptr[y2], en2 = m.rptr[y2 + 1];
                     int a = 0;
                     bool has = false;
                     for (int q2 = b2; q2 < en2; q2++) {
-                        const int ee = __ldg(m.rent + q2);
+                        const int ee = m.rent[q2];
                         if (ent_index(ee) == g) { a = ent_coef(ee); has = true; break; }
                     }
                     if (!has) continue;
@@ -213,7 +213,7 @@ __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *
                         temp = temp + (double)s2 * m.kk[y2] * (double)a * mypow(x[g], a - 1);
                     else continue;
                     for (int q2 = b2; q2 < en2; q2++) {
-                        const int o = ent_index(__ldg(m.rent + q2));
+                        const int o = ent_index(m.rent[q2]);
                         if (o != g) temp = temp * x[o];
                     }
                     J = J + temp;
@@ -239,19 +239,54 @@ __device__ __forceinline__ Piv piv_better(Piv a, Piv b) {
     return a;
 }
 
+// 8 consecutive LT from 16-byte aligned shared or global memory.
+__device__ __forceinline__ void load8(const float *p, float *o) {
+    const float4 a = reinterpret_cast<const float4 *>(p)[0];
+    const float4 b = reinterpret_cast<const float4 *>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+    o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+}
+__device__ __forceinline__ void load8(const double *p, double *o) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const double2 v = reinterpret_cast<const double2 *>(p)[q];
+        o[2 * q] = v.x;
+        o[2 * q + 1] = v.y;
+    }
+}
+__device__ __forceinline__ void load4(const float *p, float *o) {
+    const float4 a = reinterpret_cast<const float4 *>(p)[0];
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+}
+__device__ __forceinline__ void load4(const double *p, double *o) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[0];
+    const double2 b = reinterpret_cast<const double2 *>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+
 // In-place blocked right-looking LU with partial pivoting on M (row-major,
-// leading dimension ld).  Every element receives a = fma(-l, u, a) once per
-// pivot in pivot order, as in the unblocked algorithm, so the factors equal
-// the oracle's bit for bit.  perm[i] = source row of row i of P*A.
-// slot[N] (shared, scratch) and mv[4*PB] (shared) record the panel's net row
-// moves so that the other columns apply them with independent loads.
-// Returns 0, or j+1 if the pivot of column j is exactly zero (uniform).
+// leading dimension ld), N <= kThreads.  Every element receives
+// a = fma(-l, u, a) once per pivot in pivot order, as in the unblocked
+// algorithm, so the factors equal the oracle's bit for bit.
+//   panel: thread r holds row j0+r of the PB-column panel in registers; per
+//          pivot one barrier publishes the arg-max partials and one the pivot
+//          row (row interchanges are register swaps through shared memory);
+//   other columns: the panel's net row moves (recorded by thread 0 in
+//          slot/mv) with independent loads, then the unit-lower solve for
+//          the U12 rows (L11 from shared memory);
+//   trailing update: 128 x 128 tiles, thread (ty,tx) owns rows ty*8.. and
+//          columns tx*4..; L21 is kept transposed in shared memory (lt) and
+//          U12 is staged per column tile (utile), both read with 16-byte loads.
+// perm[i] = source row of row i of P*A.  Returns 0, or j+1 if the pivot of
+// column j is exactly zero (uniform across the CTA).
 template <typename LT>
-__device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot, LT *panel, LT *utile,
-                         double *red, int *ired, int *mv) {
-    constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN, PS = PB + 1;
+__device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot, LT *lt,
+                                      LT *utile, LT *rowbuf, double *red, int *ired, int *mv) {
+    constexpr int PB = LuShape<LT>::PB;
+    constexpr int TN = 128, TM = 128;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     int *mv_dst = mv, *mv_src = mv + 2 * PB;
+    LT *pivrow = rowbuf, *swaprow = rowbuf + PB;
     for (int i = tid; i < N; i += kThreads) {
         perm[i] = i;
         slot[i] = -1;
@@ -261,49 +296,46 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
     for (int j0 = 0; j0 < N; j0 += PB) {
         const int pb = min(PB, N - j0);
         const int m = N - j0;
-        // load panel rows j0..N-1, columns j0..j0+pb-1
-        for (int idx = tid; idx < m * PB; idx += kThreads) {
-            const int r = idx / PB, c = idx - r * PB;
-            panel[r * PS + c] = (c < pb) ? M[(int64_t)(j0 + r) * ld + j0 + c] : LT(0);
-        }
+        const int mp = round_up4(m);
+        const bool mine = tid < m;
+        LT row[PB];
+#pragma unroll
+        for (int c = 0; c < PB; c++)
+            row[c] = (mine && c < pb) ? M[(int64_t)(j0 + tid) * ld + j0 + c] : LT(0);
         if (tid == 0) ired[kWarps] = 0;  // number of recorded row moves
-        __syncthreads();
-        // arg-max of column 0 of the panel
         Piv best{-1.0, 1 << 30};
-        for (int r = tid; r < m; r += kThreads) {
-            double v = fabs((double)panel[r * PS]);
-            if (!isnan(v)) best = piv_better(best, Piv{v, r});
+        if (mine) {
+            const double v = fabs((double)row[0]);
+            if (!isnan(v)) best = Piv{v, tid};
         }
-        for (int jj = 0; jj < pb; jj++) {
-            // combine partial arg-max for column jj
-            for (int o = 16; o > 0; o >>= 1) {
-                Piv other{__shfl_xor_sync(0xffffffffu, best.v, o),
-                          __shfl_xor_sync(0xffffffffu, best.i, o)};
-                best = piv_better(best, other);
-            }
-            if (lane == 0) {
-                red[warp] = best.v;
-                ired[warp] = best.i;
-            }
-            __syncthreads();
-            Piv all{red[0], ired[0]};
-            for (int q = 1; q < kWarps; q++) all = piv_better(all, Piv{red[q], ired[q]});
-            int p = all.i;
-            // a NaN in the diagonal position keeps its own row (oracle rule)
-            if (isnan((double)panel[jj * PS + jj]) || p >= m) p = jj;
-            const LT pv = panel[p * PS + jj];
-            if (pv == LT(0)) {
-                fail = j0 + jj + 1;
-                break;
-            }
-            __syncthreads();  // everyone has read red/ired and the pivot
-            if (p != jj) {
-                for (int c = tid; c < PB; c += kThreads) {
-                    LT tmp = panel[jj * PS + c];
-                    panel[jj * PS + c] = panel[p * PS + c];
-                    panel[p * PS + c] = tmp;
+#pragma unroll
+        for (int jj = 0; jj < PB; jj++) {
+            if (jj < pb) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    Piv other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                              __shfl_xor_sync(0xffffffffu, best.i, o)};
+                    best = piv_better(best, other);
                 }
-                if (tid == 0) {
+                if (lane == 0) {
+                    red[warp] = best.v;
+                    ired[warp] = best.i;
+                }
+                if (tid == jj) ired[kWarps + 1] = isnan((double)row[jj]) ? 1 : 0;
+                __syncthreads();
+                Piv all{red[0], ired[0]};
+                for (int q = 1; q < kWarps; q++) all = piv_better(all, Piv{red[q], ired[q]});
+                int p = all.i;
+                // a NaN in the diagonal position keeps its own row (oracle rule)
+                if (ired[kWarps + 1] || p >= m) p = jj;
+                if (tid == p) {
+#pragma unroll
+                    for (int c = 0; c < PB; c++) pivrow[c] = row[c];
+                }
+                if (tid == jj && p != jj) {
+#pragma unroll
+                    for (int c = 0; c < PB; c++) swaprow[c] = row[c];
+                }
+                if (tid == 0 && p != jj) {
                     int tmp = perm[j0 + jj];
                     perm[j0 + jj] = perm[j0 + p];
                     perm[j0 + p] = tmp;
@@ -328,29 +360,44 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
                     mv_src[sb] = t2;
                     ired[kWarps] = n;
                 }
-            }
-            __syncthreads();
-            // eliminate below the pivot; fused arg-max for column jj+1
-            const LT d = panel[jj * PS + jj];
-            best = Piv{-1.0, 1 << 30};
-            for (int r = jj + 1 + tid; r < m; r += kThreads) {
-                const LT l = panel[r * PS + jj] / d;
-                panel[r * PS + jj] = l;
-                for (int c = jj + 1; c < pb; c++)
-                    panel[r * PS + c] = lt_fma(-l, panel[jj * PS + c], panel[r * PS + c]);
-                if (jj + 1 < pb) {
-                    double v = fabs((double)panel[r * PS + jj + 1]);
-                    if (!isnan(v)) best = piv_better(best, Piv{v, r});
+                __syncthreads();
+                const LT pv = pivrow[jj];
+                if (pv == LT(0)) {
+                    fail = j0 + jj + 1;
+                    break;
+                }
+                if (p != jj) {
+                    if (tid == jj) {
+#pragma unroll
+                        for (int c = 0; c < PB; c++) row[c] = pivrow[c];
+                    } else if (tid == p) {
+#pragma unroll
+                        for (int c = 0; c < PB; c++) row[c] = swaprow[c];
+                    }
+                }
+                best = Piv{-1.0, 1 << 30};
+                if (mine && tid > jj) {
+                    const LT l = row[jj] / pv;
+                    row[jj] = l;
+#pragma unroll
+                    for (int c = jj + 1; c < PB; c++) row[c] = lt_fma(-l, pivrow[c], row[c]);
+                    if (jj + 1 < pb) {
+                        const double v = fabs((double)row[jj + 1]);
+                        if (!isnan(v)) best = Piv{v, tid};
+                    }
                 }
             }
-            __syncthreads();
         }
         if (fail) break;
-        // write the panel back
-        for (int idx = tid; idx < m * PB; idx += kThreads) {
-            const int r = idx / PB, c = idx - r * PB;
-            if (c < pb) M[(int64_t)(j0 + r) * ld + j0 + c] = panel[r * PS + c];
+        // panel back to global; L (and U11) transposed into lt[c*mp + r]
+        if (mine) {
+#pragma unroll
+            for (int c = 0; c < PB; c++) {
+                if (c < pb) M[(int64_t)(j0 + tid) * ld + j0 + c] = row[c];
+                lt[c * mp + tid] = row[c];
+            }
         }
+        __syncthreads();
         // columns outside the panel: the panel's row moves (all loads first,
         // then all stores: the moves form a permutation), then the unit-lower
         // triangular solve for the U12 block rows.
@@ -364,6 +411,9 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
 #pragma unroll
             for (int k = 0; k < 2 * PB; k++)
                 if (k < nmv) M[(int64_t)mv_dst[k] * ld + c] = v[k];
+        }
+        __syncthreads();
+        for (int c = tid; c < N; c += kThreads) {
             if (c >= j0 + pb) {
                 LT u[PB];
 #pragma unroll
@@ -373,7 +423,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
                 for (int r = 1; r < PB; r++) {
                     LT acc = u[r];
 #pragma unroll
-                    for (int q = 0; q < r; q++) acc = lt_fma(-panel[r * PS + q], u[q], acc);
+                    for (int q = 0; q < r; q++) acc = lt_fma(-lt[q * mp + r], u[q], acc);
                     u[r] = acc;
                 }
 #pragma unroll
@@ -383,54 +433,52 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
         }
         __syncthreads();
         for (int k = tid; k < nmv; k += kThreads) slot[mv_dst[k]] = -1;
-        // trailing update A22 -= L21 * U12, tiles of 64 x TN
+        // trailing update A22 -= L21 * U12 (pb == PB whenever columns remain)
         const int c0 = j0 + pb;
         const int m2 = N - c0;
         if (m2 > 0) {
             const int tx = tid & 31, ty = tid >> 5;
             for (int tn0 = 0; tn0 < m2; tn0 += TN) {
-                for (int idx = tid; idx < pb * TN; idx += kThreads) {
-                    const int r = idx / TN, c = idx - r * TN;
-                    const int col = c0 + tn0 + c;
-                    utile[idx] = (col < N) ? M[(int64_t)(j0 + r) * ld + col] : LT(0);
+                for (int idx = tid; idx < PB * TN; idx += kThreads) {
+                    const int q = idx / TN, cc = idx - q * TN;
+                    const int col = c0 + tn0 + cc;
+                    utile[idx] = (col < N) ? M[(int64_t)(j0 + q) * ld + col] : LT(0);
                 }
                 __syncthreads();
-                for (int tm0 = 0; tm0 < m2; tm0 += 64) {
-                    const int rowb = c0 + tm0 + ty * 4;
-                    const int colb = c0 + tn0 + tx * 4;
-                    LT acc[4][4];
+                for (int tm0 = 0; tm0 < m2; tm0 += TM) {
+                    const int rl = pb + tm0 + ty * 8;  // row relative to j0
+                    const int col0 = c0 + tn0 + tx * 4;
+                    LT acc[8][4];
 #pragma unroll
-                    for (int a = 0; a < 4; a++)
+                    for (int a = 0; a < 8; a++) {
+                        const int r = j0 + rl + a;
+                        if (r < N && col0 < ld) {
+                            load4(M + (int64_t)r * ld + col0, acc[a]);
+                        } else {
 #pragma unroll
-                        for (int b = 0; b < 4; b++) {
-                            const int row = rowb + a, col = colb + b;
-                            acc[a][b] = (row < N && col < N) ? M[(int64_t)row * ld + col] : LT(0);
-                        }
-#pragma unroll 4
-                    for (int q = 0; q < PB; q++) {
-                        if (q < pb) {
-                            LT lv[4], uv[4];
-#pragma unroll
-                            for (int a = 0; a < 4; a++) {
-                                const int pr = rowb + a - j0;
-                                lv[a] = (pr < m) ? panel[pr * PS + q] : LT(0);
-                            }
-#pragma unroll
-                            for (int b = 0; b < 4; b++) uv[b] = utile[q * TN + tx * 4 + b];
-#pragma unroll
-                            for (int a = 0; a < 4; a++)
-#pragma unroll
-                                for (int b = 0; b < 4; b++)
-                                    acc[a][b] = lt_fma(-lv[a], uv[b], acc[a][b]);
+                            for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
                         }
                     }
+#pragma unroll 4
+                    for (int q = 0; q < PB; q++) {
+                        LT av[8], bv[4];
+                        load8(lt + q * mp + rl, av);
+                        load4(utile + q * TN + tx * 4, bv);
 #pragma unroll
-                    for (int a = 0; a < 4; a++)
+                        for (int a = 0; a < 8; a++)
 #pragma unroll
-                        for (int b = 0; b < 4; b++) {
-                            const int row = rowb + a, col = colb + b;
-                            if (row < N && col < N) M[(int64_t)row * ld + col] = acc[a][b];
+                            for (int b = 0; b < 4; b++)
+                                acc[a][b] = lt_fma(-av[a], bv[b], acc[a][b]);
+                    }
+#pragma unroll
+                    for (int a = 0; a < 8; a++) {
+                        const int r = j0 + rl + a;
+                        if (r < N) {
+#pragma unroll
+                            for (int b = 0; b < 4; b++)
+                                if (col0 + b < N) M[(int64_t)r * ld + col0 + b] = acc[a][b];
                         }
+                    }
                 }
                 __syncthreads();
             }
@@ -679,7 +727,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     }
     __syncthreads();
     const int N = D.n, R = D.r;
-    const SmemLayout L(P.nmax, P.rmax, P.amax, (int)sizeof(LT), PB, TN);
+    const SmemLayout L(P.nmax, P.rmax, P.amax, P.hmax, (int)sizeof(LT), PB, TN);
     double *vbase = reinterpret_cast<double *>(smem + L.vec);
     Vecs V;
     V.y1 = vbase;
@@ -699,8 +747,12 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     int *perm = reinterpret_cast<int *>(smem + L.perm);
     int *slot = reinterpret_cast<int *>(smem + L.slot);
     LT *bvec = reinterpret_cast<LT *>(smem + L.bvec);
-    LT *panel = reinterpret_cast<LT *>(smem + L.panel);
+    LT *lt = reinterpret_cast<LT *>(smem + L.lt);
     LT *utile = reinterpret_cast<LT *>(smem + L.utile);
+    LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
+    int *s_sptr = reinterpret_cast<int *>(smem + L.sptr);
+    int *s_sent = reinterpret_cast<int *>(smem + L.sent);
+    int *s_rent = reinterpret_cast<int *>(smem + L.rent);
 
     const int *ia = P.iarena;
     const double *da = P.darena;
@@ -708,11 +760,14 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     m.n = N;
     m.r = R;
     m.nnz_a = D.nnz_a;
-    m.rent = ia + D.rxn_ent;
-    m.sptr = ia + D.sp_ptr;
-    m.sent = ia + D.sp_ent;
+    m.rent = s_rent;
+    m.sptr = s_sptr;
+    m.sent = s_sent;
     m.rptr = rptr;
     m.kk = kk;
+    for (int q = tid; q < D.nnz_a; q += kThreads) s_rent[q] = ia[D.rxn_ent + q];
+    for (int q = tid; q < D.nnz_h; q += kThreads) s_sent[q] = ia[D.sp_ent + q];
+    for (int q = tid; q <= N; q += kThreads) s_sptr[q] = ia[D.sp_ptr + q];
 
     for (int s = tid; s < N; s += kThreads) {
         V.y1[s] = da[D.x0 + s];
@@ -732,6 +787,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     // FP32 form: inverted diagonal blocks of the factors follow the matrix
     float *dinv = reinterpret_cast<float *>(M + (int64_t)N * ld);
     const int refine_max = P.refine_max > 0 ? P.refine_max : 8;
+    const bool root_sqrt = (D.flags & 1) != 0;
     long long c_mark = 0;
 
     int64_t outer = 0;  // every thread keeps the loop count (uniform control)
@@ -851,7 +907,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
             V.k1[s] = w1;  // the 4th-order solution, kept on accept (u untouched)
             const double Rv = fabs(w1 - w2) / dt;
-            const double delta = 0.84 * sqrt(sqrt(V.tol[s] / Rv));
+            const double q = V.tol[s] / Rv;
+            const double delta = 0.84 * (root_sqrt ? sqrt(sqrt(q)) : pow(q, 0.25));
             if (!(Rv <= V.tol[s] && !isnan(Rv) && !isinf(Rv) && w1 > 0)) ok = false;
             if (s == 0) d0nan = isnan(delta);
             if (delta < dloc) dloc = delta;
@@ -912,7 +969,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 const long long c1 = clock64();
                 if (tid == 0) st.cycles_matrix += c1 - c_mark;
                 if (tid == 0) st.lu_factorisations++;
-                if (lu_factor<LT>(M, ld, N, perm, slot, panel, utile, red, ired, mv) != 0)
+                if (lu_factor<LT>(M, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv) != 0)
                     luFail = true;
                 if constexpr (kMixed) {
                     if (!luFail) invert_diag_blocks(M, ld, N, dinv);
@@ -961,8 +1018,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     xmax = block_max(xmax, red);
                     // stop when this correction, or the next one predicted from
                     // the contraction so far, is below FP64 resolution of dx
-                    if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) ||
-                        !(cmax * (cmax / prev) > 1e-16 * xmax) || sweep + 1 == refine_max)
+                    const bool small_next =
+                        sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
+                    if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) || small_next ||
+                        sweep + 1 == refine_max)
                         break;
                     prev = cmax;
                     // res = xr - (dx - h*J(xf)*dx)
@@ -1048,10 +1107,11 @@ __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
 
 // ------------------------------------------------------------- launch
 
-int64_t compat_smem_bytes(int nmax, int rmax, int amax, int precision) {
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision) {
     if (precision == LASSIE_PREC_FP64)
-        return SmemLayout(nmax, rmax, amax, 8, LuShape<double>::PB, LuShape<double>::TN).total;
-    return SmemLayout(nmax, rmax, amax, 4, LuShape<float>::PB, LuShape<float>::TN).total;
+        return SmemLayout(nmax, rmax, amax, hmax, 8, LuShape<double>::PB, LuShape<double>::TN)
+            .total;
+    return SmemLayout(nmax, rmax, amax, hmax, 4, LuShape<float>::PB, LuShape<float>::TN).total;
 }
 
 cudaError_t compat_configure(int precision, int64_t smem) {
@@ -1170,12 +1230,14 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
     __shared__ double red[kWarps + 1];
     __shared__ int ired[kWarps + 2 + PB];
     __shared__ int mv[4 * PB];
-    int *perm = reinterpret_cast<int *>(smem);
-    int *slot = perm + round_up4(N);
-    LT *bvec = reinterpret_cast<LT *>(smem + SmemLayout::align(int64_t(round_up4(N)) * 8));
-    LT *panel = bvec + round_up4(N);
-    LT *utile = panel + (int64_t)N * (PB + 1);
-    const int fail = lu_factor<LT>(A, ld, N, perm, slot, panel, utile, red, ired, mv);
+    const SmemLayout L(N, 1, 1, 1, (int)sizeof(LT), PB, 128);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    int *slot = reinterpret_cast<int *>(smem + L.slot);
+    LT *bvec = reinterpret_cast<LT *>(smem + L.bvec);
+    LT *lt = reinterpret_cast<LT *>(smem + L.lt);
+    LT *utile = reinterpret_cast<LT *>(smem + L.utile);
+    LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
+    const int fail = lu_factor<LT>(A, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv);
     if (threadIdx.x == 0) *info = fail;
     if (fail) return;
     for (int s = threadIdx.x; s < N; s += kThreads) bvec[s] = (LT)b[perm[s]];
@@ -1192,11 +1254,9 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
 }
 
 int64_t lu_solve_smem(int N, int precision) {
-    const int lt = precision == LASSIE_PREC_FP64 ? 8 : 4;
-    const int PB = precision == LASSIE_PREC_FP64 ? LuShape<double>::PB : LuShape<float>::PB;
-    const int TN = 128;
-    return SmemLayout::align(int64_t(round_up4(N)) * 8) + int64_t(round_up4(N)) * lt +
-           int64_t(N) * (PB + 1) * lt + int64_t(PB) * TN * lt + 64;
+    if (precision == LASSIE_PREC_FP64)
+        return SmemLayout(N, 1, 1, 1, 8, LuShape<double>::PB, 128).total;
+    return SmemLayout(N, 1, 1, 1, 4, LuShape<float>::PB, 128).total;
 }
 
 cudaError_t lu_solve_launch(int N, void *A, int ld, const double *b, double *x, int *info,

@@ -56,8 +56,11 @@ class NativeModel:
             self.handle = None
 
 
+ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
+
+
 def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int = 0,
-              deadline_s: float = 0.0, refine_max: int = 0) -> nat.Opts:
+              deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow") -> nat.Opts:
     o = nat.Opts()
     nat.load().lassie_opts_default(C.byref(o))
     if m is not None:
@@ -70,6 +73,7 @@ def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int =
     o.deadline_s = float(deadline_s)
     o.precision = ENGINES[engine]
     o.refine_max = int(refine_max)
+    o.quarter_root = ROOTS[root]
     return o
 
 
@@ -101,12 +105,12 @@ class _Packed:
 
 
 def simulate(m: Model, engine: str = "mixed", max_steps: int = 0, deadline_s: float = 0.0,
-             nm: Optional[NativeModel] = None) -> Tuple[np.ndarray, Dict]:
+             nm: Optional[NativeModel] = None, root: str = "pow") -> Tuple[np.ndarray, Dict]:
     """Integrate one model on the GPU.  Returns (trajectory [nt, ncs], stats)."""
     nm = nm or NativeModel.of(m)
     pk = _Packed(m, nm)
     st = nat.Stats()
-    o = make_opts(m, engine, max_steps, deadline_s)
+    o = make_opts(m, engine, max_steps, deadline_s, root=root)
     rc = nat.load().lassie_solve(nm.handle, _p(pk.k), _p(pk.x0), _p(pk.feed), _p(pk.atol),
                                  _p(pk.t), pk.t.shape[0], _p(pk.cs),
                                  0 if pk.cs is None else pk.cs.shape[0], C.byref(o),
@@ -124,7 +128,7 @@ class Batch:
 
     def __init__(self, models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                  deadline_s: float = 0.0, native: Optional[Sequence[NativeModel]] = None,
-                 refine_max: int = 0):
+                 refine_max: int = 0, root: str = "pow"):
         L = nat.load()
         cache: Dict[int, NativeModel] = {}
         self.packs = []
@@ -140,7 +144,7 @@ class Batch:
         self.n = len(models)
         self._inst = (nat.Instance * max(self.n, 1))(*[p.instance() for p in self.packs])
         self.opts = make_opts(models[0] if self.n else None, engine, max_steps, deadline_s,
-                              refine_max)
+                              refine_max, root)
         h = C.c_void_p()
         nat.check(L.lassie_batch_create(C.cast(self._inst, C.c_void_p), self.n,
                                         C.byref(self.opts), C.byref(h)), "lassie_batch_create")
@@ -178,7 +182,7 @@ class Batch:
 
 
 def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
-                   deadline_s: float = 0.0) -> Tuple[List[np.ndarray], List[Dict]]:
+                   deadline_s: float = 0.0, root: str = "pow") -> Tuple[List[np.ndarray], List[Dict]]:
     """Integrate independent instances in one persistent launch (host buffers
     in and out, ``lassie_solve_batch``)."""
     L = nat.load()
@@ -192,7 +196,7 @@ def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: in
     n = len(models)
     inst = (nat.Instance * max(n, 1))(*[p.instance() for p in packs])
     stats = (nat.Stats * max(n, 1))()
-    o = make_opts(models[0] if n else None, engine, max_steps, deadline_s)
+    o = make_opts(models[0] if n else None, engine, max_steps, deadline_s, root=root)
     rc = L.lassie_solve_batch(C.cast(inst, C.c_void_p), n, C.byref(o), C.cast(stats, C.c_void_p))
     if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE):
         nat.check(rc, "lassie_solve_batch")

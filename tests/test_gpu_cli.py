@@ -30,8 +30,8 @@ def test_cli_outputs(gpu, tmp_path, engine):
     m.cs = np.array([0, 3, 17, 40], np.int32)
     inp, out = tmp_path / "in", tmp_path / "out"
     write_folder(m, str(inp))
-    r = subprocess.run([build.CLI, str(inp), str(out), "-engine", engine, "-dump-f64",
-                        "-stats"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+    r = subprocess.run([build.CLI, str(inp), str(out), "-engine", engine, "-root", "sqrt",
+                        "-dump-f64", "-stats"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
                        timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "Total running time" in r.stdout
@@ -65,7 +65,8 @@ def test_cli_stochastic_rescales_output(gpu, tmp_path):
     write_folder(m_counts, str(inp))
     (inp / "modelkind").write_text("stochastic\n")
     (inp / "volume").write_text("%r\n" % vol)
-    r = subprocess.run([build.CLI, str(inp), str(out), "-engine", "fp64", "-dump-f64"],
+    r = subprocess.run([build.CLI, str(inp), str(out), "-engine", "fp64", "-root", "sqrt",
+                        "-dump-f64"],
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     full = read_table(out / "output" / "Solution.f64")

@@ -85,7 +85,7 @@ def test_lu_singular_reports_column(gpu):
 def test_solve_fp64_bit_exact(gpu, name, m):
     ref, st_ref, rc = O.solve(m, max_steps=2_000_000)
     assert rc == 0
-    out, st = solver.simulate(m, engine="fp64", deadline_s=120)
+    out, st = solver.simulate(m, engine="fp64", deadline_s=120, root="sqrt")
     assert st["status"] == 0
     assert st["be_steps"] == st_ref["be_steps"]
     assert st["rkf_accepts"] == st_ref["rkf_accepts"]
@@ -96,14 +96,14 @@ def test_solve_fp64_bit_exact(gpu, name, m):
 @pytest.mark.parametrize("name,m", list(small_cases()), ids=[c[0] for c in small_cases()])
 def test_solve_mixed_within_tolerance(gpu, name, m):
     ref, st_ref, rc = O.solve(m, max_steps=2_000_000)
-    out, st = solver.simulate(m, engine="mixed", deadline_s=120)
+    out, st = solver.simulate(m, engine="mixed", deadline_s=120, root="sqrt")
     assert st["status"] == 0
     assert within(out, ref), float(np.max(np.abs(out - ref) - RTOL * np.abs(ref)))
 
 
 def test_batch_equals_single(gpu):
     models = [synth.shorten(synth.make_c4_instance(q), 0.2, 3) for q in range(6)]
-    outs, stats = solver.simulate_batch(models, engine="fp64", deadline_s=120)
+    outs, stats = solver.simulate_batch(models, engine="fp64", deadline_s=120, root="sqrt")
     for m, o, s in zip(models, outs, stats):
         ref, _, _ = O.solve(m)
         assert s["status"] == 0
