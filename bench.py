@@ -236,6 +236,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--instances", type=int, default=2048)
+    ap.add_argument("--horizon", type=float, default=20.0,
+                    help="integrate t in [0, horizon] (20 = the workload; smaller values "
+                         "make small profiling cases)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64-form, RHS and CPU-baseline measurements")
     args = ap.parse_args()
@@ -259,6 +262,9 @@ def main():
     # weak scaling: every rank integrates its own 2048 instances
     ids = sharding.weak_shard(args.instances, rank)
     models = synth.make_c4(args.instances, first=ids.start)
+    if args.horizon != 20.0:
+        models = [synth.shorten(m, args.horizon, max(2, int(round(50 * args.horizon / 20))))
+                  for m in models]
     stream = torch.cuda.Stream()
     batch = solver.Batch(models, engine="mixed", deadline_s=600)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2
@@ -318,7 +324,9 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded, numpy default_rng(1000*4 + instance))",
-            "config": {"workload": WORKLOAD, "instances_per_gpu": args.instances,
+            "config": {"workload": WORKLOAD if (args.instances == 2048 and args.horizon == 20.0)
+                       else f"{WORKLOAD} -- reduced: {args.instances} instances, t in [0,{args.horizon:g}]",
+                       "instances_per_gpu": args.instances,
                        "form": "mixed (FP32 LU + FP64 refinement)",
                        "parallelism": f"instances sharded over {world} GPU(s)",
                        "l2": "flushed between steps (256 MB write)"},

@@ -90,6 +90,11 @@ typedef struct {
     int64_t cycles_matrix;
     int64_t cycles_lu;
     int64_t cycles_solve;
+    /* parts of cycles_lu: panel factorisation, row moves + U12 solve, trailing
+       update */
+    int64_t cycles_lu_panel;
+    int64_t cycles_lu_rows;
+    int64_t cycles_lu_trailing;
     double t_final;
     double dt_be_final;
     int32_t status;

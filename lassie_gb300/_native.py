@@ -49,7 +49,9 @@ class Stats(C.Structure):
                 ("lu_failures", C.c_int64), ("nan_reverts", C.c_int64),
                 ("refine_sweeps", C.c_int64), ("cycles_rkf", C.c_int64),
                 ("cycles_matrix", C.c_int64), ("cycles_lu", C.c_int64),
-                ("cycles_solve", C.c_int64), ("t_final", C.c_double),
+                ("cycles_solve", C.c_int64), ("cycles_lu_panel", C.c_int64),
+                ("cycles_lu_rows", C.c_int64), ("cycles_lu_trailing", C.c_int64),
+                ("t_final", C.c_double),
                 ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
 
     def as_dict(self):

@@ -38,6 +38,7 @@ struct InstResult {
     int64_t outer_iters, rkf_accepts, rkf_retries, be_steps, newton_iters,
         lu_factorisations, lu_failures, nan_reverts, refine_sweeps;
     int64_t cycles_rkf, cycles_matrix, cycles_lu, cycles_solve;
+    int64_t cycles_lu_panel, cycles_lu_rows, cycles_lu_trailing;
     double t_final, dt_be_final;
     int32_t status, pad;
 };

@@ -281,7 +281,8 @@ __device__ __forceinline__ void load4(const double *p, double *o) {
 // column j is exactly zero (uniform across the CTA).
 template <typename LT>
 __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot, LT *lt,
-                                      LT *utile, LT *rowbuf, double *red, int *ired, int *mv) {
+                                      LT *utile, LT *rowbuf, double *red, int *ired, int *mv,
+                                      long long *cyc) {
     constexpr int PB = LuShape<LT>::PB;
     constexpr int TN = 128, TM = 128;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -293,6 +294,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
     }
     __syncthreads();
     int fail = 0;
+    long long c_a = clock64();
     for (int j0 = 0; j0 < N; j0 += PB) {
         const int pb = min(PB, N - j0);
         const int m = N - j0;
@@ -389,6 +391,8 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
             }
         }
         if (fail) break;
+        long long c_b = clock64();
+        if (tid == 0) cyc[0] += c_b - c_a;
         // panel back to global; L (and U11) transposed into lt[c*mp + r]
         if (mine) {
 #pragma unroll
@@ -433,6 +437,8 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
         }
         __syncthreads();
         for (int k = tid; k < nmv; k += kThreads) slot[mv_dst[k]] = -1;
+        c_a = clock64();
+        if (tid == 0) cyc[1] += c_a - c_b;
         // trailing update A22 -= L21 * U12 (pb == PB whenever columns remain)
         const int c0 = j0 + pb;
         const int m2 = N - c0;
@@ -483,6 +489,9 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
                 __syncthreads();
             }
         }
+        c_b = clock64();
+        if (tid == 0) cyc[2] += c_b - c_a;
+        c_a = c_b;
     }
     __syncthreads();
     return fail;
@@ -938,7 +947,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         }
         dt = newDt;
         if ((t + dt) > t1) dt = fabs(t1 - t);
-        double *yv = V.k2, *xr = V.k3, *dx = V.k4, *xf = V.k5, *res = V.k6;
+        double *yv = V.k2, *xr = V.k3, *dx = V.k4, *xf = V.k5, *res = V.k6, *mdiag = V.k1;
         for (int s = tid; s < N; s += kThreads) yv[s] = V.y1[s];
         __syncthreads();
         int64_t itN = 0;
@@ -966,10 +975,13 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if (itN == 0) {
                 c_mark = clock64();
                 assemble_newton_matrix<LT>(m, yv, dt, M, ld);
+                for (int s2 = tid; s2 < N; s2 += kThreads)
+                    mdiag[s2] = (double)M[(int64_t)s2 * ld + s2];
                 const long long c1 = clock64();
                 if (tid == 0) st.cycles_matrix += c1 - c_mark;
                 if (tid == 0) st.lu_factorisations++;
-                if (lu_factor<LT>(M, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv) != 0)
+                if (lu_factor<LT>(M, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv,
+                                  reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0)
                     luFail = true;
                 if constexpr (kMixed) {
                     if (!luFail) invert_diag_blocks(M, ld, N, dinv);
@@ -994,20 +1006,34 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 for (int s = tid; s < N; s += kThreads) dx[s] = (double)bvec[s];
                 __syncthreads();
             } else {
-                // FP32 solves, FP64 residuals: dx converges to the FP64 solve
+                // FP32 solves, FP64 residuals: dx converges to the FP64 solve.
+                // Each residual is scaled by a power of two to unit max norm
+                // before the FP32 solve; rows whose scaled residual is below
+                // the FP32 normal range (species far below the others) get an
+                // FP64 diagonal correction instead, so that they keep their
+                // sign and magnitude as in the FP64 solve.
                 for (int s = tid; s < N; s += kThreads) {
                     dx[s] = 0.0;
                     res[s] = xr[s];
                 }
-                __syncthreads();
+                double rloc = 0.0;
+                for (int s = tid; s < N; s += kThreads) rloc = fmax(rloc, fabs(res[s]));
+                double rmax = block_max(rloc, red);
                 double prev = INFINITY;
                 for (int sweep = 0; sweep < refine_max; sweep++) {
-                    for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)res[perm[s]];
+                    if (!(rmax > 0.0) || isinf(rmax)) break;  // nothing to solve / not finite
+                    const int e = ilogb(rmax);
+                    const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
+                    for (int s = tid; s < N; s += kThreads)
+                        bvec[s] = (LT)(res[perm[s]] * sc);
                     __syncthreads();
                     lu_solve_fast(M, ld, N, dinv, bvec);
                     double cmax = 0.0, xmax = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
-                        const double c = (double)bvec[s];
+                        double c = (double)bvec[s] * isc;
+                        const double rs = res[s] * sc;
+                        if (fabs(rs) < 0x1p-100 && rs != 0.0 && fabs(mdiag[s]) >= 0.5)
+                            c += res[s] / mdiag[s];
                         const double nx = dx[s] + c;
                         dx[s] = nx;
                         cmax = fmax(cmax, fabs(c));
@@ -1027,11 +1053,14 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     // res = xr - (dx - h*J(xf)*dx)
                     jv_phase1(m, xf, dx, qr);
                     __syncthreads();
+                    rloc = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
                         const double jv = jv_species(m, s, qr);
-                        res[s] = xr[s] - (dx[s] - dt * jv);
+                        const double r = xr[s] - (dx[s] - dt * jv);
+                        res[s] = r;
+                        rloc = fmax(rloc, fabs(r));
                     }
-                    __syncthreads();
+                    rmax = block_max(rloc, red);
                 }
             }
             if (tid == 0) st.cycles_solve += clock64() - c_mark;
@@ -1237,7 +1266,9 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
     LT *lt = reinterpret_cast<LT *>(smem + L.lt);
     LT *utile = reinterpret_cast<LT *>(smem + L.utile);
     LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
-    const int fail = lu_factor<LT>(A, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv);
+    __shared__ long long cyc[3];
+    if (threadIdx.x == 0) cyc[0] = cyc[1] = cyc[2] = 0;
+    const int fail = lu_factor<LT>(A, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv, cyc);
     if (threadIdx.x == 0) *info = fail;
     if (fail) return;
     for (int s = threadIdx.x; s < N; s += kThreads) bvec[s] = (LT)b[perm[s]];
