@@ -229,6 +229,37 @@ def rhs_bandwidth(torch, stream, n_inst=65536, reps=20):
             "network": "256 species x 256 reactions", "instances": n_inst}
 
 
+def adjoint_measure(n_copies=64):
+    """Differentiation workload: 64 copies of a 256 x 256 network,
+    k = 10^U(-3,3), loss = sum of squares over 40 samples in (0,10] against
+    trajectories of k * exp(N(0,0.3^2)).  Returns grads/s and the cost of one
+    gradient relative to one forward solve (both through the public API)."""
+    from lassie_gb300 import synth, solver
+    from lassie_gb300.adjoint import adjoint_batch
+    base, k_t = synth.make_c5(n_copies)
+    tgt_models = []
+    for q, m in enumerate(base):
+        mt = synth.shorten(m, 10.0, 41)
+        mt.t = m.t
+        mt.k = k_t[q]
+        tgt_models.append(mt)
+    targets, _ = solver.simulate_batch(tgt_models, engine="mixed", deadline_s=600)
+    solver.simulate_batch(base, engine="mixed", deadline_s=600)  # warm-up
+    t0 = time.perf_counter()
+    solver.simulate_batch(base, engine="mixed", deadline_s=600)
+    t_fwd = time.perf_counter() - t0
+    adjoint_batch(base, targets, deadline_s=600)  # warm-up
+    t0 = time.perf_counter()
+    loss, gk, _, _, stats = adjoint_batch(base, targets, deadline_s=600)
+    t_adj = time.perf_counter() - t0
+    return {"grads_per_s": n_copies / t_adj, "forward_sims_per_s": n_copies / t_fwd,
+            "adjoint_over_forward": t_adj / t_fwd, "copies": n_copies,
+            "mean_loss": float(sum(loss) / len(loss)),
+            "be_steps_per_copy": float(sum(s["be_steps"] for s in stats) / len(stats)),
+            "workload": "c5: 64 x (256 species x 256 reactions), k~10^U(-3,3), 40 samples "
+                        "in (0,10], targets from k*exp(N(0,0.3^2))"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -360,6 +391,7 @@ def main():
             "fp64_ms": res["fp64"][0], "mixed_ms": res["mixed"][0],
             "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
             "max_rel_err_vs_fp64": worst, "points_outside_rtol1e-6_atol1e-9": nbad}
+        line["adjoint"] = adjoint_measure()
         line["rhs_hbm"] = rhs_bandwidth(torch, stream)
         line["rhs_hbm"]["frac"] = line["rhs_hbm"]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
         line["cpu_baseline"] = cpu_baseline(args.instances)

@@ -43,6 +43,7 @@ extern "C" {
 #define LASSIE_ERR_TOO_LARGE (-23)   /* network does not fit the engine */
 #define LASSIE_ERR_DEADLINE (-24)    /* opts.deadline_s elapsed on the device */
 #define LASSIE_ERR_NO_DEVICE (-25)   /* no CUDA device / not sm_103 */
+#define LASSIE_ERR_RECORD_FULL (-26) /* adjoint step record capacity reached */
 
 /* precision of the Newton matrix factorisation */
 #define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */
@@ -172,6 +173,22 @@ int lassie_batch_launches(const lassie_batch *batch);
    (trajectories and stats) for this batch */
 int lassie_batch_bytes(const lassie_batch *batch, int64_t *h2d, int64_t *d2h);
 void lassie_batch_destroy(lassie_batch *batch);
+
+/* Discrete adjoint (no reference counterpart).  Integrates the instances with
+   the mixed form, recording the step sequence, then runs the backward pass
+   of that exact step sequence for
+       L_q = sum over samples i and sampled species j of (y_ij - target_ij)^2
+   and returns loss[q], grad_logk[q][R] = dL_q/dlog k and (when grad_x0 is
+   not NULL) grad_x0[q][N] = dL_q/dx0.  targets[q] has the layout of
+   inst[q].out, which also receives the forward trajectory.  Backward-Euler
+   steps are differentiated as exactly solved; steps that reverted species
+   or failed to factor are treated as the identity.  Accepted RKF45 steps
+   store their output every ckpt_every steps (0 = 8) and are recomputed in
+   between; max_record caps the recorded steps per instance (0 = 100000). */
+int lassie_adjoint_batch(const lassie_instance *inst, int32_t n, const double *const *targets,
+                         const lassie_opts *opts, int32_t ckpt_every, int32_t max_record,
+                         double *loss, double *const *grad_logk, double *const *grad_x0,
+                         lassie_stats *stats);
 
 /* ---------------------------------------------------- single evaluations */
 /* dx = f(x) for n_inst parameterisations of one network, device buffers,

@@ -17,6 +17,7 @@ ERR_ALLOC = -22
 ERR_TOO_LARGE = -23
 ERR_DEADLINE = -24
 ERR_NO_DEVICE = -25
+ERR_RECORD_FULL = -26
 ERR_CUDA = -13
 PREC_FP64 = 0
 PREC_MIXED = 1
@@ -30,7 +31,7 @@ EXPORTS = (
     "lassie_model_info", "lassie_solve", "lassie_solve_batch", "lassie_batch_create",
     "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
     "lassie_batch_bytes", "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
-    "lassie_lu_solve",
+    "lassie_lu_solve", "lassie_adjoint_batch",
 )
 
 
@@ -121,6 +122,7 @@ def load():
         L.lassie_rhs.argtypes = [vp, vp, vp, vp]
         L.lassie_newton_matrix.argtypes = [vp, vp, vp, dbl, vp]
         L.lassie_lu_solve.argtypes = [i32, vp, vp, vp, i32]
+        L.lassie_adjoint_batch.argtypes = [vp, i32, vp, C.POINTER(Opts), i32, i32, vp, vp, vp, vp]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int and name not in ("lassie_device_ok",):

@@ -30,6 +30,8 @@ cudaError_t newton_matrix_launch(int N, int R, int nnz_a, const int *rptr, const
 cudaError_t lu_solve_launch(int N, void *A, int ld, const double *b, double *x, int *info,
                             int precision, cudaStream_t stream);
 int64_t lu_solve_smem(int N, int precision);
+int64_t adjoint_smem_bytes(int nmax, int rmax, int amax, int hmax);
+cudaError_t adjoint_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
 }  // namespace lassie
 
 using namespace lassie;
@@ -56,6 +58,10 @@ static int set_error(int status, const std::string &msg) {
 struct lassie_model {
     int32_t N = 0, R = 0;
     std::vector<int32_t> rxn_ptr, rxn_ent, sp_ptr, sp_ent;
+    // for vector-Jacobian products (adjoint): net stoichiometry by reaction
+    // (species * 256 + coefficient), and the reactant entries of each species
+    // (indices into rxn_ent)
+    std::vector<int32_t> hr_ptr, hr_ent, as_ptr, as_ent;
     std::mutex mu;
     int dev = -1;
     int32_t *d_struct = nullptr;  // [rxn_ptr | rxn_ent | sp_ptr | sp_ent]
@@ -63,7 +69,21 @@ struct lassie_model {
     int64_t off_rent() const { return R + 1; }
     int64_t off_sptr() const { return off_rent() + (int64_t)rxn_ent.size(); }
     int64_t off_sent() const { return off_sptr() + N + 1; }
-    int64_t struct_len() const { return off_sent() + (int64_t)sp_ent.size(); }
+    int64_t off_hrptr() const { return off_sent() + (int64_t)sp_ent.size(); }
+    int64_t off_hrent() const { return off_hrptr() + R + 1; }
+    int64_t off_asptr() const { return off_hrent() + (int64_t)hr_ent.size(); }
+    int64_t off_asent() const { return off_asptr() + N + 1; }
+    int64_t struct_len() const { return off_asent() + (int64_t)as_ent.size(); }
+    void pack(std::vector<int32_t> &out) const {
+        out.insert(out.end(), rxn_ptr.begin(), rxn_ptr.end());
+        out.insert(out.end(), rxn_ent.begin(), rxn_ent.end());
+        out.insert(out.end(), sp_ptr.begin(), sp_ptr.end());
+        out.insert(out.end(), sp_ent.begin(), sp_ent.end());
+        out.insert(out.end(), hr_ptr.begin(), hr_ptr.end());
+        out.insert(out.end(), hr_ent.begin(), hr_ent.end());
+        out.insert(out.end(), as_ptr.begin(), as_ptr.end());
+        out.insert(out.end(), as_ent.begin(), as_ent.end());
+    }
 };
 
 static const int kMaxIndex = (1 << 23) - 1;
@@ -103,6 +123,21 @@ static int build_model(int32_t N, int32_t R, const std::vector<std::vector<std::
         }
     }
     m->sp_ptr[N] = (int32_t)m->sp_ent.size();
+    m->hr_ptr.resize(R + 1);
+    for (int j = 0; j < R; j++) {
+        m->hr_ptr[j] = (int32_t)m->hr_ent.size();
+        for (auto &e : H[j]) m->hr_ent.push_back(make_ent(e.first, e.second));
+    }
+    m->hr_ptr[R] = (int32_t)m->hr_ent.size();
+    std::vector<std::vector<int>> as(N);
+    for (int j = 0; j < R; j++)
+        for (int q = m->rxn_ptr[j]; q < m->rxn_ptr[j + 1]; q++) as[ent_index(m->rxn_ent[q])].push_back(q);
+    m->as_ptr.resize(N + 1);
+    for (int sp = 0; sp < N; sp++) {
+        m->as_ptr[sp] = (int32_t)m->as_ent.size();
+        for (int q : as[sp]) m->as_ent.push_back(q);
+    }
+    m->as_ptr[N] = (int32_t)m->as_ent.size();
     *out = m;
     return LASSIE_OK;
 }
@@ -184,11 +219,8 @@ static int model_device(lassie_model *m, const int32_t **d) {
     if (m->d_struct) {
         return set_error(LASSIE_ERR_ARGS, "model already bound to another device");
     }
-    std::vector<int32_t> h((size_t)m->struct_len());
-    std::copy(m->rxn_ptr.begin(), m->rxn_ptr.end(), h.begin());
-    std::copy(m->rxn_ent.begin(), m->rxn_ent.end(), h.begin() + m->off_rent());
-    std::copy(m->sp_ptr.begin(), m->sp_ptr.end(), h.begin() + m->off_sptr());
-    std::copy(m->sp_ent.begin(), m->sp_ent.end(), h.begin() + m->off_sent());
+    std::vector<int32_t> h;
+    m->pack(h);
     CU(cudaMalloc(&m->d_struct, h.size() * sizeof(int32_t)));
     CU(cudaMemcpy(m->d_struct, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     m->dev = dev;
@@ -228,6 +260,7 @@ extern "C" const char *lassie_status_string(int s) {
     case LASSIE_ERR_TOO_LARGE: return "network too large for the engine";
     case LASSIE_ERR_DEADLINE: return "device deadline elapsed";
     case LASSIE_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+    case LASSIE_ERR_RECORD_FULL: return "adjoint step record is full";
     default: return "unknown status";
     }
 }
@@ -350,10 +383,7 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         if (it == model_off.end()) {
             base = (int64_t)hint.size();
             model_off[m] = base;
-            hint.insert(hint.end(), m->rxn_ptr.begin(), m->rxn_ptr.end());
-            hint.insert(hint.end(), m->rxn_ent.begin(), m->rxn_ent.end());
-            hint.insert(hint.end(), m->sp_ptr.begin(), m->sp_ptr.end());
-            hint.insert(hint.end(), m->sp_ent.begin(), m->sp_ent.end());
+            m->pack(hint);
         } else {
             base = it->second;
         }
@@ -368,6 +398,10 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         D.rxn_ent = base + m->off_rent();
         D.sp_ptr = base + m->off_sptr();
         D.sp_ent = base + m->off_sent();
+        D.hr_ptr = base + m->off_hrptr();
+        D.hr_ent = base + m->off_hrent();
+        D.as_ptr = base + m->off_asptr();
+        D.as_ent = base + m->off_asent();
         if (I.cs) {
             D.cs = (int64_t)hint.size();
             hint.insert(hint.end(), I.cs, I.cs + I.ncs);
@@ -554,6 +588,140 @@ extern "C" int lassie_solve(const lassie_model *model, const double *k, const do
     I.cs = cs;
     I.out = out;
     return lassie_solve_batch(&I, 1, opts, stats);
+}
+
+// --------------------------------------------------------------- adjoint
+
+extern "C" int lassie_adjoint_batch(const lassie_instance *inst, int32_t n,
+                                    const double *const *targets, const lassie_opts *opts,
+                                    int32_t ckpt_every, int32_t max_record, double *loss,
+                                    double *const *grad_logk, double *const *grad_x0,
+                                    lassie_stats *stats) {
+    if (n < 0 || (n > 0 && (!inst || !targets || !grad_logk)))
+        return set_error(LASSIE_ERR_ARGS, "adjoint_batch");
+    if (n == 0) return LASSIE_OK;
+    lassie_opts o;
+    if (opts) o = *opts;
+    else lassie_opts_default(&o);
+    o.precision = LASSIE_PREC_MIXED;
+    const int K = ckpt_every > 0 ? ckpt_every : 8;
+    const int cap = max_record > 0 ? max_record : 100000;
+    lassie_batch *b = nullptr;
+    int rc = lassie_batch_create(inst, n, &o, &b);
+    if (rc) return rc;
+    // per-instance record layout
+    std::vector<AdjDesc> ad(n);
+    int64_t rec = 0, st = 0, samp = 0, grad = 0;
+    for (int q = 0; q < n; q++) {
+        const InstDesc &D = b->desc[q];
+        ad[q].rec = rec;
+        ad[q].states = st;
+        ad[q].samp = samp;
+        ad[q].grad = grad;
+        ad[q].cap_steps = cap;
+        ad[q].cap_states = cap + 1;
+        rec += cap;
+        st += (int64_t)(cap + 1) * D.n;
+        samp += D.nt;
+        grad += D.r + D.n;
+    }
+    if (st * 8 > (int64_t)64 << 30) {
+        lassie_batch_destroy(b);
+        return set_error(LASSIE_ERR_TOO_LARGE, "adjoint record needs more than 64 GiB");
+    }
+    std::vector<double> htarget((size_t)b->n_out, 0.0);
+    for (int q = 0; q < n; q++) {
+        const InstDesc &D = b->desc[q];
+        if (!targets[q]) {
+            lassie_batch_destroy(b);
+            return set_error(LASSIE_ERR_ARGS, "adjoint_batch: missing target");
+        }
+        std::memcpy(htarget.data() + D.out, targets[q], sizeof(double) * (size_t)D.nt * D.ncs);
+    }
+    DevBuf d_ad, d_kind, d_dt, d_slot, d_states, d_nsteps, d_samp, d_target, d_grad, d_scratch;
+    const int64_t scratch_stride = (int64_t)(K + 1) * b->nmax;
+    auto cleanup = [&]() {
+        d_ad.release(); d_kind.release(); d_dt.release(); d_slot.release(); d_states.release();
+        d_nsteps.release(); d_samp.release(); d_target.release(); d_grad.release();
+        d_scratch.release();
+        lassie_batch_destroy(b);
+    };
+    if ((rc = d_ad.grow(sizeof(AdjDesc) * n)) || (rc = d_kind.grow(rec * 4)) ||
+        (rc = d_dt.grow(rec * 8)) || (rc = d_slot.grow(rec * 4)) || (rc = d_states.grow(st * 8)) ||
+        (rc = d_nsteps.grow(4 * n)) || (rc = d_samp.grow(std::max<int64_t>(samp, 1) * 4)) ||
+        (rc = d_target.grow(htarget.size() * 8)) || (rc = d_grad.grow(grad * 8)) ||
+        (rc = d_scratch.grow((size_t)scratch_stride * 8 * b->grid))) {
+        cleanup();
+        return rc;
+    }
+    if (cudaMemcpy(d_ad.p, ad.data(), sizeof(AdjDesc) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(d_target.p, htarget.data(), htarget.size() * 8, cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemset(d_nsteps.p, 0, 4 * n) != cudaSuccess ||
+        cudaMemset(d_samp.p, 0, std::max<int64_t>(samp, 1) * 4) != cudaSuccess) {
+        cleanup();
+        return set_error(LASSIE_ERR_CUDA, "adjoint upload");
+    }
+    AdjArrays &A = b->P.adj;
+    A.desc = (const AdjDesc *)d_ad.p;
+    A.rec_kind = (int32_t *)d_kind.p;
+    A.rec_dt = (double *)d_dt.p;
+    A.rec_slot = (int32_t *)d_slot.p;
+    A.states = (double *)d_states.p;
+    A.nsteps = (int32_t *)d_nsteps.p;
+    A.samp_step = (int32_t *)d_samp.p;
+    A.target = (const double *)d_target.p;
+    A.grad = (double *)d_grad.p;
+    A.scratch = (double *)d_scratch.p;
+    A.scratch_stride = scratch_stride;
+    A.ckpt_every = K;
+    // forward with recording
+    rc = lassie_batch_run(b, nullptr);
+    if (!rc) rc = lassie_batch_sync(b);
+    std::vector<lassie_stats> hst(n);
+    if (!rc) rc = lassie_batch_read(b, inst, hst.data());
+    if (stats) std::memcpy(stats, hst.data(), sizeof(lassie_stats) * n);
+    if (rc) {
+        cleanup();
+        return rc;
+    }
+    for (int q = 0; q < n; q++) {
+        const InstDesc &D = b->desc[q];
+        double L = 0.0;
+        for (int64_t i = 0; i < (int64_t)D.nt * D.ncs; i++) {
+            const double d = inst[q].out[i] - targets[q][i];
+            L += d * d;
+        }
+        if (loss) loss[q] = L;
+    }
+    // backward
+    const int64_t smem = adjoint_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax);
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
+    if (smem > max_optin - 1024) {
+        cleanup();
+        return set_error(LASSIE_ERR_TOO_LARGE, "adjoint shared memory");
+    }
+    if (cudaMemset(b->d_queue.p, 0, 16) != cudaSuccess ||
+        adjoint_launch(b->P, b->grid, smem, nullptr) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {
+        std::string msg = cudaGetErrorString(cudaGetLastError());
+        cleanup();
+        return set_error(LASSIE_ERR_CUDA, "adjoint kernel: " + msg);
+    }
+    std::vector<double> hgrad(grad);
+    if (cudaMemcpy(hgrad.data(), d_grad.p, grad * 8, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cleanup();
+        return set_error(LASSIE_ERR_CUDA, "adjoint download");
+    }
+    for (int q = 0; q < n; q++) {
+        const InstDesc &D = b->desc[q];
+        std::memcpy(grad_logk[q], hgrad.data() + ad[q].grad, sizeof(double) * D.r);
+        if (grad_x0 && grad_x0[q])
+            std::memcpy(grad_x0[q], hgrad.data() + ad[q].grad + D.r, sizeof(double) * D.n);
+    }
+    cleanup();
+    return LASSIE_OK;
 }
 
 // ---------------------------------------------------- single evaluations

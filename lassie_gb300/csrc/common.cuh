@@ -26,6 +26,7 @@ struct InstDesc {
     int32_t n, r, nt, ncs;
     int32_t nnz_a, nnz_h, flags, pad;
     int64_t rxn_ptr, rxn_ent, sp_ptr, sp_ent;  // int arena
+    int64_t hr_ptr, hr_ent, as_ptr, as_ent;    // int arena (adjoint structure)
     int64_t cs;                                // int arena, -1 = all species
     int64_t k, x0, feed, atol, t;              // double arena, feed/atol -1 = none
     int64_t out;                               // output arena
@@ -44,6 +45,35 @@ struct InstResult {
 };
 static_assert(sizeof(InstResult) == sizeof(lassie_stats), "stats layout");
 
+// Per-instance record of the forward step sequence (adjoint).  Step kinds:
+// 0 accepted RKF45 step, 1 backward-Euler step, 2 backward-Euler step that
+// left the state unchanged (LU failure), 3 backward-Euler step with reverted
+// species.  The output state of every backward-Euler step is stored; accepted
+// RKF45 steps store their output every `ckpt_every` steps (the others are
+// recomputed in the backward pass).  Slot 0 holds the initial state.
+struct AdjDesc {
+    int64_t rec;       // offset into rec_kind / rec_dt / rec_slot
+    int64_t states;    // offset into the state store (doubles)
+    int64_t samp;      // offset into samp_step (one per sample)
+    int64_t grad;      // offset into grad: d loss / d log k [R], then d loss / d x0 [N]
+    int32_t cap_steps, cap_states;
+};
+
+struct AdjArrays {
+    const AdjDesc *desc;
+    int32_t *rec_kind;
+    double *rec_dt;
+    int32_t *rec_slot;
+    double *states;
+    int32_t *nsteps;     // per instance
+    int32_t *samp_step;
+    const double *target;  // same layout as the outputs
+    double *grad;
+    double *scratch;       // per CTA: (ckpt_every + 1) states for recomputation
+    int64_t scratch_stride;
+    int32_t ckpt_every;
+};
+
 struct LaunchParams {
     const InstDesc *inst;
     int32_t n_inst;
@@ -58,6 +88,7 @@ struct LaunchParams {
     int32_t nmax, rmax, amax, hmax;  // largest N, R, nnz_A, nnz_H in the batch
     int32_t precision, refine_max;
     uint64_t deadline_ns;      // per-launch wall-clock limit (ns), 0 = none
+    AdjArrays adj;             // adj.desc == nullptr: no recording
 };
 
 // Dynamic shared-memory layout of the integrator (bytes), identical on host

@@ -166,13 +166,60 @@ __device__ __forceinline__ double jv_species(const Net &m, int i, const double *
     return acc;
 }
 
+// Vector-Jacobian products with the exact Jacobian of f (adjoint).
+// Phase 1, per reaction j: g_j = sum_i S_ij v_i (net stoichiometry by
+// reaction), t[q] = d prop_j / d x_{species(q)} * g_j for each reactant entry
+// q of j, and, when theta is given, theta_j += h * prop_j(x) * g_j
+// (d f / d log k_j = S_:j prop_j).  Phase 2, per species g:
+// (J^T v)_g = sum of t[q] over the reactant entries q of species g.
+struct AdjNet {
+    const int *hrptr;  // [R+1] net stoichiometry by reaction
+    const int *hrent;  // species * 256 + coefficient
+    const int *asptr;  // [N+1] reactant entries by species
+    const int *asent;  // reactant-entry indices q
+};
+
+__device__ void jtv_phase1(const Net &m, const AdjNet &a, const double *x, const double *v,
+                           double *t, double *theta, double h) {
+    for (int j = threadIdx.x; j < m.r; j += kThreads) {
+        double g = 0.0;
+        for (int e = a.hrptr[j]; e < a.hrptr[j + 1]; e++) {
+            const int ent = a.hrent[e];
+            g = fma((double)ent_coef(ent), v[ent_index(ent)], g);
+        }
+        const int b = m.rptr[j], en = m.rptr[j + 1];
+        if (theta) {
+            double prop = m.kk[j];
+            for (int q = b; q < en; q++) prop *= mypow(x[ent_index(m.rent[q])], ent_coef(m.rent[q]));
+            theta[j] += h * prop * g;
+        }
+        for (int q = b; q < en; q++) {
+            const int eq = m.rent[q];
+            const int sg = ent_index(eq), aq = ent_coef(eq);
+            double d = aq > 0 ? m.kk[j] * (double)aq * mypow(x[sg], aq - 1) : 0.0;
+            for (int q2 = b; q2 < en; q2++)
+                if (q2 != q) d *= mypow(x[ent_index(m.rent[q2])], ent_coef(m.rent[q2]));
+            t[q] = d * g;
+        }
+    }
+}
+
+__device__ __forceinline__ double jtv_species(const AdjNet &a, int g, const double *t) {
+    double acc = 0.0;
+    for (int e = a.asptr[g]; e < a.asptr[g + 1]; e++) acc += t[a.asent[e]];
+    return acc;
+}
+
 // M = I - h*J(x) into M (row-major, leading dimension ld), J with the
 // semantics of createJac + aggiorna_Jacobiano1 (kernels.cuh:205-271,393-402).
 // Entry (i,g) accumulates, over the reactions of H row i in ascending order,
 // temp = s*k [*a*x_g^(a-1)] * (each other reactant once).
+// exact = true (adjoint): the exact derivative (other reactants enter with
+// their stoichiometry) and rows i with mask[i] != 0 left as identity rows.
 template <typename LT>
 __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *x, double h, LT *M,
-                                       int ld) {
+                                                    int ld, bool exact = false,
+                                                    const double *mask = nullptr) {
     const int N = m.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int row = warp; row < N; row += kWarps) {
@@ -181,6 +228,7 @@ __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *
     }
     __syncthreads();
     for (int i = threadIdx.x; i < N; i += kThreads) {
+        if (mask && mask[i] != 0.0) continue;
         const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
         for (int e = e0; e < e1; e++) {
             const int y = ent_index(m.sent[e]);
@@ -213,8 +261,9 @@ __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *
                         temp = temp + (double)s2 * m.kk[y2] * (double)a * mypow(x[g], a - 1);
                     else continue;
                     for (int q2 = b2; q2 < en2; q2++) {
-                        const int o = ent_index(m.rent[q2]);
-                        if (o != g) temp = temp * x[o];
+                        const int eo = m.rent[q2];
+                        const int o = ent_index(eo);
+                        if (o != g) temp = exact ? temp * mypow(x[o], ent_coef(eo)) : temp * x[o];
                     }
                     J = J + temp;
                 }
@@ -717,6 +766,83 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
     }
 }
 
+// Transposed solve with the same factors (adjoint): P A = L U, so
+// A^T mu = b is U^T z = b (forward, blocks ascending), L^T w = z (backward),
+// mu[perm[i]] = w[i] (done by the caller).  Diagonal blocks are applied as
+// the transposes of the inverted blocks; the off-diagonal updates read rows
+// of U (resp. L) of the current block, one column per thread.
+__device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, const float *dinv,
+                                             float *bvec) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nblk = (N + 31) / 32;
+    for (int b = 0; b < nblk; b++) {
+        const int r0 = b * 32;
+        const int nb = min(32, N - r0);
+        const int i = r0 + nb + tid;
+        float seg[32];
+        if (i < N) {
+#pragma unroll
+            for (int k = 0; k < 32; k++) seg[k] = (k < nb) ? M[(int64_t)(r0 + k) * ld + i] : 0.f;
+        }
+        if (warp == 0) {
+            const float *Ui = dinv + (int64_t)b * 2048 + 1024;
+            const float bi = (lane < nb) ? bvec[r0 + lane] : 0.f;
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                acc = __fmaf_rn(Ui[k * 32 + lane], __shfl_sync(0xffffffffu, bi, k), acc);
+            if (lane < nb) bvec[r0 + lane] = acc;
+        }
+        __syncthreads();
+        if (i < N) {
+            float acc = bvec[i];
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k < nb) acc = __fmaf_rn(-seg[k], bvec[r0 + k], acc);
+            bvec[i] = acc;
+        }
+        for (int i2 = i + kThreads; i2 < N; i2 += kThreads) {
+            float acc = bvec[i2];
+            for (int k = 0; k < nb; k++) acc = __fmaf_rn(-M[(int64_t)(r0 + k) * ld + i2], bvec[r0 + k], acc);
+            bvec[i2] = acc;
+        }
+        __syncthreads();
+    }
+    for (int b = nblk - 1; b >= 0; b--) {
+        const int r0 = b * 32;
+        const int nb = min(32, N - r0);
+        const int i = tid;
+        float seg[32];
+        if (i < r0) {
+#pragma unroll
+            for (int k = 0; k < 32; k++) seg[k] = (k < nb) ? M[(int64_t)(r0 + k) * ld + i] : 0.f;
+        }
+        if (warp == 0) {
+            const float *Li = dinv + (int64_t)b * 2048;
+            const float bi = (lane < nb) ? bvec[r0 + lane] : 0.f;
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                acc = __fmaf_rn(Li[k * 32 + lane], __shfl_sync(0xffffffffu, bi, k), acc);
+            if (lane < nb) bvec[r0 + lane] = acc;
+        }
+        __syncthreads();
+        if (i < r0) {
+            float acc = bvec[i];
+#pragma unroll
+            for (int k = 0; k < 32; k++)
+                if (k < nb) acc = __fmaf_rn(-seg[k], bvec[r0 + k], acc);
+            bvec[i] = acc;
+        }
+        for (int i2 = i + kThreads; i2 < r0; i2 += kThreads) {
+            float acc = bvec[i2];
+            for (int k = 0; k < nb; k++) acc = __fmaf_rn(-M[(int64_t)(r0 + k) * ld + i2], bvec[r0 + k], acc);
+            bvec[i2] = acc;
+        }
+        __syncthreads();
+    }
+}
+
 // ----------------------------------------------------------- integrator
 
 struct Vecs {
@@ -800,6 +926,15 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     long long c_mark = 0;
 
     int64_t outer = 0;  // every thread keeps the loop count (uniform control)
+    // forward recording for the adjoint
+    const bool rec = P.adj.desc != nullptr;
+    AdjDesc AD{};
+    if (rec) AD = P.adj.desc[id];
+    int nsteps = 0, nstates = 0, rkf_run = 0;
+    if (rec) {
+        for (int s2 = tid; s2 < N; s2 += kThreads) P.adj.states[AD.states + s2] = V.y1[s2];
+        nstates = 1;
+    }
     int status = LASSIE_OK;
     int i = 0;
     double t1 = D.nt > 0 ? tv[0] : 0.0;
@@ -828,6 +963,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         if (fabs(t1 - t) < 1e-5) {
             for (int j = tid; j < ncs; j += kThreads)
                 out[(int64_t)i * ncs + j] = V.y1[cs ? cs[j] : j];
+            if (rec && tid == 0) P.adj.samp_step[AD.samp + i] = nsteps;
             i++;
             if (i >= nt) break;
             t1 = tv[i];
@@ -931,6 +1067,25 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             // accept (Simulation.cuh:742-768)
             for (int s = tid; s < N; s += kThreads) V.y1[s] = V.k1[s];
             __syncthreads();
+            if (rec) {
+                if (nsteps >= AD.cap_steps || nstates >= AD.cap_states) {
+                    status = LASSIE_ERR_RECORD_FULL;
+                    break;
+                }
+                int slot = -1;
+                if (++rkf_run >= P.adj.ckpt_every) {
+                    slot = nstates++;
+                    rkf_run = 0;
+                    for (int s2 = tid; s2 < N; s2 += kThreads)
+                        P.adj.states[AD.states + (int64_t)slot * N + s2] = V.y1[s2];
+                }
+                if (tid == 0) {
+                    P.adj.rec_kind[AD.rec + nsteps] = 0;
+                    P.adj.rec_dt[AD.rec + nsteps] = dt;
+                    P.adj.rec_slot[AD.rec + nsteps] = slot;
+                }
+                nsteps++;
+            }
             const double d_temp = dt * dmin;
             if ((t + d_temp) > t1) dt = fabs(t1 - t);
             else dt = d_temp;
@@ -1031,9 +1186,12 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     double cmax = 0.0, xmax = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
                         double c = (double)bvec[s] * isc;
+                        // the part of this row's right-hand side that the FP32
+                        // cast lost (below the FP32 normal range), applied
+                        // through the diagonal
                         const double rs = res[s] * sc;
-                        if (fabs(rs) < 0x1p-100 && rs != 0.0 && fabs(mdiag[s]) >= 0.5)
-                            c += res[s] / mdiag[s];
+                        if (fabs(rs) < 0x1p-126 && fabs(mdiag[s]) >= 0.5)
+                            c += (rs - (double)(float)rs) * isc / mdiag[s];
                         const double nx = dx[s] + c;
                         dx[s] = nx;
                         cmax = fmax(cmax, fabs(c));
@@ -1079,11 +1237,13 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             itN = itN + 1;
             if (tid == 0) st.newton_iters++;
         }
+        bool reverted = false;
         if (!luFail) {
             // Simulation.cuh:894-909
             bool anybad = false;
             for (int s = tid; s < N; s += kThreads) anybad |= bad_value(yv[s]);
             if (__syncthreads_or(anybad)) {
+                reverted = true;
                 for (int s = tid; s < N; s += kThreads)
                     if (bad_value(yv[s])) yv[s] = V.y1[s];
                 newDt = dt * 0.1;
@@ -1095,11 +1255,28 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             status = LASSIE_ERR_DEADLINE;
             break;
         }
+        if (rec) {
+            if (nsteps >= AD.cap_steps || nstates >= AD.cap_states) {
+                status = LASSIE_ERR_RECORD_FULL;
+                break;
+            }
+            const int slot = nstates++;
+            rkf_run = 0;
+            for (int s2 = tid; s2 < N; s2 += kThreads)
+                P.adj.states[AD.states + (int64_t)slot * N + s2] = yv[s2];
+            if (tid == 0) {
+                P.adj.rec_kind[AD.rec + nsteps] = luFail ? 2 : (reverted ? 3 : 1);
+                P.adj.rec_dt[AD.rec + nsteps] = dt;
+                P.adj.rec_slot[AD.rec + nsteps] = slot;
+            }
+            nsteps++;
+        }
         double *tmp = V.y1;
         V.y1 = V.k2;
         V.k2 = tmp;
         t = t + dt;
     }
+    if (rec && tid == 0) P.adj.nsteps[id] = nsteps;
     __syncthreads();
     if (tid == 0) {
         st.outer_iters = outer;
@@ -1132,6 +1309,360 @@ __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
         if (q >= P.n_inst) break;
         integrate<LT>(P, P.order[q], smem, red, ired, mv, D, st, deadline);
     }
+}
+
+// ------------------------------------------------------------- adjoint
+
+// Fehlberg coefficients of the stages (kernels.cuh:79-143) and of the
+// 4th-order solution kept on acceptance (kernels.cuh:172).
+__constant__ double kRkA[6][5] = {
+    {0, 0, 0, 0, 0},
+    {1.0 / 4.0, 0, 0, 0, 0},
+    {3.0 / 32.0, 9.0 / 32.0, 0, 0, 0},
+    {1932.0 / 2197.0, -7200.0 / 2197.0, 7296.0 / 2197.0, 0, 0},
+    {439.0 / 216.0, -8.0, 3680.0 / 513.0, -845.0 / 4104.0, 0},
+    {-8.0 / 27.0, 2.0, -3544.0 / 2565.0, 1859.0 / 4104.0, -11.0 / 40.0}};
+__constant__ double kRkB[5] = {25.0 / 216.0, 0.0, 1408.0 / 2565.0, 2197.0 / 4104.0, -1.0 / 5.0};
+
+// Stage inputs Y[0..4] and slopes K[0..4] of an RKF45 step of size dt from y
+// (Y[0] may alias y), with the forward attempt's exact arithmetic, so a
+// recomputed step equals the forward one bit for bit; fed species take the
+// feed as slope and 0 as later stage input.  w (optional) receives the
+// 4th-order solution.
+__device__ void rkf_stages(const Net &m, const double *y, double dt, const double *fd,
+                           double *const *Y, double *const *K, double *pw, double *w) {
+    const int N = m.n, tid = threadIdx.x;
+    if (Y[0] != y) {
+        for (int s = tid; s < N; s += kThreads) Y[0][s] = y[s];
+    }
+    for (int s = tid; s < N; s += kThreads)
+        for (int i = 1; i < 5; i++) Y[i][s] = 0.0;
+    __syncthreads();
+    for (int st = 0; st < 5; st++) {
+        rhs_phase1(m, Y[st], pw);
+        __syncthreads();
+        for (int s = tid; s < N; s += kThreads) {
+            const double f = rhs_species(m, s, pw);
+            if (fd[s] != 0.0) {
+                K[st][s] = fd[s];
+                continue;
+            }
+            K[st][s] = f * dt;
+            const double y0 = y[s];
+            const double *k1 = K[0], *k2 = K[1], *k3 = K[2], *k4 = K[3], *k5 = K[4];
+            if (st == 0) Y[1][s] = y0 + k1[s] / 4.0;
+            else if (st == 1) Y[2][s] = y0 + (3.0 * k1[s]) / 32.0 + (9.0 * k2[s]) / 32.0;
+            else if (st == 2)
+                Y[3][s] = y0 + (1932.0 * k1[s]) / 2197.0 - (7200.0 * k2[s]) / 2197.0 +
+                          (7296.0 * k3[s]) / 2197.0;
+            else if (st == 3)
+                Y[4][s] = y0 + (439.0 * k1[s]) / 216.0 - (8.0 * k2[s]) +
+                          (3680.0 * k3[s]) / 513.0 - (845.0 * k4[s]) / 4104.0;
+            else if (w)
+                w[s] = y0 + (25.0 * k1[s]) / 216.0 + (1408.0 * k3[s]) / 2565.0 +
+                       (2197.0 * k4[s]) / 4104.0 - k5[s] / 5.0;
+        }
+        __syncthreads();
+    }
+    if (w) {
+        for (int s = tid; s < N; s += kThreads)
+            if (fd[s] != 0.0) w[s] = fd[s];
+        __syncthreads();
+    }
+}
+
+struct AdjSmem {
+    int64_t vec, kk, pw, tq, theta, rptr, sptr, sent, rent, hrptr, hrent, asptr, asent, perm,
+        slot, bvec, lt, utile, rowbuf, total;
+    __host__ __device__ AdjSmem(int nmax, int rmax, int amax, int hmax) {
+        auto al = [](int64_t v) { return (v + 15) & ~int64_t(15); };
+        const int PB = LuShape<float>::PB;
+        int64_t o = 0;
+        vec = o;    o = al(o + int64_t(16) * nmax * 8);
+        kk = o;     o = al(o + int64_t(rmax) * 8);
+        pw = o;     o = al(o + int64_t(amax > 0 ? amax : 1) * 8);
+        tq = o;     o = al(o + int64_t(amax > 0 ? amax : 1) * 8);
+        theta = o;  o = al(o + int64_t(rmax) * 8);
+        rptr = o;   o = al(o + int64_t(rmax + 1) * 4);
+        sptr = o;   o = al(o + int64_t(nmax + 1) * 4);
+        sent = o;   o = al(o + int64_t(hmax > 0 ? hmax : 1) * 4);
+        rent = o;   o = al(o + int64_t(amax > 0 ? amax : 1) * 4);
+        hrptr = o;  o = al(o + int64_t(rmax + 1) * 4);
+        hrent = o;  o = al(o + int64_t(hmax > 0 ? hmax : 1) * 4);
+        asptr = o;  o = al(o + int64_t(nmax + 1) * 4);
+        asent = o;  o = al(o + int64_t(amax > 0 ? amax : 1) * 4);
+        perm = o;   o = al(o + int64_t(nmax) * 4);
+        slot = o;   o = al(o + int64_t(nmax) * 4);
+        bvec = o;   o = al(o + int64_t(nmax) * 4);
+        lt = o;     o = al(o + (int64_t(PB) * ((nmax + 3) & ~3) + 160) * 4);
+        utile = o;  o = al(o + int64_t(PB) * 128 * 4);
+        rowbuf = o; o = al(o + int64_t(2 * PB) * 4);
+        total = o;
+    }
+};
+
+// Backward pass of one instance: the discrete adjoint of its recorded step
+// sequence for L = sum over samples and sampled species of (y - target)^2.
+// Accepted RKF45 steps: reverse stage recursion with J^T products at the
+// recomputed stage inputs.  Backward-Euler steps y' = y + h f(y') (taken as
+// exactly solved): (I - h J(y'))^T mu = lambda with an FP32 LU of the exact
+// Jacobian and FP64 refinement; lambda <- mu.  d L / d log k accumulates
+// h * prop_j * (S^T kbar)_j at every stage and step.
+__device__ void adjoint_instance(const LaunchParams &P, int id, unsigned char *smem, double *red,
+                                 int *ired, int *mv, InstDesc &D, double *cyc_dummy) {
+    const int tid = threadIdx.x;
+    if (tid == 0) D = P.inst[id];
+    __syncthreads();
+    const AdjDesc AD = P.adj.desc[id];
+    const int N = D.n, R = D.r;
+    const AdjSmem L(P.nmax, P.rmax, P.amax, P.hmax);
+    double *vb = reinterpret_cast<double *>(smem + L.vec);
+    double *lam = vb, *lnew = vb + P.nmax, *kbar = vb + 2 * P.nmax, *fd = vb + 3 * P.nmax;
+    double *Y[5], *Yb[5], *Kst[5];
+    for (int i = 0; i < 5; i++) Y[i] = vb + (4 + i) * P.nmax;
+    for (int i = 1; i < 5; i++) Yb[i] = vb + (8 + i) * P.nmax;  // slots 9..12
+    Yb[0] = nullptr;
+    // slopes alias the adjoint stage vectors Yb (not live while stages are built)
+    Kst[0] = vb + 13 * P.nmax;
+    Kst[1] = vb + 14 * P.nmax;
+    Kst[2] = vb + 15 * P.nmax;
+    Kst[3] = Yb[1];
+    Kst[4] = Yb[2];
+    double *kk = reinterpret_cast<double *>(smem + L.kk);
+    double *pw = reinterpret_cast<double *>(smem + L.pw);
+    double *tq = reinterpret_cast<double *>(smem + L.tq);
+    double *theta = reinterpret_cast<double *>(smem + L.theta);
+    int *rptr = reinterpret_cast<int *>(smem + L.rptr);
+    int *s_sptr = reinterpret_cast<int *>(smem + L.sptr);
+    int *s_sent = reinterpret_cast<int *>(smem + L.sent);
+    int *s_rent = reinterpret_cast<int *>(smem + L.rent);
+    int *s_hrptr = reinterpret_cast<int *>(smem + L.hrptr);
+    int *s_hrent = reinterpret_cast<int *>(smem + L.hrent);
+    int *s_asptr = reinterpret_cast<int *>(smem + L.asptr);
+    int *s_asent = reinterpret_cast<int *>(smem + L.asent);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    int *slot = reinterpret_cast<int *>(smem + L.slot);
+    float *bvec = reinterpret_cast<float *>(smem + L.bvec);
+    float *lt = reinterpret_cast<float *>(smem + L.lt);
+    float *utile = reinterpret_cast<float *>(smem + L.utile);
+    float *rowbuf = reinterpret_cast<float *>(smem + L.rowbuf);
+    const int *ia = P.iarena;
+    const double *da = P.darena;
+    for (int q = tid; q < D.nnz_a; q += kThreads) s_rent[q] = ia[D.rxn_ent + q];
+    for (int q = tid; q < D.nnz_h; q += kThreads) {
+        s_sent[q] = ia[D.sp_ent + q];
+        s_hrent[q] = ia[D.hr_ent + q];
+    }
+    for (int q = tid; q <= N; q += kThreads) {
+        s_sptr[q] = ia[D.sp_ptr + q];
+        s_asptr[q] = ia[D.as_ptr + q];
+    }
+    for (int q = tid; q < D.nnz_a; q += kThreads) s_asent[q] = ia[D.as_ent + q];
+    for (int j = tid; j <= R; j += kThreads) {
+        rptr[j] = ia[D.rxn_ptr + j];
+        s_hrptr[j] = ia[D.hr_ptr + j];
+    }
+    for (int j = tid; j < R; j += kThreads) {
+        kk[j] = da[D.k + j];
+        theta[j] = 0.0;
+    }
+    for (int s = tid; s < N; s += kThreads) {
+        fd[s] = D.feed >= 0 ? da[D.feed + s] : 0.0;
+        lam[s] = 0.0;
+    }
+    __syncthreads();
+    Net m;
+    m.n = N;
+    m.r = R;
+    m.nnz_a = D.nnz_a;
+    m.rent = s_rent;
+    m.sptr = s_sptr;
+    m.sent = s_sent;
+    m.rptr = rptr;
+    m.kk = kk;
+    AdjNet an{s_hrptr, s_hrent, s_asptr, s_asent};
+
+    const int *cs = D.cs >= 0 ? ia + D.cs : nullptr;
+    const int ncs = D.ncs;
+    const double *target = P.adj.target + D.out;
+    const int *samp = P.adj.samp_step + AD.samp;
+    const int *rk = P.adj.rec_kind + AD.rec;
+    const double *rdt = P.adj.rec_dt + AD.rec;
+    const int *rslot = P.adj.rec_slot + AD.rec;
+    const double *states = P.adj.states + AD.states;
+    double *buf = P.adj.scratch + (int64_t)blockIdx.x * P.adj.scratch_stride;
+    float *M = reinterpret_cast<float *>(P.workspace + (int64_t)blockIdx.x * P.ws_stride);
+    const int ld = round_up4(N);
+    float *dinv = M + (int64_t)N * ld;
+    const int ns = P.adj.nsteps[id];
+    int ip = D.nt - 1;
+    // samples taken at state index `si`: lambda += 2 (y - target) on sampled species
+    auto add_samples = [&](int si, const double *y) {
+        while (ip >= 0 && samp[ip] == si) {
+            for (int j = tid; j < ncs; j += kThreads) {
+                const int sp = cs ? cs[j] : j;
+                lam[sp] += 2.0 * (y[sp] - target[(int64_t)ip * ncs + j]);
+            }
+            __syncthreads();
+            ip--;
+        }
+    };
+    while (ip >= 0 && samp[ip] > ns) ip--;  // (not expected) samples past the record
+    int n = ns - 1;
+    while (n >= 0) {
+        int p = n;
+        while (p > 0 && rslot[p - 1] < 0) p--;
+        const int sp0 = (p == 0) ? 0 : rslot[p - 1];
+        for (int s = tid; s < N; s += kThreads) buf[s] = states[(int64_t)sp0 * N + s];
+        __syncthreads();
+        for (int q = p; q <= n; q++) {
+            double *yo = buf + (int64_t)(q - p + 1) * N;
+            if (rslot[q] >= 0) {
+                for (int s = tid; s < N; s += kThreads) yo[s] = states[(int64_t)rslot[q] * N + s];
+                __syncthreads();
+            } else {
+                rkf_stages(m, buf + (int64_t)(q - p) * N, rdt[q], fd, Y, Kst, pw, yo);
+            }
+        }
+        for (int q = n; q >= p; q--) {
+            const double *yin = buf + (int64_t)(q - p) * N;
+            const double *yout = buf + (int64_t)(q - p + 1) * N;
+            add_samples(q + 1, yout);
+            const int kind = rk[q];
+            const double h = rdt[q];
+            if (kind == 0) {
+                rkf_stages(m, yin, h, fd, Y, Kst, pw, nullptr);
+                for (int s = tid; s < N; s += kThreads) lnew[s] = (fd[s] != 0.0) ? 0.0 : lam[s];
+                __syncthreads();
+                for (int i = 4; i >= 0; i--) {
+                    for (int s = tid; s < N; s += kThreads) {
+                        double kb = 0.0;
+                        if (fd[s] == 0.0) {
+                            kb = kRkB[i] * lam[s];
+                            for (int mm = i + 1; mm < 5; mm++) kb += kRkA[mm][i] * Yb[mm][s];
+                        }
+                        kbar[s] = kb;
+                    }
+                    __syncthreads();
+                    jtv_phase1(m, an, Y[i], kbar, tq, theta, h);
+                    __syncthreads();
+                    for (int s = tid; s < N; s += kThreads) {
+                        double yb = h * jtv_species(an, s, tq);
+                        if (i >= 1 && fd[s] != 0.0) yb = 0.0;
+                        if (i >= 1) Yb[i][s] = yb;
+                        lnew[s] += yb;
+                    }
+                    __syncthreads();
+                }
+                for (int s = tid; s < N; s += kThreads) lam[s] = lnew[s];
+                __syncthreads();
+            } else if (kind == 1) {
+                // (I - h D J(y'))^T mu = lambda, D masks fed rows
+                double *mu = Y[0], *res = Y[1], *mdiag = Y[2], *vm = Y[3];
+                assemble_newton_matrix<float>(m, yout, h, M, ld, true, fd);
+                for (int s = tid; s < N; s += kThreads) mdiag[s] = (double)M[(int64_t)s * ld + s];
+                const int fail = lu_factor<float>(M, ld, N, perm, slot, lt, utile, rowbuf, red,
+                                                  ired, mv, reinterpret_cast<long long *>(cyc_dummy));
+                if (fail == 0) {
+                    invert_diag_blocks(M, ld, N, dinv);
+                    __syncthreads();
+                    double rloc = 0.0;
+                    for (int s = tid; s < N; s += kThreads) {
+                        mu[s] = 0.0;
+                        res[s] = lam[s];
+                        rloc = fmax(rloc, fabs(lam[s]));
+                    }
+                    double rmax = block_max(rloc, red);
+                    double prev = INFINITY;
+                    for (int sweep = 0; sweep < 12; sweep++) {
+                        if (!(rmax > 0.0) || isinf(rmax)) break;
+                        const int e = ilogb(rmax);
+                        const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
+                        for (int s = tid; s < N; s += kThreads) bvec[s] = (float)(res[s] * sc);
+                        __syncthreads();
+                        lu_solve_fast_T(M, ld, N, dinv, bvec);
+                        double cmax = 0.0, xmax = 0.0;
+                        for (int i2 = tid; i2 < N; i2 += kThreads) {
+                            const int s = perm[i2];
+                            double c = (double)bvec[i2] * isc;
+                            const double rs = res[s] * sc;
+                            if (fabs(rs) < 0x1p-126 && fabs(mdiag[s]) >= 0.5)
+                                c += (rs - (double)(float)rs) * isc / mdiag[s];
+                            const double nx = mu[s] + c;
+                            mu[s] = nx;
+                            cmax = fmax(cmax, fabs(c));
+                            xmax = fmax(xmax, fabs(nx));
+                        }
+                        cmax = block_max(cmax, red);
+                        xmax = block_max(xmax, red);
+                        const bool small_next = sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
+                        if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) || small_next) break;
+                        prev = cmax;
+                        // res = lambda - (mu - h J^T (D mu))
+                        for (int s = tid; s < N; s += kThreads) vm[s] = (fd[s] != 0.0) ? 0.0 : mu[s];
+                        __syncthreads();
+                        jtv_phase1(m, an, yout, vm, tq, nullptr, h);
+                        __syncthreads();
+                        rloc = 0.0;
+                        for (int s = tid; s < N; s += kThreads) {
+                            const double r = lam[s] - (mu[s] - h * jtv_species(an, s, tq));
+                            res[s] = r;
+                            rloc = fmax(rloc, fabs(r));
+                        }
+                        rmax = block_max(rloc, red);
+                    }
+                    for (int s = tid; s < N; s += kThreads) vm[s] = (fd[s] != 0.0) ? 0.0 : mu[s];
+                    __syncthreads();
+                    jtv_phase1(m, an, yout, vm, tq, theta, h);  // d/dlog k contributions
+                    __syncthreads();
+                    for (int s = tid; s < N; s += kThreads) lam[s] = vm[s];
+                    __syncthreads();
+                }
+            }
+            // kinds 2 and 3 (state unchanged / reverted species): identity
+        }
+        n = p - 1;
+        if (n < 0) add_samples(0, buf);
+    }
+    if (ns == 0) {
+        for (int s = tid; s < N; s += kThreads) buf[s] = states[s];
+        __syncthreads();
+        add_samples(0, buf);
+    }
+    double *g = P.adj.grad + AD.grad;
+    for (int j = tid; j < R; j += kThreads) g[j] = theta[j];
+    for (int s = tid; s < N; s += kThreads) g[R + s] = lam[s];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads, 1) adjoint_kernel(LaunchParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[kWarps + 1];
+    __shared__ int ired[kWarps + 2 + LuShape<float>::PB];
+    __shared__ int mv[4 * LuShape<float>::PB];
+    __shared__ InstDesc D;
+    __shared__ double cyc[4];
+    __shared__ int next;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(P.queue, 1);
+        __syncthreads();
+        const int q = next;
+        __syncthreads();
+        if (q >= P.n_inst) break;
+        adjoint_instance(P, P.order[q], smem, red, ired, mv, D, cyc);
+    }
+}
+
+int64_t adjoint_smem_bytes(int nmax, int rmax, int amax, int hmax) {
+    return AdjSmem(nmax, rmax, amax, hmax).total;
+}
+
+cudaError_t adjoint_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(adjoint_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    adjoint_kernel<<<grid, kThreads, smem, stream>>>(P);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------- launch

@@ -228,10 +228,43 @@ void lo_lu_solve(int n, const double *lu, const int *piv, double *b) {
      the identical matrix at every Newton iteration, with identical results;
    - the Newton norm sums in index order (thrust's order in the reference);
      only its comparison with newton_tol is used. */
+typedef struct {
+    int cap;
+    int *kind;     /* 0 accepted RKF45, 1 backward Euler, 2 unchanged, 3 reverted */
+    double *dt;
+    int *nsteps;
+    int *samp;     /* steps taken before each sample */
+} lo_record;
+
+static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
+                         const double *feed, const double *atol, const double *tv,
+                         int nt, const int *cs, int ncs, const lo_opts *opts_in,
+                         double *out, lo_stats *st_out, lo_record *rec);
+
 int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
                     const double *feed, const double *atol, const double *tv,
                     int nt, const int *cs, int ncs, const lo_opts *opts_in,
                     double *out, lo_stats *st_out) {
+    return lo_solve_impl(m, k, x0, feed, atol, tv, nt, cs, ncs, opts_in, out, st_out, NULL);
+}
+
+/* As lo_solve_compat, also recording the step sequence (kind and step size
+   of every state-changing step, and the steps taken before each sample) for
+   the sensitivity checks of the adjoint. */
+int lo_solve_compat_rec(const lo_model *m, const double *k, const double *x0,
+                        const double *feed, const double *atol, const double *tv,
+                        int nt, const int *cs, int ncs, const lo_opts *opts_in,
+                        double *out, lo_stats *st_out, int cap, int *kind, double *dt,
+                        int *nsteps, int *samp) {
+    lo_record r = {cap, kind, dt, nsteps, samp};
+    *nsteps = 0;
+    return lo_solve_impl(m, k, x0, feed, atol, tv, nt, cs, ncs, opts_in, out, st_out, &r);
+}
+
+static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
+                         const double *feed, const double *atol, const double *tv,
+                         int nt, const int *cs, int ncs, const lo_opts *opts_in,
+                         double *out, lo_stats *st_out, lo_record *rec) {
     lo_opts o;
     if (opts_in)
         o = *opts_in;
@@ -287,6 +320,7 @@ int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
         /* Simulation.cuh:674-690 */
         if (fabs(t1 - t) < 1e-5) {
             for (int j = 0; j < ncs; j++) out[(size_t)i * ncs + j] = y1[cs ? cs[j] : j];
+            if (rec) rec->samp[i] = *rec->nsteps;
             i++;
             if (i >= nt) break;
             t1 = tv[i];
@@ -363,6 +397,15 @@ int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
         if (count == N) {
             /* accept: Simulation.cuh:742-768 */
             memcpy(y1, w1, sizeof(double) * N);
+            if (rec) {
+                if (*rec->nsteps >= rec->cap) {
+                    status = LO_ERR_MAX_STEPS;
+                    break;
+                }
+                rec->kind[*rec->nsteps] = 0;
+                rec->dt[*rec->nsteps] = dt;
+                (*rec->nsteps)++;
+            }
             double d_temp = dt * dmin;
             if ((t + d_temp) > t1) dt = fabs(t1 - t);
             else dt = d_temp;
@@ -419,6 +462,7 @@ int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
                     itN = itN + 1;
                     st.newton_iters++;
                 }
+                int reverted = 0;
                 if (!luFail) {
                     /* Simulation.cuh:894-909 */
                     int bad = 0;
@@ -429,7 +473,17 @@ int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
                             if (isnan(yv[s]) || isinf(yv[s]) || yv[s] < 0) yv[s] = y1[s];
                         newDtBDF = dt * 0.1;
                         st.nan_reverts++;
+                        reverted = 1;
                     }
+                }
+                if (rec) {
+                    if (*rec->nsteps >= rec->cap) {
+                        status = LO_ERR_MAX_STEPS;
+                        break;
+                    }
+                    rec->kind[*rec->nsteps] = luFail ? 2 : (reverted ? 3 : 1);
+                    rec->dt[*rec->nsteps] = dt;
+                    (*rec->nsteps)++;
                 }
                 memcpy(y1, yv, sizeof(double) * N);
                 t = t + dt;

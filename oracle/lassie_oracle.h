@@ -93,6 +93,16 @@ int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
                     int nt, const int *cs, int ncs, const lo_opts *opts,
                     double *out, lo_stats *stats);
 
+/* As lo_solve_compat, recording the step sequence: kind[n] (0 accepted
+   RKF45, 1 backward Euler, 2 state unchanged, 3 reverted species) and dt[n]
+   of every state-changing step, *nsteps, and samp[i] = steps taken before
+   sample i.  Returns LO_ERR_MAX_STEPS when more than cap steps are taken. */
+int lo_solve_compat_rec(const lo_model *m, const double *k, const double *x0,
+                        const double *feed, const double *atol, const double *t,
+                        int nt, const int *cs, int ncs, const lo_opts *opts,
+                        double *out, lo_stats *stats, int cap, int *kind, double *dt,
+                        int *nsteps, int *samp);
+
 /* Batch of independent instances solved on `threads` host threads
    (the CPU baseline).  Arrays are per-instance pointers. */
 int lo_solve_batch(int n_inst, const lo_model *const *models,

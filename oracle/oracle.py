@@ -73,6 +73,11 @@ def lib():
                                           C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Opts), _f64p, C.POINTER(Stats)]
             L.lo_solve_compat.restype = C.c_int
+            L.lo_solve_compat_rec.argtypes = [C.POINTER(_Model), _f64p, _f64p, C.c_void_p,
+                                              C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
+                                              C.POINTER(Opts), _f64p, C.POINTER(Stats), C.c_int,
+                                              _i32p, _f64p, C.POINTER(C.c_int), _i32p]
+            L.lo_solve_compat_rec.restype = C.c_int
             L.lo_solve_batch.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.c_void_p, _i32p, C.POINTER(Opts), C.c_void_p,
                                          C.c_void_p, _i32p, C.c_int]
@@ -145,6 +150,30 @@ def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None):
                                t.shape[0], _ptr(cs), cs.shape[0], C.byref(o), out,
                                C.byref(st))
     return out, st.as_dict(), rc
+
+
+def solve_recorded(model, cap: int = 1_000_000):
+    """Integrate and return (trajectory, stats, status, kinds, dts, samp):
+    the step sequence of the integration, for sensitivity checks."""
+    om = OracleModel(model.left, model.right)
+    N = model.n_species
+    k = np.ascontiguousarray(model.k, np.float64)
+    x0 = np.ascontiguousarray(model.x0[:N], np.float64)
+    t = np.ascontiguousarray(model.t, np.float64)
+    cs = model.sampled().astype(np.int32)
+    feed = None if model.feed is None else np.ascontiguousarray(model.feed[:N], np.float64)
+    out = np.zeros((t.shape[0], cs.shape[0]))
+    st = Stats()
+    o = make_opts(model)
+    kind = np.zeros(cap, np.int32)
+    dts = np.zeros(cap)
+    ns = C.c_int(0)
+    samp = np.zeros(max(1, t.shape[0]), np.int32)
+    rc = lib().lo_solve_compat_rec(C.byref(om._m), k, x0, _ptr(feed), None, t, t.shape[0],
+                                   _ptr(cs), cs.shape[0], C.byref(o), out, C.byref(st), cap,
+                                   kind, dts, C.byref(ns), samp)
+    n = ns.value
+    return out, st.as_dict(), rc, kind[:n].copy(), dts[:n].copy(), samp[: t.shape[0]].copy()
 
 
 def solve_batch(models: Sequence, threads: int = 0, max_steps: int = 0):
