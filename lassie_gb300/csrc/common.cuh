@@ -93,8 +93,8 @@ struct LaunchParams {
 
 // Dynamic shared-memory layout of the integrator (bytes), identical on host
 // and device.  Vectors are FP64 N-vectors; the sparse structure of the
-// network is staged here too; lt holds the factor panel transposed
-// (PB x round_up4(N), plus slack for the 8-row tile reads past its end),
+// network is staged here too; lt holds the factor panel column-major
+// (PB x (round_up32(N) + 4), plus slack for the 8-row tile reads past its end),
 // utile one PB x 128 tile of U12, rowbuf the pivot and swap rows.
 struct SmemLayout {
     int64_t vec, kk, pw, qr, rptr, sptr, sent, rent, perm, slot, bvec, lt, utile, rowbuf, total;
@@ -113,7 +113,7 @@ struct SmemLayout {
         perm = o;   o = align(o + int64_t(nmax) * 4);
         slot = o;   o = align(o + int64_t(nmax) * 4);
         bvec = o;   o = align(o + int64_t(nmax) * lt_bytes);
-        lt = o;     o = align(o + (int64_t(pb) * ((nmax + 3) & ~3) + 160) * lt_bytes);
+        lt = o;     o = align(o + (int64_t(pb) * (((nmax + 31) & ~31) + 4) + 160) * lt_bytes);
         utile = o;  o = align(o + int64_t(pb) * tn * lt_bytes);
         rowbuf = o; o = align(o + int64_t(2 * pb) * lt_bytes);
         total = o;

@@ -313,179 +313,132 @@ __device__ __forceinline__ void load4(const double *p, double *o) {
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
 }
 
-// In-place blocked right-looking LU with partial pivoting on M (row-major,
-// leading dimension ld), N <= kThreads.  Every element receives
-// a = fma(-l, u, a) once per pivot in pivot order, as in the unblocked
-// algorithm, so the factors equal the oracle's bit for bit.
-//   panel: thread r holds row j0+r of the PB-column panel in registers; per
-//          pivot one barrier publishes the arg-max partials and one the pivot
-//          row (row interchanges are register swaps through shared memory);
-//   other columns: the panel's net row moves (recorded by thread 0 in
-//          slot/mv) with independent loads, then the unit-lower solve for
-//          the U12 rows (L11 from shared memory);
+// In-place blocked right-looking LU with partial pivoting, N <= kThreads, on
+// M (row-major, leading dimension ld) with implicit row interchanges: logical
+// row i of P*A is physical row perm[i] of M, and no row is ever moved.
+// Every element receives a = fma(-l, u, a) once per pivot in pivot order, as
+// in the unblocked algorithm, so the factors equal the oracle's bit for bit.
+//   panel: shared memory, column-major (lt), one row position per thread;
+//          per pivot one barrier publishes the arg-max partials and one the
+//          pivot row; thread jj moves the pivot row into place and eliminates
+//          the displaced row, so no position has two writers;
+//   U12:   unit-lower solve, one column per thread (L11 from lt);
 //   trailing update: 128 x 128 tiles, thread (ty,tx) owns rows ty*8.. and
-//          columns tx*4..; L21 is kept transposed in shared memory (lt) and
-//          U12 is staged per column tile (utile), both read with 16-byte loads.
-// perm[i] = source row of row i of P*A.  Returns 0, or j+1 if the pivot of
-// column j is exactly zero (uniform across the CTA).
+//          columns tx*4..; L21 is read from lt and U12 from a staged tile
+//          (utile), both with 16-byte loads.
+// Returns 0, or j+1 if the pivot of column j is exactly zero (uniform).
 template <typename LT>
-__device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot, LT *lt,
-                                      LT *utile, LT *rowbuf, double *red, int *ired, int *mv,
-                                      long long *cyc) {
+__device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, LT *utile,
+                                      LT *rowbuf, double *red, int *ired, long long *cyc) {
     constexpr int PB = LuShape<LT>::PB;
     constexpr int TN = 128, TM = 128;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    int *mv_dst = mv, *mv_src = mv + 2 * PB;
     LT *pivrow = rowbuf, *swaprow = rowbuf + PB;
-    for (int i = tid; i < N; i += kThreads) {
-        perm[i] = i;
-        slot[i] = -1;
-    }
+    for (int i = tid; i < N; i += kThreads) perm[i] = i;
     __syncthreads();
     int fail = 0;
     long long c_a = clock64();
     for (int j0 = 0; j0 < N; j0 += PB) {
         const int pb = min(PB, N - j0);
         const int m = N - j0;
-        const int mp = round_up4(m);
-        const bool mine = tid < m;
-        LT row[PB];
-#pragma unroll
-        for (int c = 0; c < PB; c++)
-            row[c] = (mine && c < pb) ? M[(int64_t)(j0 + tid) * ld + j0 + c] : LT(0);
-        if (tid == 0) ired[kWarps] = 0;  // number of recorded row moves
+        // panel column-major in lt: lt[c*mp + r]; mp = 4 mod 32 keeps the
+        // transposed writes at 4-way bank conflicts and rows 16-byte aligned
+        const int mp = ((m + 31) & ~31) + 4;
+        for (int idx = tid; idx < m * PB; idx += kThreads) {
+            const int r = idx / PB, c = idx - r * PB;
+            lt[c * mp + r] = (c < pb) ? M[(int64_t)perm[j0 + r] * ld + j0 + c] : LT(0);
+        }
+        __syncthreads();
         Piv best{-1.0, 1 << 30};
-        if (mine) {
-            const double v = fabs((double)row[0]);
+        if (tid < m) {
+            const double v = fabs((double)lt[tid]);
             if (!isnan(v)) best = Piv{v, tid};
         }
-#pragma unroll
-        for (int jj = 0; jj < PB; jj++) {
-            if (jj < pb) {
-                for (int o = 16; o > 0; o >>= 1) {
-                    Piv other{__shfl_xor_sync(0xffffffffu, best.v, o),
-                              __shfl_xor_sync(0xffffffffu, best.i, o)};
-                    best = piv_better(best, other);
+        for (int jj = 0; jj < pb; jj++) {
+            for (int o = 16; o > 0; o >>= 1) {
+                Piv other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                          __shfl_xor_sync(0xffffffffu, best.i, o)};
+                best = piv_better(best, other);
+            }
+            if (lane == 0) {
+                red[warp] = best.v;
+                ired[warp] = best.i;
+            }
+            __syncthreads();
+            Piv all{red[0], ired[0]};
+            for (int q = 1; q < kWarps; q++) all = piv_better(all, Piv{red[q], ired[q]});
+            int p = all.i;
+            // a NaN in the diagonal position keeps its own row (oracle rule)
+            if (isnan((double)lt[jj * mp + jj]) || p >= m) p = jj;
+            if (tid < PB) {
+                pivrow[tid] = lt[tid * mp + p];
+                swaprow[tid] = lt[tid * mp + jj];
+            }
+            if (tid == 0 && p != jj) {
+                int tmp = perm[j0 + jj];
+                perm[j0 + jj] = perm[j0 + p];
+                perm[j0 + p] = tmp;
+            }
+            __syncthreads();
+            const LT d = pivrow[jj];
+            if (d == LT(0)) {
+                fail = j0 + jj + 1;
+                break;
+            }
+            best = Piv{-1.0, 1 << 30};
+            if (tid > jj && tid < m && tid != p) {
+                // own row, untouched by the interchange
+                const LT l = lt[jj * mp + tid] / d;
+                lt[jj * mp + tid] = l;
+                for (int c = jj + 1; c < pb; c++)
+                    lt[c * mp + tid] = lt_fma(-l, pivrow[c], lt[c * mp + tid]);
+                if (jj + 1 < pb) {
+                    const double v = fabs((double)lt[(jj + 1) * mp + tid]);
+                    if (!isnan(v)) best = Piv{v, tid};
                 }
-                if (lane == 0) {
-                    red[warp] = best.v;
-                    ired[warp] = best.i;
-                }
-                if (tid == jj) ired[kWarps + 1] = isnan((double)row[jj]) ? 1 : 0;
-                __syncthreads();
-                Piv all{red[0], ired[0]};
-                for (int q = 1; q < kWarps; q++) all = piv_better(all, Piv{red[q], ired[q]});
-                int p = all.i;
-                // a NaN in the diagonal position keeps its own row (oracle rule)
-                if (ired[kWarps + 1] || p >= m) p = jj;
-                if (tid == p) {
-#pragma unroll
-                    for (int c = 0; c < PB; c++) pivrow[c] = row[c];
-                }
-                if (tid == jj && p != jj) {
-#pragma unroll
-                    for (int c = 0; c < PB; c++) swaprow[c] = row[c];
-                }
-                if (tid == 0 && p != jj) {
-                    int tmp = perm[j0 + jj];
-                    perm[j0 + jj] = perm[j0 + p];
-                    perm[j0 + p] = tmp;
-                    // net move list: mv_src[k] = pre-panel row now at mv_dst[k]
-                    int n = ired[kWarps];
-                    int sa = slot[j0 + jj];
-                    if (sa < 0) {
-                        sa = n++;
-                        slot[j0 + jj] = sa;
-                        mv_dst[sa] = j0 + jj;
-                        mv_src[sa] = j0 + jj;
-                    }
-                    int sb = slot[j0 + p];
-                    if (sb < 0) {
-                        sb = n++;
-                        slot[j0 + p] = sb;
-                        mv_dst[sb] = j0 + p;
-                        mv_src[sb] = j0 + p;
-                    }
-                    int t2 = mv_src[sa];
-                    mv_src[sa] = mv_src[sb];
-                    mv_src[sb] = t2;
-                    ired[kWarps] = n;
-                }
-                __syncthreads();
-                const LT pv = pivrow[jj];
-                if (pv == LT(0)) {
-                    fail = j0 + jj + 1;
-                    break;
-                }
-                if (p != jj) {
-                    if (tid == jj) {
-#pragma unroll
-                        for (int c = 0; c < PB; c++) row[c] = pivrow[c];
-                    } else if (tid == p) {
-#pragma unroll
-                        for (int c = 0; c < PB; c++) row[c] = swaprow[c];
-                    }
-                }
-                best = Piv{-1.0, 1 << 30};
-                if (mine && tid > jj) {
-                    const LT l = row[jj] / pv;
-                    row[jj] = l;
-#pragma unroll
-                    for (int c = jj + 1; c < PB; c++) row[c] = lt_fma(-l, pivrow[c], row[c]);
-                    if (jj + 1 < pb) {
-                        const double v = fabs((double)row[jj + 1]);
-                        if (!isnan(v)) best = Piv{v, tid};
-                    }
+            } else if (tid == jj && p != jj) {
+                // the pivot row moves to position jj; the displaced row jj goes
+                // to position p and is eliminated there
+                for (int c = 0; c < pb; c++) lt[c * mp + jj] = pivrow[c];
+                const LT l = swaprow[jj] / d;
+                lt[jj * mp + p] = l;
+                for (int c = 0; c < jj; c++) lt[c * mp + p] = swaprow[c];
+                for (int c = jj + 1; c < pb; c++)
+                    lt[c * mp + p] = lt_fma(-l, pivrow[c], swaprow[c]);
+                if (jj + 1 < pb) {
+                    const double v = fabs((double)lt[(jj + 1) * mp + p]);
+                    if (!isnan(v)) best = Piv{v, p};
                 }
             }
         }
         if (fail) break;
         long long c_b = clock64();
         if (tid == 0) cyc[0] += c_b - c_a;
-        // panel back to global; L (and U11) transposed into lt[c*mp + r]
-        if (mine) {
+        __syncthreads();
+        // panel back to its physical rows
+        for (int idx = tid; idx < m * PB; idx += kThreads) {
+            const int r = idx / PB, c = idx - r * PB;
+            if (c < pb) M[(int64_t)perm[j0 + r] * ld + j0 + c] = lt[c * mp + r];
+        }
+        // U12: unit-lower triangular solve on the panel's rows, one column per
+        // thread
+        for (int c = j0 + pb + tid; c < N; c += kThreads) {
+            LT u[PB];
 #pragma unroll
-            for (int c = 0; c < PB; c++) {
-                if (c < pb) M[(int64_t)(j0 + tid) * ld + j0 + c] = row[c];
-                lt[c * mp + tid] = row[c];
+            for (int r = 0; r < PB; r++)
+                u[r] = (r < pb) ? M[(int64_t)perm[j0 + r] * ld + c] : LT(0);
+#pragma unroll
+            for (int r = 1; r < PB; r++) {
+                LT acc = u[r];
+#pragma unroll
+                for (int q = 0; q < r; q++) acc = lt_fma(-lt[q * mp + r], u[q], acc);
+                u[r] = acc;
             }
+#pragma unroll
+            for (int r = 1; r < PB; r++)
+                if (r < pb) M[(int64_t)perm[j0 + r] * ld + c] = u[r];
         }
         __syncthreads();
-        // columns outside the panel: the panel's row moves (all loads first,
-        // then all stores: the moves form a permutation), then the unit-lower
-        // triangular solve for the U12 block rows.
-        const int nmv = ired[kWarps];
-        for (int c = tid; c < N; c += kThreads) {
-            if (c >= j0 && c < j0 + pb) continue;
-            LT v[2 * PB];
-#pragma unroll
-            for (int k = 0; k < 2 * PB; k++)
-                if (k < nmv) v[k] = M[(int64_t)mv_src[k] * ld + c];
-#pragma unroll
-            for (int k = 0; k < 2 * PB; k++)
-                if (k < nmv) M[(int64_t)mv_dst[k] * ld + c] = v[k];
-        }
-        __syncthreads();
-        for (int c = tid; c < N; c += kThreads) {
-            if (c >= j0 + pb) {
-                LT u[PB];
-#pragma unroll
-                for (int r = 0; r < PB; r++)
-                    u[r] = (r < pb) ? M[(int64_t)(j0 + r) * ld + c] : LT(0);
-#pragma unroll
-                for (int r = 1; r < PB; r++) {
-                    LT acc = u[r];
-#pragma unroll
-                    for (int q = 0; q < r; q++) acc = lt_fma(-lt[q * mp + r], u[q], acc);
-                    u[r] = acc;
-                }
-#pragma unroll
-                for (int r = 1; r < PB; r++)
-                    if (r < pb) M[(int64_t)(j0 + r) * ld + c] = u[r];
-            }
-        }
-        __syncthreads();
-        for (int k = tid; k < nmv; k += kThreads) slot[mv_dst[k]] = -1;
         c_a = clock64();
         if (tid == 0) cyc[1] += c_a - c_b;
         // trailing update A22 -= L21 * U12 (pb == PB whenever columns remain)
@@ -497,7 +450,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
                 for (int idx = tid; idx < PB * TN; idx += kThreads) {
                     const int q = idx / TN, cc = idx - q * TN;
                     const int col = c0 + tn0 + cc;
-                    utile[idx] = (col < N) ? M[(int64_t)(j0 + q) * ld + col] : LT(0);
+                    utile[idx] = (col < N) ? M[(int64_t)perm[j0 + q] * ld + col] : LT(0);
                 }
                 __syncthreads();
                 for (int tm0 = 0; tm0 < m2; tm0 += TM) {
@@ -508,7 +461,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
                     for (int a = 0; a < 8; a++) {
                         const int r = j0 + rl + a;
                         if (r < N && col0 < ld) {
-                            load4(M + (int64_t)r * ld + col0, acc[a]);
+                            load4(M + (int64_t)perm[r] * ld + col0, acc[a]);
                         } else {
 #pragma unroll
                             for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
@@ -531,7 +484,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
                         if (r < N) {
 #pragma unroll
                             for (int b = 0; b < 4; b++)
-                                if (col0 + b < N) M[(int64_t)r * ld + col0 + b] = acc[a][b];
+                                if (col0 + b < N) M[(int64_t)perm[r] * ld + col0 + b] = acc[a][b];
                         }
                     }
                 }
@@ -551,7 +504,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, int *slot
 // accumulation then one division (the oracle's order).  Used by the FP64
 // form, whose results must equal the oracle's.
 template <typename LT>
-__device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
+__device__ __noinline__ void lu_solve(const LT *M, int ld, int N, const int *perm, LT *bvec) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // forward substitution, unit lower
     for (int r0 = 0; r0 < N; r0 += 32) {
@@ -561,7 +514,7 @@ __device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
             LT row[32];
 #pragma unroll
             for (int q = 0; q < 32; q++)
-                row[q] = (lane < nb && q < lane) ? M[(int64_t)(r0 + lane) * ld + r0 + q] : LT(0);
+                row[q] = (lane < nb && q < lane) ? M[(int64_t)perm[r0 + lane] * ld + r0 + q] : LT(0);
 #pragma unroll
             for (int q = 0; q < 32; q++) {
                 const LT bq = __shfl_sync(0xffffffffu, v, q);
@@ -571,7 +524,7 @@ __device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
         }
         __syncthreads();
         for (int i = r0 + nb + tid; i < N; i += kThreads) {
-            const LT *ri = M + (int64_t)i * ld + r0;
+            const LT *ri = M + (int64_t)perm[i] * ld + r0;
             LT seg[32];
 #pragma unroll
             for (int q = 0; q < 32; q++) seg[q] = (q < nb) ? ri[q] : LT(0);
@@ -593,7 +546,7 @@ __device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
             LT row[32];
 #pragma unroll
             for (int q = 0; q < 32; q++)
-                row[q] = (lane < nb && q >= lane && q < nb) ? M[(int64_t)(r0 + lane) * ld + r0 + q]
+                row[q] = (lane < nb && q >= lane && q < nb) ? M[(int64_t)perm[r0 + lane] * ld + r0 + q]
                                                             : LT(1);
 #pragma unroll
             for (int q = 31; q >= 0; q--) {
@@ -608,7 +561,7 @@ __device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
         }
         __syncthreads();
         for (int i = tid; i < r0; i += kThreads) {
-            const LT *ri = M + (int64_t)i * ld + r0;
+            const LT *ri = M + (int64_t)perm[i] * ld + r0;
             LT seg[32];
 #pragma unroll
             for (int q = 0; q < 32; q++) seg[q] = (q < nb) ? ri[q] : LT(0);
@@ -626,7 +579,8 @@ __device__ __noinline__ void lu_solve(const LT *M, int ld, int N, LT *bvec) {
 // dinv[b*2048 + i*32 + j] (L^-1) and dinv[b*2048 + 1024 + i*32 + j] (U^-1);
 // rows/columns past N are identity.  One warp per block, lane j builds
 // column j by substitution on the block rows held in registers.
-__device__ __noinline__ void invert_diag_blocks(const float *M, int ld, int N, float *dinv) {
+__device__ __noinline__ void invert_diag_blocks(const float *M, int ld, int N, const int *perm,
+                                                float *dinv) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nblk = (N + 31) / 32;
     for (int b = warp; b < nblk; b += kWarps) {
@@ -635,7 +589,7 @@ __device__ __noinline__ void invert_diag_blocks(const float *M, int ld, int N, f
         float row[32];  // row `lane` of the diagonal block (identity past nb)
 #pragma unroll
         for (int k = 0; k < 32; k++)
-            row[k] = (lane < nb && k < nb) ? M[(int64_t)(r0 + lane) * ld + r0 + k]
+            row[k] = (lane < nb && k < nb) ? M[(int64_t)perm[r0 + lane] * ld + r0 + k]
                                           : (lane == k ? 1.f : 0.f);
         float x[32];
         // L^-1 column `lane`: unit lower
@@ -682,7 +636,8 @@ __device__ __forceinline__ void load_seg32(const float *M, int ld, int r, int c0
 // FP32 form solve: 32-row block steps; the diagonal blocks are applied as
 // their inverses (one 32 x 32 matvec by warp 0), the off-diagonal rows update
 // with row segments loaded before the block step's barrier.
-__device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const float *dinv, float *bvec) {
+__device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const int *perm,
+                                           const float *dinv, float *bvec) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nblk = (N + 31) / 32;
     for (int b = 0; b < nblk; b++) {
@@ -690,7 +645,7 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
         const int nb = min(32, N - r0);
         const int r = r0 + nb + tid;
         float seg[32];
-        if (r < N) load_seg32(M, ld, r, r0, seg);
+        if (r < N) load_seg32(M, ld, perm[r], r0, seg);
         if (warp == 0) {
             float li[32];
             const float4 *lp = reinterpret_cast<const float4 *>(dinv + (int64_t)b * 2048 + lane * 32);
@@ -715,7 +670,7 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
         }
         for (int r2 = r + kThreads; r2 < N; r2 += kThreads) {
             float s2[32];
-            load_seg32(M, ld, r2, r0, s2);
+            load_seg32(M, ld, perm[r2], r0, s2);
             float acc = bvec[r2];
 #pragma unroll
             for (int k = 0; k < 32; k++)
@@ -729,7 +684,7 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
         const int nb = min(32, N - r0);
         const int r = tid;
         float seg[32];
-        if (r < r0) load_seg32(M, ld, r, r0, seg);
+        if (r < r0) load_seg32(M, ld, perm[r], r0, seg);
         if (warp == 0) {
             float ui[32];
             const float4 *up =
@@ -755,7 +710,7 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
         }
         for (int r2 = r + kThreads; r2 < r0; r2 += kThreads) {
             float s2[32];
-            load_seg32(M, ld, r2, r0, s2);
+            load_seg32(M, ld, perm[r2], r0, s2);
             float acc = bvec[r2];
 #pragma unroll
             for (int k = 0; k < 32; k++)
@@ -771,8 +726,8 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
 // mu[perm[i]] = w[i] (done by the caller).  Diagonal blocks are applied as
 // the transposes of the inverted blocks; the off-diagonal updates read rows
 // of U (resp. L) of the current block, one column per thread.
-__device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, const float *dinv,
-                                             float *bvec) {
+__device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, const int *perm,
+                                             const float *dinv, float *bvec) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nblk = (N + 31) / 32;
     for (int b = 0; b < nblk; b++) {
@@ -782,7 +737,7 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
         float seg[32];
         if (i < N) {
 #pragma unroll
-            for (int k = 0; k < 32; k++) seg[k] = (k < nb) ? M[(int64_t)(r0 + k) * ld + i] : 0.f;
+            for (int k = 0; k < 32; k++) seg[k] = (k < nb) ? M[(int64_t)perm[r0 + k] * ld + i] : 0.f;
         }
         if (warp == 0) {
             const float *Ui = dinv + (int64_t)b * 2048 + 1024;
@@ -803,7 +758,7 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
         }
         for (int i2 = i + kThreads; i2 < N; i2 += kThreads) {
             float acc = bvec[i2];
-            for (int k = 0; k < nb; k++) acc = __fmaf_rn(-M[(int64_t)(r0 + k) * ld + i2], bvec[r0 + k], acc);
+            for (int k = 0; k < nb; k++) acc = __fmaf_rn(-M[(int64_t)perm[r0 + k] * ld + i2], bvec[r0 + k], acc);
             bvec[i2] = acc;
         }
         __syncthreads();
@@ -815,7 +770,7 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
         float seg[32];
         if (i < r0) {
 #pragma unroll
-            for (int k = 0; k < 32; k++) seg[k] = (k < nb) ? M[(int64_t)(r0 + k) * ld + i] : 0.f;
+            for (int k = 0; k < 32; k++) seg[k] = (k < nb) ? M[(int64_t)perm[r0 + k] * ld + i] : 0.f;
         }
         if (warp == 0) {
             const float *Li = dinv + (int64_t)b * 2048;
@@ -836,7 +791,7 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
         }
         for (int i2 = i + kThreads; i2 < r0; i2 += kThreads) {
             float acc = bvec[i2];
-            for (int k = 0; k < nb; k++) acc = __fmaf_rn(-M[(int64_t)(r0 + k) * ld + i2], bvec[r0 + k], acc);
+            for (int k = 0; k < nb; k++) acc = __fmaf_rn(-M[(int64_t)perm[r0 + k] * ld + i2], bvec[r0 + k], acc);
             bvec[i2] = acc;
         }
         __syncthreads();
@@ -1135,11 +1090,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 const long long c1 = clock64();
                 if (tid == 0) st.cycles_matrix += c1 - c_mark;
                 if (tid == 0) st.lu_factorisations++;
-                if (lu_factor<LT>(M, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv,
+                if (lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
                                   reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0)
                     luFail = true;
                 if constexpr (kMixed) {
-                    if (!luFail) invert_diag_blocks(M, ld, N, dinv);
+                    if (!luFail) invert_diag_blocks(M, ld, N, perm, dinv);
                     __syncthreads();
                 }
                 if (tid == 0) st.cycles_lu += clock64() - c1;
@@ -1157,7 +1112,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if constexpr (!kMixed) {
                 for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)xr[perm[s]];
                 __syncthreads();
-                lu_solve<LT>(M, ld, N, bvec);
+                lu_solve<LT>(M, ld, N, perm, bvec);
                 for (int s = tid; s < N; s += kThreads) dx[s] = (double)bvec[s];
                 __syncthreads();
             } else {
@@ -1176,13 +1131,16 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 double rmax = block_max(rloc, red);
                 double prev = INFINITY;
                 for (int sweep = 0; sweep < refine_max; sweep++) {
-                    if (!(rmax > 0.0) || isinf(rmax)) break;  // nothing to solve / not finite
-                    const int e = ilogb(rmax);
+                    if (rmax == 0.0) break;  // exact
+                    // a non-finite residual is solved unscaled, so that inf/NaN
+                    // reach the update as in the FP64 solve
+                    const bool finite = isfinite(rmax);
+                    const int e = finite ? ilogb(rmax) : 0;
                     const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
                     for (int s = tid; s < N; s += kThreads)
                         bvec[s] = (LT)(res[perm[s]] * sc);
                     __syncthreads();
-                    lu_solve_fast(M, ld, N, dinv, bvec);
+                    lu_solve_fast(M, ld, N, perm, dinv, bvec);
                     double cmax = 0.0, xmax = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
                         double c = (double)bvec[s] * isc;
@@ -1204,8 +1162,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     // the contraction so far, is below FP64 resolution of dx
                     const bool small_next =
                         sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
-                    if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) || small_next ||
-                        sweep + 1 == refine_max)
+                    if (!finite || !(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) ||
+                        small_next || sweep + 1 == refine_max)
                         break;
                     prev = cmax;
                     // res = xr - (dx - h*J(xf)*dx)
@@ -1394,7 +1352,7 @@ struct AdjSmem {
         perm = o;   o = al(o + int64_t(nmax) * 4);
         slot = o;   o = al(o + int64_t(nmax) * 4);
         bvec = o;   o = al(o + int64_t(nmax) * 4);
-        lt = o;     o = al(o + (int64_t(PB) * ((nmax + 3) & ~3) + 160) * 4);
+        lt = o;     o = al(o + (int64_t(PB) * (((nmax + 31) & ~31) + 4) + 160) * 4);
         utile = o;  o = al(o + int64_t(PB) * 128 * 4);
         rowbuf = o; o = al(o + int64_t(2 * PB) * 4);
         total = o;
@@ -1561,10 +1519,10 @@ __device__ void adjoint_instance(const LaunchParams &P, int id, unsigned char *s
                 double *mu = Y[0], *res = Y[1], *mdiag = Y[2], *vm = Y[3];
                 assemble_newton_matrix<float>(m, yout, h, M, ld, true, fd);
                 for (int s = tid; s < N; s += kThreads) mdiag[s] = (double)M[(int64_t)s * ld + s];
-                const int fail = lu_factor<float>(M, ld, N, perm, slot, lt, utile, rowbuf, red,
-                                                  ired, mv, reinterpret_cast<long long *>(cyc_dummy));
+                const int fail = lu_factor<float>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
+                                                  reinterpret_cast<long long *>(cyc_dummy));
                 if (fail == 0) {
-                    invert_diag_blocks(M, ld, N, dinv);
+                    invert_diag_blocks(M, ld, N, perm, dinv);
                     __syncthreads();
                     double rloc = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
@@ -1575,12 +1533,13 @@ __device__ void adjoint_instance(const LaunchParams &P, int id, unsigned char *s
                     double rmax = block_max(rloc, red);
                     double prev = INFINITY;
                     for (int sweep = 0; sweep < 12; sweep++) {
-                        if (!(rmax > 0.0) || isinf(rmax)) break;
-                        const int e = ilogb(rmax);
+                        if (rmax == 0.0) break;
+                        const bool finite = isfinite(rmax);
+                        const int e = finite ? ilogb(rmax) : 0;
                         const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
                         for (int s = tid; s < N; s += kThreads) bvec[s] = (float)(res[s] * sc);
                         __syncthreads();
-                        lu_solve_fast_T(M, ld, N, dinv, bvec);
+                        lu_solve_fast_T(M, ld, N, perm, dinv, bvec);
                         double cmax = 0.0, xmax = 0.0;
                         for (int i2 = tid; i2 < N; i2 += kThreads) {
                             const int s = perm[i2];
@@ -1596,7 +1555,8 @@ __device__ void adjoint_instance(const LaunchParams &P, int id, unsigned char *s
                         cmax = block_max(cmax, red);
                         xmax = block_max(xmax, red);
                         const bool small_next = sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
-                        if (!(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) || small_next) break;
+                        if (!finite || !(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) || small_next)
+                            break;
                         prev = cmax;
                         // res = lambda - (mu - h J^T (D mu))
                         for (int s = tid; s < N; s += kThreads) vm[s] = (fd[s] != 0.0) ? 0.0 : mu[s];
@@ -1799,18 +1759,18 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
     LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
     __shared__ long long cyc[3];
     if (threadIdx.x == 0) cyc[0] = cyc[1] = cyc[2] = 0;
-    const int fail = lu_factor<LT>(A, ld, N, perm, slot, lt, utile, rowbuf, red, ired, mv, cyc);
+    const int fail = lu_factor<LT>(A, ld, N, perm, lt, utile, rowbuf, red, ired, cyc);
     if (threadIdx.x == 0) *info = fail;
     if (fail) return;
     for (int s = threadIdx.x; s < N; s += kThreads) bvec[s] = (LT)b[perm[s]];
     __syncthreads();
     if constexpr (std::is_same<LT, float>::value) {
         float *dinv = A + (int64_t)N * ld;
-        invert_diag_blocks(A, ld, N, dinv);
+        invert_diag_blocks(A, ld, N, perm, dinv);
         __syncthreads();
-        lu_solve_fast(A, ld, N, dinv, bvec);
+        lu_solve_fast(A, ld, N, perm, dinv, bvec);
     } else {
-        lu_solve<LT>(A, ld, N, bvec);
+        lu_solve<LT>(A, ld, N, perm, bvec);
     }
     for (int s = threadIdx.x; s < N; s += kThreads) x[s] = (double)bvec[s];
 }

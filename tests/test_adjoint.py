@@ -84,5 +84,8 @@ def test_torch_autograd(gpu):
                         requires_grad=True)
     L = trajectory_misfit(logk, models, targets)
     (L[0] + 2.0 * L[1]).backward()
+    # the same rate constants the autograd path used: exp(log k)
+    for b, m in enumerate(models):
+        m.k = np.exp(logk.detach().numpy()[b])
     _, gk, _, _, _ = adjoint_batch(models, targets)
     assert np.allclose(logk.grad.numpy(), np.stack([gk[0], 2.0 * gk[1]]), rtol=1e-12, atol=0)
