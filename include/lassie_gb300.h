@@ -190,6 +190,29 @@ int lassie_adjoint_batch(const lassie_instance *inst, int32_t n, const double *c
                          double *loss, double *const *grad_logk, double *const *grad_x0,
                          lassie_stats *stats);
 
+/* One integration that allocates no device memory (no counterpart in the
+   reference, which allocates in every solve).  For callers that cannot call
+   cudaMalloc -- code running under another framework's memory pool or
+   inside a stream capture, plugins that may not allocate after start-up,
+   real-time loops that must not wait on the allocator.  All working memory
+   (network structure, descriptor, Newton matrix, result) lives in one
+   static device arena of LASSIE_NOALLOC_ARENA_BYTES that every device which
+   loads the library keeps until the process exits.  d_k[R], d_x0[N], d_t[nt]
+   and d_out[nt*N] (all species sampled) are device buffers owned by the
+   caller; stats is host memory (may be NULL).  Networks above the limits
+   below are rejected with LASSIE_ERR_TOO_LARGE.  The first call on a device
+   looks up the arena's device address: make it before any stream capture.
+   Calls share the arena and keep its last contents (the queue counter and
+   the result are cleared per call); calls that overlap on the GPU race, so
+   serialise them.  Returns the instance status; synchronises `stream`. */
+#define LASSIE_NOALLOC_MAX_SPECIES 128
+#define LASSIE_NOALLOC_MAX_REACTIONS 256
+#define LASSIE_NOALLOC_MAX_SAMPLES 4096
+#define LASSIE_NOALLOC_ARENA_BYTES (512 * 1024)
+int lassie_solve_noalloc(const lassie_model *model, const double *d_k, const double *d_x0,
+                         const double *d_t, int32_t nt, const lassie_opts *opts, double *d_out,
+                         lassie_stats *stats, void *stream);
+
 /* ---------------------------------------------------- single evaluations */
 /* dx = f(x) for n_inst parameterisations of one network, device buffers,
    instance-major: k [n_inst][R], x and dx [n_inst][N].  Replaces

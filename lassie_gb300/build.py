@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I" + INCLUDE, "-I" + CSRC] + ARCH
 
-SOURCES = ["compat_engine.cu", "capi.cu"]
+SOURCES = ["compat_engine.cu", "capi.cu", "noalloc.cu"]
 
 
 def _nvcc() -> str:

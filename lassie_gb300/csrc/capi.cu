@@ -228,6 +228,30 @@ static int model_device(lassie_model *m, const int32_t **d) {
     return LASSIE_OK;
 }
 
+namespace lassie {
+// Host-side packing of a model for lassie_solve_noalloc (no device memory).
+int model_pack_for_noalloc(const lassie_model *m, std::vector<int32_t> &out, int32_t *n,
+                           int32_t *r, int32_t *nnz_a, int32_t *nnz_h, int64_t offs[8]) {
+    if (!m) return set_error(LASSIE_ERR_ARGS, "null model");
+    out.clear();
+    m->pack(out);
+    *n = m->N;
+    *r = m->R;
+    *nnz_a = (int32_t)m->rxn_ent.size();
+    *nnz_h = (int32_t)m->sp_ent.size();
+    offs[0] = 0;
+    offs[1] = m->off_rent();
+    offs[2] = m->off_sptr();
+    offs[3] = m->off_sent();
+    offs[4] = m->off_hrptr();
+    offs[5] = m->off_hrent();
+    offs[6] = m->off_asptr();
+    offs[7] = m->off_asent();
+    return LASSIE_OK;
+}
+int set_error_noalloc(int status, const char *msg) { return set_error(status, msg); }
+}  // namespace lassie
+
 // ------------------------------------------------------------- utilities
 
 extern "C" void lassie_opts_default(lassie_opts *o) {
