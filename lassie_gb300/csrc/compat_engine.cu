@@ -64,34 +64,42 @@ __device__ double block_sum(double v, double *red) {
     return s;
 }
 
-// Block max of non-negative doubles (NaN propagates).
+// Block max of non-negative doubles (NaN propagates), on their IEEE bit
+// patterns: for non-negative values the patterns order like the values and
+// every NaN pattern sorts above +inf, so no FP64 instruction is needed.
 __device__ double block_max(double v, double *red) {
+    long long b = __double_as_longlong(fabs(v));
     for (int o = 16; o > 0; o >>= 1) {
-        double u = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (isnan(u) || u > v) ? u : v;
+        const long long u = __shfl_xor_sync(0xffffffffu, b, o);
+        b = u > b ? u : b;
     }
+    long long *ired = reinterpret_cast<long long *>(red);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
-    if (l == 0) red[w] = v;
+    if (l == 0) ired[w] = b;
     __syncthreads();
-    double s = red[0];
-    for (int q = 1; q < kWarps; q++) s = (isnan(red[q]) || red[q] > s) ? red[q] : s;
-    return s;
+    long long s = ired[0];
+    for (int q = 1; q < kWarps; q++) s = ired[q] > s ? ired[q] : s;
+    return __longlong_as_double(s);
 }
 
-// Block minimum of non-NaN values (+inf if none).
+// Block minimum of the non-NaN values among non-negative doubles (+inf if
+// none), on bit patterns as above (NaN counts as +inf).
 __device__ double block_min_nonnan(double v, double *red) {
+    const long long kInf = 0x7ff0000000000000LL;
+    long long b = isnan(v) ? kInf : __double_as_longlong(fabs(v));
     for (int o = 16; o > 0; o >>= 1) {
-        double u = __shfl_xor_sync(0xffffffffu, v, o);
-        v = (u < v) ? u : v;
+        const long long u = __shfl_xor_sync(0xffffffffu, b, o);
+        b = u < b ? u : b;
     }
+    long long *ired = reinterpret_cast<long long *>(red);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     __syncthreads();
-    if (l == 0) red[w] = v;
+    if (l == 0) ired[w] = b;
     __syncthreads();
-    double s = red[0];
-    for (int q = 1; q < kWarps; q++) s = (red[q] < s) ? red[q] : s;
-    return s;
+    long long s = ired[0];
+    for (int q = 1; q < kWarps; q++) s = ired[q] < s ? ired[q] : s;
+    return __longlong_as_double(s);
 }
 
 // --------------------------------------------------------------- model
@@ -277,12 +285,16 @@ __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *
 
 // ------------------------------------------------------------------ LU
 
-// Arg-max of |v| with the oracle's tie and NaN rules, combined over lanes.
-struct Piv {
-    double v;
+// Arg-max of |v| with the oracle's tie and NaN rules, combined over lanes,
+// in the factor's own type (FP64 instructions are slow on this GPU, so the
+// FP32 factorisation never touches the FP64 pipe here).
+template <typename T>
+struct PivT {
+    T v;
     int i;
 };
-__device__ __forceinline__ Piv piv_better(Piv a, Piv b) {
+template <typename T>
+__device__ __forceinline__ PivT<T> piv_better(PivT<T> a, PivT<T> b) {
     // larger |value| wins, ties to the smaller index; NaN values never win
     if (b.v > a.v || (b.v == a.v && b.i < a.i)) return b;
     return a;
@@ -349,27 +361,29 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
             lt[c * mp + r] = (c < pb) ? M[(int64_t)perm[j0 + r] * ld + j0 + c] : LT(0);
         }
         __syncthreads();
-        Piv best{-1.0, 1 << 30};
+        PivT<LT> best{LT(-1), 1 << 30};
         if (tid < m) {
-            const double v = fabs((double)lt[tid]);
-            if (!isnan(v)) best = Piv{v, tid};
+            const LT v = fabs(lt[tid]);
+            if (!isnan(v)) best = PivT<LT>{v, tid};
         }
         for (int jj = 0; jj < pb; jj++) {
             for (int o = 16; o > 0; o >>= 1) {
-                Piv other{__shfl_xor_sync(0xffffffffu, best.v, o),
-                          __shfl_xor_sync(0xffffffffu, best.i, o)};
+                PivT<LT> other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                               __shfl_xor_sync(0xffffffffu, best.i, o)};
                 best = piv_better(best, other);
             }
+            LT *redv = reinterpret_cast<LT *>(red);
             if (lane == 0) {
-                red[warp] = best.v;
+                redv[warp] = best.v;
                 ired[warp] = best.i;
             }
             __syncthreads();
-            Piv all{red[0], ired[0]};
-            for (int q = 1; q < kWarps; q++) all = piv_better(all, Piv{red[q], ired[q]});
+            PivT<LT> all{redv[0], ired[0]};
+            for (int q = 1; q < kWarps; q++)
+                all = piv_better(all, PivT<LT>{redv[q], ired[q]});
             int p = all.i;
             // a NaN in the diagonal position keeps its own row (oracle rule)
-            if (isnan((double)lt[jj * mp + jj]) || p >= m) p = jj;
+            if (isnan(lt[jj * mp + jj]) || p >= m) p = jj;
             if (tid < PB) {
                 pivrow[tid] = lt[tid * mp + p];
                 swaprow[tid] = lt[tid * mp + jj];
@@ -385,7 +399,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
                 fail = j0 + jj + 1;
                 break;
             }
-            best = Piv{-1.0, 1 << 30};
+            best = PivT<LT>{LT(-1), 1 << 30};
             if (tid > jj && tid < m && tid != p) {
                 // own row, untouched by the interchange
                 const LT l = lt[jj * mp + tid] / d;
@@ -393,8 +407,8 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
                 for (int c = jj + 1; c < pb; c++)
                     lt[c * mp + tid] = lt_fma(-l, pivrow[c], lt[c * mp + tid]);
                 if (jj + 1 < pb) {
-                    const double v = fabs((double)lt[(jj + 1) * mp + tid]);
-                    if (!isnan(v)) best = Piv{v, tid};
+                    const LT v = fabs(lt[(jj + 1) * mp + tid]);
+                    if (!isnan(v)) best = PivT<LT>{v, tid};
                 }
             } else if (tid == jj && p != jj) {
                 // the pivot row moves to position jj; the displaced row jj goes
@@ -406,8 +420,8 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
                 for (int c = jj + 1; c < pb; c++)
                     lt[c * mp + p] = lt_fma(-l, pivrow[c], swaprow[c]);
                 if (jj + 1 < pb) {
-                    const double v = fabs((double)lt[(jj + 1) * mp + p]);
-                    if (!isnan(v)) best = Piv{v, p};
+                    const LT v = fabs(lt[(jj + 1) * mp + p]);
+                    if (!isnan(v)) best = PivT<LT>{v, p};
                 }
             }
         }
@@ -633,92 +647,83 @@ __device__ __forceinline__ void load_seg32(const float *M, int ld, int r, int c0
     }
 }
 
-// FP32 form solve: 32-row block steps; the diagonal blocks are applied as
-// their inverses (one 32 x 32 matvec by warp 0), the off-diagonal rows update
-// with row segments loaded before the block step's barrier.
+// FP32 form solve, N <= kThreads: thread t owns row t and keeps its running
+// value in a register; warp w owns diagonal block w, whose inverse (from
+// invert_diag_blocks) it holds in registers from the start.  Forward: at
+// step b warp b applies L_bb^-1 and publishes the block's solution through
+// a double-buffered shared array (xs, 64 floats); the rows below update with
+// the segment of their row in block b, loaded one step ahead.  Backward:
+// the same with U.  One barrier per block step.  bvec holds P*b on entry
+// and x on exit.
 __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const int *perm,
-                                           const float *dinv, float *bvec) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+                                           const float *dinv, float *bvec, float *xs) {
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     const int nblk = (N + 31) / 32;
+    const bool mine = tid < N;
+    const int prow = mine ? perm[tid] : 0;
+    const float *Mr = M + (int64_t)prow * ld;
+    float acc = mine ? bvec[tid] : 0.f;
+    float inv[32], seg[32];
+    // forward: unit lower
+    if (w < nblk) {
+        const float4 *ip = reinterpret_cast<const float4 *>(dinv + (int64_t)w * 2048 + lane * 32);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const float4 v = ip[q];
+            inv[4 * q] = v.x; inv[4 * q + 1] = v.y; inv[4 * q + 2] = v.z; inv[4 * q + 3] = v.w;
+        }
+    }
+    if (mine && w > 0) load_seg32(M, ld, prow, 0, seg);
     for (int b = 0; b < nblk; b++) {
-        const int r0 = b * 32;
-        const int nb = min(32, N - r0);
-        const int r = r0 + nb + tid;
-        float seg[32];
-        if (r < N) load_seg32(M, ld, perm[r], r0, seg);
-        if (warp == 0) {
-            float li[32];
-            const float4 *lp = reinterpret_cast<const float4 *>(dinv + (int64_t)b * 2048 + lane * 32);
+        float *xb = xs + (b & 1) * 32;
+        if (w == b) {
+            float x = 0.f;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                float4 v = lp[q];
-                li[4 * q] = v.x; li[4 * q + 1] = v.y; li[4 * q + 2] = v.z; li[4 * q + 3] = v.w;
-            }
-            const float bi = (lane < nb) ? bvec[r0 + lane] : 0.f;
-            float acc = 0.f;
-#pragma unroll
-            for (int k = 0; k < 32; k++) acc = __fmaf_rn(li[k], __shfl_sync(0xffffffffu, bi, k), acc);
-            if (lane < nb) bvec[r0 + lane] = acc;
+            for (int k = 0; k < 32; k++) x = __fmaf_rn(inv[k], __shfl_sync(0xffffffffu, acc, k), x);
+            acc = x;
+            xb[lane] = x;
         }
         __syncthreads();
-        if (r < N) {
-            float acc = bvec[r];
+        if (mine && w > b) {
+            const int nb = min(32, N - b * 32);
 #pragma unroll
             for (int k = 0; k < 32; k++)
-                if (k < nb) acc = __fmaf_rn(-seg[k], bvec[r0 + k], acc);
-            bvec[r] = acc;
+                if (k < nb) acc = __fmaf_rn(-seg[k], xb[k], acc);
+            if (b + 1 < w) load_seg32(M, ld, prow, (b + 1) * 32, seg);
         }
-        for (int r2 = r + kThreads; r2 < N; r2 += kThreads) {
-            float s2[32];
-            load_seg32(M, ld, perm[r2], r0, s2);
-            float acc = bvec[r2];
-#pragma unroll
-            for (int k = 0; k < 32; k++)
-                if (k < nb) acc = __fmaf_rn(-s2[k], bvec[r0 + k], acc);
-            bvec[r2] = acc;
-        }
-        __syncthreads();
     }
+    __syncthreads();
+    // backward: upper
+    if (w < nblk) {
+        const float4 *ip =
+            reinterpret_cast<const float4 *>(dinv + (int64_t)w * 2048 + 1024 + lane * 32);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            const float4 v = ip[q];
+            inv[4 * q] = v.x; inv[4 * q + 1] = v.y; inv[4 * q + 2] = v.z; inv[4 * q + 3] = v.w;
+        }
+    }
+    if (mine && w < nblk - 1) load_seg32(M, ld, prow, (nblk - 1) * 32, seg);
     for (int b = nblk - 1; b >= 0; b--) {
-        const int r0 = b * 32;
-        const int nb = min(32, N - r0);
-        const int r = tid;
-        float seg[32];
-        if (r < r0) load_seg32(M, ld, perm[r], r0, seg);
-        if (warp == 0) {
-            float ui[32];
-            const float4 *up =
-                reinterpret_cast<const float4 *>(dinv + (int64_t)b * 2048 + 1024 + lane * 32);
+        float *xb = xs + (b & 1) * 32;
+        if (w == b) {
+            float x = 0.f;
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                float4 v = up[q];
-                ui[4 * q] = v.x; ui[4 * q + 1] = v.y; ui[4 * q + 2] = v.z; ui[4 * q + 3] = v.w;
-            }
-            const float bi = (lane < nb) ? bvec[r0 + lane] : 0.f;
-            float acc = 0.f;
-#pragma unroll
-            for (int k = 0; k < 32; k++) acc = __fmaf_rn(ui[k], __shfl_sync(0xffffffffu, bi, k), acc);
-            if (lane < nb) bvec[r0 + lane] = acc;
+            for (int k = 0; k < 32; k++) x = __fmaf_rn(inv[k], __shfl_sync(0xffffffffu, acc, k), x);
+            acc = x;
+            xb[lane] = x;
         }
         __syncthreads();
-        if (r < r0) {
-            float acc = bvec[r];
+        if (mine && w < b) {
+            const int nb = min(32, N - b * 32);
 #pragma unroll
             for (int k = 0; k < 32; k++)
-                if (k < nb) acc = __fmaf_rn(-seg[k], bvec[r0 + k], acc);
-            bvec[r] = acc;
+                if (k < nb) acc = __fmaf_rn(-seg[k], xb[k], acc);
+            if (b - 1 > w) load_seg32(M, ld, prow, (b - 1) * 32, seg);
         }
-        for (int r2 = r + kThreads; r2 < r0; r2 += kThreads) {
-            float s2[32];
-            load_seg32(M, ld, perm[r2], r0, s2);
-            float acc = bvec[r2];
-#pragma unroll
-            for (int k = 0; k < 32; k++)
-                if (k < nb) acc = __fmaf_rn(-s2[k], bvec[r0 + k], acc);
-            bvec[r2] = acc;
-        }
-        __syncthreads();
     }
+    if (mine) bvec[tid] = acc;
+    __syncthreads();
 }
 
 // Transposed solve with the same factors (adjoint): P A = L U, so
@@ -1140,7 +1145,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     for (int s = tid; s < N; s += kThreads)
                         bvec[s] = (LT)(res[perm[s]] * sc);
                     __syncthreads();
-                    lu_solve_fast(M, ld, N, perm, dinv, bvec);
+                    lu_solve_fast(M, ld, N, perm, dinv, bvec, reinterpret_cast<float *>(rowbuf));
                     double cmax = 0.0, xmax = 0.0;
                     for (int s = tid; s < N; s += kThreads) {
                         double c = (double)bvec[s] * isc;
@@ -1768,7 +1773,7 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
         float *dinv = A + (int64_t)N * ld;
         invert_diag_blocks(A, ld, N, perm, dinv);
         __syncthreads();
-        lu_solve_fast(A, ld, N, perm, dinv, bvec);
+        lu_solve_fast(A, ld, N, perm, dinv, bvec, reinterpret_cast<float *>(rowbuf));
     } else {
         lu_solve<LT>(A, ld, N, perm, bvec);
     }
