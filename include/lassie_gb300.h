@@ -174,8 +174,9 @@ int lassie_batch_launches(const lassie_batch *batch);
 int lassie_batch_bytes(const lassie_batch *batch, int64_t *h2d, int64_t *d2h);
 void lassie_batch_destroy(lassie_batch *batch);
 
-/* Discrete adjoint (no reference counterpart).  Integrates the instances with
-   the mixed form, recording the step sequence, then runs the backward pass
+/* Discrete adjoint (no reference counterpart).  Integrates the instances in
+   the form opts->precision names (mixed or FP64), recording the step
+   sequence, then runs the backward pass
    of that exact step sequence for
        L_q = sum over samples i and sampled species j of (y_ij - target_ij)^2
    and returns loss[q], grad_logk[q][R] = dL_q/dlog k and (when grad_x0 is

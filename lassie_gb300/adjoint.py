@@ -26,8 +26,12 @@ from .solver import NativeModel, _Packed, make_opts
 
 def adjoint_batch(models: Sequence[Model], targets: Sequence[np.ndarray],
                   ckpt_every: int = 8, max_record: int = 0, deadline_s: float = 0.0,
-                  root: str = "pow", native: Optional[Sequence[NativeModel]] = None):
-    """Returns (loss [B], grad_logk [B][R], grad_x0 [B][N], trajectories, stats)."""
+                  root: str = "pow", native: Optional[Sequence[NativeModel]] = None,
+                  engine: str = "mixed"):
+    """Returns (loss [B], grad_logk [B][R], grad_x0 [B][N], trajectories, stats).
+
+    ``engine`` is the form of the recorded forward integration ("mixed" or
+    "fp64"); the backward pass is the same for both."""
     L = nat.load()
     n = len(models)
     cache = {}
@@ -50,7 +54,7 @@ def adjoint_batch(models: Sequence[Model], targets: Sequence[np.ndarray],
     loss = np.zeros(n)
     stats = (nat.Stats * max(n, 1))()
     arr = lambda lst: (C.c_void_p * max(n, 1))(*[a.ctypes.data for a in lst])  # noqa: E731
-    o = make_opts(models[0] if n else None, "mixed", 0, deadline_s, root=root)
+    o = make_opts(models[0] if n else None, engine, 0, deadline_s, root=root)
     rc = L.lassie_adjoint_batch(C.cast(inst, C.c_void_p), n, C.cast(arr(tg), C.c_void_p),
                                 C.byref(o), int(ckpt_every), int(max_record),
                                 loss.ctypes.data, C.cast(arr(gk), C.c_void_p),

@@ -482,8 +482,9 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     }
     b->grid = std::max(1, std::min(n, b->sm_count));
     const int lt = o.precision == LASSIE_PREC_FP64 ? 8 : 4;
-    const int64_t dinv_bytes =
-        o.precision == LASSIE_PREC_MIXED ? (int64_t)((b->nmax + 31) / 32) * 2048 * 4 : 0;
+    // FP32 inverses of the 32x32 diagonal blocks after the matrix: the mixed
+    // forward's solves and the adjoint's transposed solves (either form) use them
+    const int64_t dinv_bytes = (int64_t)((b->nmax + 31) / 32) * 2048 * 4;
     const int64_t ws_stride =
         ((int64_t)b->nmax * round_up4(b->nmax) * lt + dinv_bytes + 255) / 256 * 256;
     if ((rc = b->d_int.grow(b->n_int * 4)) || (rc = b->d_dbl.grow(b->n_dbl * 8)) ||
@@ -627,7 +628,6 @@ extern "C" int lassie_adjoint_batch(const lassie_instance *inst, int32_t n,
     lassie_opts o;
     if (opts) o = *opts;
     else lassie_opts_default(&o);
-    o.precision = LASSIE_PREC_MIXED;
     const int K = ckpt_every > 0 ? ckpt_every : 8;
     const int cap = max_record > 0 ? max_record : 100000;
     lassie_batch *b = nullptr;

@@ -236,6 +236,31 @@ typedef struct {
     int *samp;     /* steps taken before each sample */
 } lo_record;
 
+/* Decision-sensitivity probe (tests only): when g_perturb_rel > 0, every
+   Newton correction from the LU solve is multiplied componentwise by
+   (1 +- g_perturb_rel), signs from a seeded xorshift stream -- a stand-in for
+   a linear solver that differs from this one in the last bits (another LU
+   order, cuSOLVER, FP32 LU + refinement).  Process-global and not thread
+   safe: set it, solve on one thread, reset it to 0. */
+static double g_perturb_rel = 0.0;
+static uint64_t g_perturb_state = 0;
+
+void lo_set_solve_perturbation(double rel, uint64_t seed) {
+    g_perturb_rel = rel;
+    g_perturb_state = seed * 0x9E3779B97F4A7C15ull + 1;
+}
+
+static void lo_perturb(int n, double *dx) {
+    for (int s = 0; s < n; s++) {
+        uint64_t z = g_perturb_state;
+        z ^= z << 13;
+        z ^= z >> 7;
+        z ^= z << 17;
+        g_perturb_state = z;
+        dx[s] = dx[s] * ((z & 1) ? 1.0 + g_perturb_rel : 1.0 - g_perturb_rel);
+    }
+}
+
 static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
                          const double *feed, const double *atol, const double *tv,
                          int nt, const int *cs, int ncs, const lo_opts *opts_in,
@@ -449,6 +474,7 @@ static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
                     }
                     memcpy(dx, xr, sizeof(double) * N);
                     lo_lu_solve(N, M, piv, dx);
+                    if (g_perturb_rel > 0) lo_perturb(N, dx);
                     /* kernels.cuh:462-477 and Simulation.cuh:883-890 */
                     double sum = 0.0;
                     for (int s = 0; s < N; s++) {

@@ -71,6 +71,10 @@ typedef struct {
 #define LO_ERR_MAX_STEPS (-21)
 #define LO_ERR_ALLOC (-22)
 
+/* Tests only: multiply each Newton correction componentwise by (1 +- rel)
+   with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
+void lo_set_solve_perturbation(double rel, uint64_t seed);
+
 int lo_model_build(int n_reactions, int n_species, const int32_t *left,
                    const int32_t *right, lo_model *out);
 void lo_model_free(lo_model *m);

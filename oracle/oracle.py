@@ -69,6 +69,7 @@ def lib():
             L.lo_lu_factor.argtypes = [C.c_int, _f64p, _i32p]
             L.lo_lu_factor.restype = C.c_int
             L.lo_lu_solve.argtypes = [C.c_int, _f64p, _i32p, _f64p]
+            L.lo_set_solve_perturbation.argtypes = [C.c_double, C.c_uint64]
             L.lo_solve_compat.argtypes = [C.POINTER(_Model), _f64p, _f64p, C.c_void_p,
                                           C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Opts), _f64p, C.POINTER(Stats)]
@@ -213,3 +214,20 @@ def lu_solve(lu: np.ndarray, piv: np.ndarray, b: np.ndarray) -> np.ndarray:
     b = np.ascontiguousarray(b, np.float64).copy()
     lib().lo_lu_solve(lu.shape[0], np.ascontiguousarray(lu), piv, b)
     return b
+
+
+class solve_perturbation:
+    """Context manager: inside it, every oracle Newton correction is scaled
+    componentwise by (1 +- rel) with seeded signs -- a linear solver that
+    differs from the oracle's in the last bits.  Single-threaded use only."""
+
+    def __init__(self, rel: float, seed: int = 1):
+        self.rel, self.seed = float(rel), int(seed)
+
+    def __enter__(self):
+        lib().lo_set_solve_perturbation(self.rel, self.seed)
+        return self
+
+    def __exit__(self, *exc):
+        lib().lo_set_solve_perturbation(0.0, 0)
+        return False

@@ -30,10 +30,11 @@ def problem(copy=0, t_end=1.0, n=9):
 def test_adjoint_matches_forward_sensitivities(gpu):
     m, target = problem()
     out_o, st_o, rc, kinds, dts, samp = O.solve_recorded(m)
-    loss, gk, gx, outs, stats = adjoint_batch([m], [target], root="sqrt", deadline_s=120)
+    loss, gk, gx, outs, stats = adjoint_batch([m], [target], root="sqrt", deadline_s=120,
+                                              engine="fp64")
     g = gk[0]
     assert stats[0]["status"] == 0
-    # the GPU forward took the oracle's step sequence
+    # the FP64 GPU forward took the oracle's step sequence
     assert stats[0]["be_steps"] == int(np.sum(kinds >= 1))
     assert stats[0]["rkf_accepts"] == int(np.sum(kinds == 0))
     assert loss[0] == pytest.approx(float(np.sum((out_o - target) ** 2)), rel=1e-9)
@@ -49,11 +50,24 @@ def test_adjoint_matches_forward_sensitivities(gpu):
 def test_adjoint_matches_central_differences(gpu):
     m, target = problem()
     _, _, _, kinds, dts, samp = O.solve_recorded(m)
-    _, gk, _, _, _ = adjoint_batch([m], [target], root="sqrt", deadline_s=120)
+    _, gk, _, _, _ = adjoint_batch([m], [target], root="sqrt", deadline_s=120, engine="fp64")
     g = gk[0]
     idx = list(np.argsort(-np.abs(g))[:3])  # the three most sensitive constants
     fd = S.fd_gradient(m, np.log(m.k), target, kinds, dts, samp, idx, h=1e-6)
     assert np.allclose(g[idx], fd, rtol=1e-4, atol=1e-6 * np.abs(g).max())
+
+
+def test_mixed_forward_gives_the_fp64_gradient(gpu):
+    """The mixed forward (FP32 LU + FP64 refinement) records the same step
+    sequence on this case (t in [0, 0.8]: backward-Euler steps only, and
+    insensitive to last-bit differences of the linear solve); its gradient
+    then agrees with the FP64 forward's."""
+    m, target = problem(t_end=0.8, n=9)
+    l64, g64, _, _, s64 = adjoint_batch([m], [target], root="sqrt", engine="fp64")
+    lmx, gmx, _, _, smx = adjoint_batch([m], [target], root="sqrt", engine="mixed")
+    assert (smx[0]["be_steps"], smx[0]["rkf_accepts"]) == (s64[0]["be_steps"], s64[0]["rkf_accepts"])
+    assert lmx[0] == pytest.approx(l64[0], rel=1e-6)
+    assert np.abs(gmx[0] - g64[0]).max() <= 1e-6 * np.abs(g64[0]).sum()
 
 
 def test_checkpoint_interval_does_not_change_the_gradient(gpu):

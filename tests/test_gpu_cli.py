@@ -26,7 +26,9 @@ def read_table(path):
 @pytest.mark.parametrize("engine", ["fp64", "mixed"])
 def test_cli_outputs(gpu, tmp_path, engine):
     build.build()
-    m = synth.shorten(synth.make_c4_instance(2), 1.0, 11)
+    # instance 35: backward-Euler steps and one RKF45 step, and its trajectory
+    # is insensitive to last-bit differences of the linear solve
+    m = synth.shorten(synth.make_c4_instance(35), 1.0, 11)
     m.cs = np.array([0, 3, 17, 40], np.int32)
     inp, out = tmp_path / "in", tmp_path / "out"
     write_folder(m, str(inp))

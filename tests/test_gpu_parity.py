@@ -20,9 +20,22 @@ def within(a, b, rtol=RTOL, atol=ATOL):
     return bool(np.all(np.abs(a - b) <= atol + rtol * np.abs(b)))
 
 
+def excess(a, b, rtol=RTOL, atol=ATOL):
+    """Per sample: the largest amount by which |a - b| exceeds the tolerance."""
+    return np.max(np.abs(a - b) - atol - rtol * np.abs(b), axis=1)
+
+
+# Cases whose trajectory moves beyond rtol 1e-6 when the oracle's own Newton
+# corrections are perturbed by one ulp: LASSIE's step-size controller turns
+# last-bit differences into different step sequences (the reference binary
+# differs from the oracle on them for the same reason).
+DECISION_SENSITIVE = ("c4-2-short",)
+
+
 def small_cases():
     yield "c1", synth.make_c1()
     yield "c4-2-short", synth.shorten(synth.make_c4_instance(2), 1.0, 11)
+    yield "c4-33-short", synth.shorten(synth.make_c4_instance(33), 1.0, 11)
     yield "c4-5-short", synth.shorten(synth.make_c4_instance(5), 0.3, 4)
     yield "c2-short", synth.shorten(synth.make_c2(), 0.012, 3)
     for kind in ("decay", "conversion", "dimer", "bimolecular", "source", "reversible"):
@@ -93,12 +106,38 @@ def test_solve_fp64_bit_exact(gpu, name, m):
     assert np.array_equal(out, ref), float(np.max(np.abs(out - ref)))
 
 
-@pytest.mark.parametrize("name,m", list(small_cases()), ids=[c[0] for c in small_cases()])
+@pytest.mark.parametrize("name,m", [c for c in small_cases() if c[0] not in DECISION_SENSITIVE],
+                         ids=[c[0] for c in small_cases() if c[0] not in DECISION_SENSITIVE])
 def test_solve_mixed_within_tolerance(gpu, name, m):
     ref, st_ref, rc = O.solve(m, max_steps=2_000_000)
     out, st = solver.simulate(m, engine="mixed", deadline_s=120, root="sqrt")
     assert st["status"] == 0
-    assert within(out, ref), float(np.max(np.abs(out - ref) - RTOL * np.abs(ref)))
+    assert within(out, ref), float(np.max(excess(out, ref)))
+
+
+@pytest.mark.parametrize("name,m", [c for c in small_cases() if c[0] in DECISION_SENSITIVE],
+                         ids=list(DECISION_SENSITIVE))
+def test_solve_mixed_decision_sensitive(gpu, name, m):
+    """On a decision-sensitive case the mixed form is held to the oracle's own
+    spread: five oracle runs whose Newton corrections are perturbed by one
+    ulp give the first sample that leaves the tolerance and the largest
+    excess; the mixed form must agree within tolerance before that sample
+    and stay within twice that excess."""
+    ref, _, rc = O.solve(m, max_steps=2_000_000)
+    assert rc == 0
+    firsts, worst = [], 0.0
+    for seed in range(1, 6):
+        with O.solve_perturbation(2.0 ** -52, seed):
+            p, _, _ = O.solve(m, max_steps=2_000_000)
+        e = excess(p, ref)
+        firsts.append(int(np.argmax(e > 0)) if np.any(e > 0) else len(e))
+        worst = max(worst, float(e.max()))
+    assert worst > 0, "the case is not decision-sensitive any more"
+    out, st = solver.simulate(m, engine="mixed", deadline_s=120, root="sqrt")
+    assert st["status"] == 0
+    e = excess(out, ref)
+    assert np.all(e[:min(firsts)] <= 0), (e, firsts)
+    assert e.max() <= 2 * worst, (float(e.max()), worst)
 
 
 def test_batch_equals_single(gpu):

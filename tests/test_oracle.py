@@ -165,3 +165,34 @@ def test_batch_equals_single():
     for m, o, s in zip(models, outs, status):
         ref, _, _ = O.solve(m)
         assert s == 0 and np.array_equal(o, ref)
+
+
+def _perturbed_excess(m, seeds=3):
+    ref, _, rc = O.solve(m)
+    assert rc == 0
+    worst = -1.0
+    for seed in range(1, seeds + 1):
+        with O.solve_perturbation(2.0 ** -52, seed):
+            p, _, rc = O.solve(m)
+        assert rc == 0
+        worst = max(worst, float(np.max(np.abs(p - ref) - 1e-9 - 1e-6 * np.abs(ref))))
+    return worst
+
+
+def test_decision_sensitivity_of_the_parity_cases():
+    """One-ulp changes of the Newton corrections move the trajectory of c4
+    instance 2 (t in [0,1]) beyond rtol 1e-6 / atol 1e-9 -- the RKF45 step
+    controller amplifies them -- while instances 33 and 35 stay within it.
+    The GPU parity tests hold the first kind to the oracle's own spread."""
+    assert _perturbed_excess(synth.shorten(synth.make_c4_instance(2), 1.0, 11)) > 1e-5
+    for q in (33, 35):
+        assert _perturbed_excess(synth.shorten(synth.make_c4_instance(q), 1.0, 11)) <= 0
+
+
+def test_perturbation_is_off_by_default():
+    m = synth.shorten(synth.make_c4_instance(2), 0.3, 4)
+    a, _, _ = O.solve(m)
+    with O.solve_perturbation(2.0 ** -52, 1):
+        pass
+    b, _, _ = O.solve(m)
+    assert np.array_equal(a, b)
