@@ -9,6 +9,15 @@ FP64 refinement) in one persistent launch.  A step integrates the whole
 batch; ``value`` is instances per second with inputs resident in HBM,
 ``e2e`` the same through the public host-buffer API (``lassie_solve_batch``).
 
+Under the reference's step control a few instances never finish in practice:
+every NaN/negative revert divides the backward-Euler step by 10 for good, so
+22 of the 2048 end at dt = 1e-4 (2e5 steps), one at 1e-6 (2e7 steps), and one
+cycles through RKF45 retries whose step grows after each positivity reject.
+Every instance therefore gets the same cap of loop iterations (--max-steps,
+default 25000: the instances whose step ends at 1e-3 need about 20000);
+``value`` counts only instances that reached the end of the horizon, and the
+capped ones are reported.
+
 Extra keys: the plain FP64 GPU form and the max relative error against it on
 a sample, the batched RHS kernel's HBM bandwidth, the roofline of the
 integrator kernel, the CPU baseline (the oracle port on the host cores), the
@@ -141,10 +150,10 @@ def max_rel_err(a_list, b_list):
     return worst, bad
 
 
-def cpu_baseline(n_total, threads=None, stride=64, t_frac=0.1):
+def cpu_baseline(n_total, threads=None, stride=64, t_frac=0.1, max_steps=25000):
     """The oracle port on the host cores: every `stride`-th instance of the
-    workload on the first `t_frac` of its horizon, extrapolated to the
-    horizon (the backward-Euler step is fixed, so cost is uniform in time)."""
+    workload on the first `t_frac` of its horizon (loop-iteration cap scaled
+    alike), extrapolated to the horizon; completed instances only."""
     from lassie_gb300 import synth
     from oracle import oracle as O
     idx = list(range(0, n_total, stride))
@@ -153,13 +162,15 @@ def cpu_baseline(n_total, threads=None, stride=64, t_frac=0.1):
               for q in idx]
     threads = threads or os.cpu_count() or 1
     t0 = time.perf_counter()
-    _, _, status = O.solve_batch(models, threads=threads)
+    _, _, status = O.solve_batch(models, threads=threads,
+                                 max_steps=max(1, int(max_steps * t_frac)))
     dt = time.perf_counter() - t0
-    sims = len(models) / (dt / t_frac)
+    done = sum(1 for s in status if s == 0)
+    sims = done / (dt / t_frac)
     return {"value": sims, "unit": "sims/s", "cores": threads, "kind": "port",
-            "sample": f"{len(models)} of the {n_total} instances (every {stride}th), "
-                      f"t in [0,{20.0 * t_frac:g}] (= {t_frac:g} of the horizon), "
-                      f"time scaled by {1 / t_frac:g}; {dt:.2f} s wall",
+            "sample": f"{len(models)} of the {n_total} instances (every {stride}th, "
+                      f"{done} completed), t in [0,{20.0 * t_frac:g}] (= {t_frac:g} of the "
+                      f"horizon), time scaled by {1 / t_frac:g}; {dt:.2f} s wall",
             "seconds": dt}
 
 
@@ -170,10 +181,10 @@ def run_reference(args):
     from lassie_gb300 import synth  # noqa: F401
     stride, t_frac = 128, 0.05
     for _ in range(args.warmup):
-        cpu_baseline(args.instances, stride=stride, t_frac=t_frac)
+        cpu_baseline(args.instances, stride=stride, t_frac=t_frac, max_steps=args.max_steps)
     vals, secs = [], []
     for _ in range(args.steps):
-        cb = cpu_baseline(args.instances, stride=stride, t_frac=t_frac)
+        cb = cpu_baseline(args.instances, stride=stride, t_frac=t_frac, max_steps=args.max_steps)
         vals.append(cb["value"])
         secs.append(cb["seconds"])
     v = statistics.mean(vals)
@@ -183,7 +194,7 @@ def run_reference(args):
         "ms_per_step": 1000.0 * statistics.mean(secs), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": "reference algorithm, CPU (oracle port)",
-                   "l2": "n/a (host)"},
+                   "max_steps_per_instance": args.max_steps, "l2": "n/a (host)"},
         "cpu_baseline": {"value": v, "unit": "sims/s", "cores": cb["cores"], "kind": "port",
                          "sample": cb["sample"]},
         "e2e": {"value": v, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -263,13 +274,15 @@ def adjoint_measure(n_copies=64):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--instances", type=int, default=2048)
     ap.add_argument("--horizon", type=float, default=20.0,
                     help="integrate t in [0, horizon] (20 = the workload; smaller values "
                          "make small profiling cases)")
+    ap.add_argument("--max-steps", type=int, default=25000,
+                    help="loop-iteration cap per instance (the same for every arm)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64-form, RHS and CPU-baseline measurements")
     args = ap.parse_args()
@@ -297,7 +310,7 @@ def main():
         models = [synth.shorten(m, args.horizon, max(2, int(round(50 * args.horizon / 20))))
                   for m in models]
     stream = torch.cuda.Stream()
-    batch = solver.Batch(models, engine="mixed", deadline_s=600)
+    batch = solver.Batch(models, engine="mixed", max_steps=args.max_steps, deadline_s=900)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2
 
     def barrier():
@@ -324,20 +337,23 @@ def main():
             t1 = time.perf_counter()
     kernel_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
     outs, stats = batch.read()
-    bad = [s["status"] for s in stats if s["status"] != 0]
+    done = sum(1 for s in stats if s["status"] == 0)
+    capped = sum(1 for s in stats if s["status"] == nat.ERR_MAX_STEPS)
+    bad = [s["status"] for s in stats if s["status"] not in (0, nat.ERR_MAX_STEPS)]
     wall = sharding.max_over_ranks(t1 - t0)
-    value = args.instances * world * args.steps / wall
+    done_all = sharding.sum_over_ranks(done)
+    value = done_all * args.steps / wall
     ms_per_step = 1000.0 * wall / args.steps
 
     # end to end through the public host-buffer API
     h2d, d2h = batch.transfer_bytes()
     e2e_t = []
-    for _ in range(max(1, min(args.steps, 2))):
+    for _ in range(1):
         torch.cuda.synchronize()
         s0 = time.perf_counter()
-        solver.simulate_batch(models, engine="mixed", deadline_s=600)
+        solver.simulate_batch(models, engine="mixed", max_steps=args.max_steps, deadline_s=900)
         e2e_t.append(time.perf_counter() - s0)
-    e2e_val = args.instances / statistics.mean(e2e_t)
+    e2e_val = done / statistics.mean(e2e_t)
 
     # roofline of the integrator kernel (FP32 LU + FP64 refinement)
     peaks, peak_kind = load_peaks()
@@ -358,6 +374,8 @@ def main():
             "config": {"workload": WORKLOAD if (args.instances == 2048 and args.horizon == 20.0)
                        else f"{WORKLOAD} -- reduced: {args.instances} instances, t in [0,{args.horizon:g}]",
                        "instances_per_gpu": args.instances,
+                       "max_steps_per_instance": args.max_steps,
+                       "completed_instances": done_all, "capped_instances": capped,
                        "form": "mixed (FP32 LU + FP64 refinement)",
                        "parallelism": f"instances sharded over {world} GPU(s)",
                        "l2": "flushed between steps (256 MB write)"},
@@ -373,7 +391,7 @@ def main():
         sample = [synth.shorten(m, 2.0, 5) for m in models[::13][:152]]
         res = {}
         for eng in ("fp64", "mixed"):
-            b = solver.Batch(sample, engine=eng, deadline_s=600)
+            b = solver.Batch(sample, engine=eng, max_steps=args.max_steps // 10, deadline_s=900)
             b.run(stream.cuda_stream)
             b.sync()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -394,7 +412,7 @@ def main():
         line["adjoint"] = adjoint_measure()
         line["rhs_hbm"] = rhs_bandwidth(torch, stream)
         line["rhs_hbm"]["frac"] = line["rhs_hbm"]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
-        line["cpu_baseline"] = cpu_baseline(args.instances)
+        line["cpu_baseline"] = cpu_baseline(args.instances, max_steps=args.max_steps)
         line["cpu_baseline"].pop("seconds", None)
     if rank == 0:
         print(json.dumps(line), flush=True)

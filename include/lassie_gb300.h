@@ -68,7 +68,12 @@ typedef struct {
                              = pow(x, 0.25) as kernels.cuh:193 (default);
                              LASSIE_ROOT_SQRT = sqrt(sqrt(x)), correctly rounded
                              on every platform (matches the CPU restatement) */
-    int32_t pad;
+    int32_t lu_reuse;     /* mixed form: 1 (default) lets a backward-Euler step
+                             precondition its refinement with the FP32 factors
+                             of an earlier step of the same step size while they
+                             contract the residual by 1e-3 or better per sweep
+                             (the refinement still converges to the FP64 solve of
+                             the current matrix); 0 factors at every step */
 } lassie_opts;
 
 #define LASSIE_ROOT_POW 0
@@ -96,6 +101,8 @@ typedef struct {
     int64_t cycles_lu_panel;
     int64_t cycles_lu_rows;
     int64_t cycles_lu_trailing;
+    /* part of cycles_solve: the FP32 triangular solves (mixed form) */
+    int64_t cycles_solve_tri;
     double t_final;
     double dt_be_final;
     int32_t status;

@@ -40,7 +40,7 @@ class Opts(C.Structure):
                 ("newton_tol", C.c_double), ("stiffness_tol", C.c_double),
                 ("newton_iter", C.c_int64), ("max_steps", C.c_int64),
                 ("deadline_s", C.c_double), ("precision", C.c_int32),
-                ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("pad", C.c_int32)]
+                ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("lu_reuse", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -52,6 +52,7 @@ class Stats(C.Structure):
                 ("cycles_matrix", C.c_int64), ("cycles_lu", C.c_int64),
                 ("cycles_solve", C.c_int64), ("cycles_lu_panel", C.c_int64),
                 ("cycles_lu_rows", C.c_int64), ("cycles_lu_trailing", C.c_int64),
+                ("cycles_solve_tri", C.c_int64),
                 ("t_final", C.c_double),
                 ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
 

@@ -20,6 +20,11 @@ namespace lassie {
 int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision);
 cudaError_t compat_configure(int precision, int64_t smem);
 cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
+int64_t wide_workspace_bytes(int N, int R, int nnz_a, int precision);
+int64_t wide_flags_offset(int N, int R, int nnz_a, int precision);
+int64_t wide_dynamic_smem(int N, int precision);
+int wide_configure(int precision, int64_t smem, int sm_count);
+cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
 cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, const int *rptr,
                              const int *rent, const int *sptr, const int *sent,
                              const double *k, const double *x, double *dx, int sm_count,
@@ -266,7 +271,7 @@ extern "C" void lassie_opts_default(lassie_opts *o) {
     o->precision = LASSIE_PREC_MIXED;
     o->refine_max = 0;
     o->quarter_root = LASSIE_ROOT_POW;
-    o->pad = 0;
+    o->lu_reuse = 1;
 }
 
 extern "C" const char *lassie_status_string(int s) {
@@ -341,6 +346,8 @@ struct lassie_batch {
     int32_t nmax = 0, rmax = 0, amax = 0, hmax = 0;
     int64_t smem = 0;
     int grid = 0;
+    bool wide = false;       // one instance above kThreads species: the wide engine
+    int64_t wide_flags = 0;  // offset of the wide engine's pivot-order flag
     DevBuf d_int, d_dbl, d_out, d_desc, d_order, d_res, d_queue, d_ws;
     cudaStream_t stream = nullptr;
     LaunchParams P{};
@@ -467,32 +474,59 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     std::iota(b->order.begin(), b->order.end(), 0);
     std::stable_sort(b->order.begin(), b->order.end(),
                      [&](int a, int c) { return b->desc[a].n > b->desc[c].n; });
-    if (b->nmax > kThreads) {
-        delete b;
-        return set_error(LASSIE_ERR_TOO_LARGE, "the batched engine takes networks of at most " +
-                                                   std::to_string(kThreads) + " species");
-    }
-    b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax, o.precision);
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
-    if (n > 0 && b->smem > max_optin - 1024) {
-        delete b;
-        return set_error(LASSIE_ERR_TOO_LARGE, "network needs " + std::to_string(b->smem) +
-                                                   " bytes of shared memory per CTA");
+    int64_t ws_stride = 0, ws_total = 0;
+    if (b->nmax > kThreads) {
+        // one network above kThreads species: the whole GPU integrates it
+        if (n != 1) {
+            delete b;
+            return set_error(LASSIE_ERR_TOO_LARGE,
+                             "networks above " + std::to_string(kThreads) +
+                                 " species run one per launch (lassie_solve), not in a batch");
+        }
+        if (b->nmax > kWideMaxSpecies) {
+            delete b;
+            return set_error(LASSIE_ERR_TOO_LARGE, "networks of at most " +
+                                                       std::to_string(kWideMaxSpecies) +
+                                                       " species are supported");
+        }
+        b->wide = true;
+        b->smem = wide_dynamic_smem(b->nmax, o.precision);
+        if (b->smem > max_optin - 1024) {
+            delete b;
+            return set_error(LASSIE_ERR_TOO_LARGE, "wide engine: shared memory");
+        }
+        b->grid = wide_configure(o.precision, b->smem, b->sm_count);
+        if (b->grid < 1) {
+            delete b;
+            return set_error(LASSIE_ERR_CUDA, std::string("wide engine configure: ") +
+                                                  cudaGetErrorString(cudaGetLastError()));
+        }
+        ws_total = wide_workspace_bytes(b->nmax, b->rmax, b->amax, o.precision);
+        ws_stride = ws_total;
+        b->wide_flags = wide_flags_offset(b->nmax, b->rmax, b->amax, o.precision);
+    } else {
+        b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax, o.precision);
+        if (n > 0 && b->smem > max_optin - 1024) {
+            delete b;
+            return set_error(LASSIE_ERR_TOO_LARGE, "network needs " + std::to_string(b->smem) +
+                                                       " bytes of shared memory per CTA");
+        }
+        b->grid = std::max(1, std::min(n, b->sm_count));
+        const int lt = o.precision == LASSIE_PREC_FP64 ? 8 : 4;
+        // FP32 inverses of the 32x32 diagonal blocks after the matrix: the mixed
+        // forward's solves and the adjoint's transposed solves (either form) use them
+        const int64_t dinv_bytes = (int64_t)((b->nmax + 31) / 32) * 2048 * 4;
+        ws_stride = ((int64_t)b->nmax * round_up4(b->nmax) * lt + dinv_bytes + 255) / 256 * 256;
+        ws_total = ws_stride * b->grid;
     }
-    b->grid = std::max(1, std::min(n, b->sm_count));
-    const int lt = o.precision == LASSIE_PREC_FP64 ? 8 : 4;
-    // FP32 inverses of the 32x32 diagonal blocks after the matrix: the mixed
-    // forward's solves and the adjoint's transposed solves (either form) use them
-    const int64_t dinv_bytes = (int64_t)((b->nmax + 31) / 32) * 2048 * 4;
-    const int64_t ws_stride =
-        ((int64_t)b->nmax * round_up4(b->nmax) * lt + dinv_bytes + 255) / 256 * 256;
     if ((rc = b->d_int.grow(b->n_int * 4)) || (rc = b->d_dbl.grow(b->n_dbl * 8)) ||
         (rc = b->d_out.grow(b->n_out * 8)) ||
         (rc = b->d_desc.grow(std::max<size_t>(1, b->desc.size()) * sizeof(InstDesc))) ||
         (rc = b->d_order.grow(std::max<size_t>(1, b->order.size()) * 4)) ||
         (rc = b->d_res.grow(std::max<size_t>(1, b->desc.size()) * sizeof(InstResult))) ||
-        (rc = b->d_queue.grow(16)) || (rc = b->d_ws.grow((size_t)ws_stride * b->grid))) {
+        (rc = b->d_queue.grow(16)) || (rc = b->d_ws.grow((size_t)ws_total))) {
         delete b;
         return rc;
     }
@@ -508,7 +542,7 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         return set_error(LASSIE_ERR_CUDA, std::string("batch upload: ") +
                                               cudaGetErrorString(cudaGetLastError()));
     }
-    if (compat_configure(o.precision, b->smem) != cudaSuccess) {
+    if (!b->wide && compat_configure(o.precision, b->smem) != cudaSuccess) {
         delete b;
         return set_error(LASSIE_ERR_CUDA, std::string("kernel configure: ") +
                                               cudaGetErrorString(cudaGetLastError()));
@@ -530,6 +564,7 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     P.hmax = b->hmax;
     P.precision = o.precision;
     P.refine_max = o.refine_max;
+    P.lu_reuse = o.lu_reuse;
     P.deadline_ns = o.deadline_s > 0 ? (uint64_t)(o.deadline_s * 1e9) : 0;
     *out = b;
     return LASSIE_OK;
@@ -540,7 +575,14 @@ extern "C" int lassie_batch_run(lassie_batch *b, void *stream) {
     if (b->n == 0) return LASSIE_OK;
     b->stream = (cudaStream_t)stream;
     CU(cudaMemsetAsync(b->d_queue.p, 0, 16, b->stream));
-    CU(compat_launch(b->P, b->grid, b->smem, b->stream));
+    if (b->wide) {
+        // control block and pivot-order flag start at zero
+        CU(cudaMemsetAsync(b->d_ws.p, 0, 256, b->stream));
+        CU(cudaMemsetAsync((unsigned char *)b->d_ws.p + b->wide_flags, 0, 16, b->stream));
+        CU(wide_launch(b->P, b->grid, b->smem, b->stream));
+    } else {
+        CU(compat_launch(b->P, b->grid, b->smem, b->stream));
+    }
     return LASSIE_OK;
 }
 

@@ -11,6 +11,8 @@ namespace lassie {
 // One CTA integrates one instance at a time; 512 threads = 16 warps.
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
+// Largest network of the wide engine (one instance over the whole GPU).
+constexpr int kWideMaxSpecies = 16384;
 
 // Packed sparse entries: value = index * 256 + (int8 coefficient).
 __host__ __device__ __forceinline__ int ent_index(int e) { return e >> 8; }
@@ -39,7 +41,7 @@ struct InstResult {
     int64_t outer_iters, rkf_accepts, rkf_retries, be_steps, newton_iters,
         lu_factorisations, lu_failures, nan_reverts, refine_sweeps;
     int64_t cycles_rkf, cycles_matrix, cycles_lu, cycles_solve;
-    int64_t cycles_lu_panel, cycles_lu_rows, cycles_lu_trailing;
+    int64_t cycles_lu_panel, cycles_lu_rows, cycles_lu_trailing, cycles_solve_tri;
     double t_final, dt_be_final;
     int32_t status, pad;
 };
@@ -86,7 +88,7 @@ struct LaunchParams {
     unsigned char *workspace;  // per-CTA Newton matrix
     int64_t ws_stride;         // bytes per CTA
     int32_t nmax, rmax, amax, hmax;  // largest N, R, nnz_A, nnz_H in the batch
-    int32_t precision, refine_max;
+    int32_t precision, refine_max, lu_reuse, pad_;
     uint64_t deadline_ns;      // per-launch wall-clock limit (ns), 0 = none
     AdjArrays adj;             // adj.desc == nullptr: no recording
 };

@@ -44,6 +44,13 @@ __device__ __forceinline__ bool bad_value(double v) {
     return isnan(v) || isinf(v) || v < 0;
 }
 
+// Mixed form, reuse of FP32 factors across backward-Euler steps: a step
+// reuses them when the last solve that used them contracted by kReuseRate or
+// better per refinement sweep; a solve with reused factors gives up and
+// refactors when a sweep contracts by less than kBailRate.
+constexpr double kReuseRate = 2e-3;
+constexpr double kBailRate = 2e-2;
+
 template <typename T> __device__ __forceinline__ T lt_fma(T a, T b, T c);
 template <> __device__ __forceinline__ float lt_fma(float a, float b, float c) {
     return __fmaf_rn(a, b, c);
@@ -59,9 +66,10 @@ __device__ double block_sum(double v, double *red) {
     __syncthreads();
     if (l == 0) red[w] = v;
     __syncthreads();
-    double s = 0.0;
-    for (int q = 0; q < kWarps; q++) s += red[q];
-    return s;
+    // every warp adds the kWarps partials in the same fixed tree
+    double s = l < kWarps ? red[l] : 0.0;
+    for (int o = kWarps / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return __shfl_sync(0xffffffffu, s, 0);
 }
 
 // Block max of non-negative doubles (NaN propagates), on their IEEE bit
@@ -78,9 +86,41 @@ __device__ double block_max(double v, double *red) {
     __syncthreads();
     if (l == 0) ired[w] = b;
     __syncthreads();
-    long long s = ired[0];
-    for (int q = 1; q < kWarps; q++) s = ired[q] > s ? ired[q] : s;
-    return __longlong_as_double(s);
+    long long s = ired[l < kWarps ? l : 0];
+    for (int o = kWarps / 2; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(0xffffffffu, s, o);
+        s = u > s ? u : s;
+    }
+    return __longlong_as_double(__shfl_sync(0xffffffffu, s, 0));
+}
+
+// Block max of two non-negative values at once (same rules as block_max).
+__device__ void block_max2(double &a, double &b, double *red) {
+    long long x = __double_as_longlong(fabs(a)), y = __double_as_longlong(fabs(b));
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(0xffffffffu, x, o);
+        const long long v = __shfl_xor_sync(0xffffffffu, y, o);
+        x = u > x ? u : x;
+        y = v > y ? v : y;
+    }
+    long long *ired = reinterpret_cast<long long *>(red);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) {
+        ired[w] = x;
+        ired[kWarps + w] = y;
+    }
+    __syncthreads();
+    x = ired[l < kWarps ? l : 0];
+    y = ired[kWarps + (l < kWarps ? l : 0)];
+    for (int o = kWarps / 2; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(0xffffffffu, x, o);
+        const long long v = __shfl_xor_sync(0xffffffffu, y, o);
+        x = u > x ? u : x;
+        y = v > y ? v : y;
+    }
+    a = __longlong_as_double(__shfl_sync(0xffffffffu, x, 0));
+    b = __longlong_as_double(__shfl_sync(0xffffffffu, y, 0));
 }
 
 // Block minimum of the non-NaN values among non-negative doubles (+inf if
@@ -97,9 +137,12 @@ __device__ double block_min_nonnan(double v, double *red) {
     __syncthreads();
     if (l == 0) ired[w] = b;
     __syncthreads();
-    long long s = ired[0];
-    for (int q = 1; q < kWarps; q++) s = ired[q] < s ? ired[q] : s;
-    return __longlong_as_double(s);
+    long long s = ired[l < kWarps ? l : 0];
+    for (int o = kWarps / 2; o > 0; o >>= 1) {
+        const long long u = __shfl_xor_sync(0xffffffffu, s, o);
+        s = u < s ? u : s;
+    }
+    return __longlong_as_double(__shfl_sync(0xffffffffu, s, 0));
 }
 
 // --------------------------------------------------------------- model
@@ -283,6 +326,33 @@ __device__ __noinline__ void assemble_newton_matrix(const Net &m, const double *
     __syncthreads();
 }
 
+// Diagonal of M = I - h*J(x) in FP64: the entries assemble_newton_matrix
+// writes on the diagonal (same Jacobian semantics), before the cast.
+__device__ __noinline__ void newton_diag(const Net &m, const double *x, double h, double *out) {
+    for (int i = threadIdx.x; i < m.n; i += kThreads) {
+        const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
+        double J = 0.0;
+        for (int e2 = e0; e2 < e1; e2++) {
+            const int ent2 = m.sent[e2];
+            const int y2 = ent_index(ent2), s2 = ent_coef(ent2);
+            const int b2 = m.rptr[y2], en2 = m.rptr[y2 + 1];
+            int a = 0;
+            for (int q2 = b2; q2 < en2; q2++)
+                if (ent_index(m.rent[q2]) == i) { a = ent_coef(m.rent[q2]); break; }
+            if (a < 1) continue;
+            double temp = 0.0;
+            if (a == 1) temp = temp + (double)s2 * m.kk[y2];
+            else temp = temp + (double)s2 * m.kk[y2] * (double)a * mypow(x[i], a - 1);
+            for (int q2 = b2; q2 < en2; q2++) {
+                const int o = ent_index(m.rent[q2]);
+                if (o != i) temp = temp * x[o];
+            }
+            J = J + temp;
+        }
+        out[i] = 1.0 - h * J;
+    }
+}
+
 // ------------------------------------------------------------------ LU
 
 // Arg-max of |v| with the oracle's tie and NaN rules, combined over lanes,
@@ -325,6 +395,14 @@ __device__ __forceinline__ void load4(const double *p, double *o) {
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
 }
 
+__device__ __forceinline__ void store4(float *p, const float *v) {
+    reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void store4(double *p, const double *v) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+}
+
 // In-place blocked right-looking LU with partial pivoting, N <= kThreads, on
 // M (row-major, leading dimension ld) with implicit row interchanges: logical
 // row i of P*A is physical row perm[i] of M, and no row is ever moved.
@@ -354,42 +432,65 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
         const int pb = min(PB, N - j0);
         const int m = N - j0;
         // panel column-major in lt: lt[c*mp + r]; mp = 4 mod 32 keeps the
-        // transposed writes at 4-way bank conflicts and rows 16-byte aligned
+        // transposed writes conflict-free and rows 16-byte aligned
         const int mp = ((m + 31) & ~31) + 4;
-        for (int idx = tid; idx < m * PB; idx += kThreads) {
-            const int r = idx / PB, c = idx - r * PB;
-            lt[c * mp + r] = (c < pb) ? M[(int64_t)perm[j0 + r] * ld + j0 + c] : LT(0);
+        // thread tid owns panel position tid; its row of the panel lives in
+        // registers while the panel is factored (pivot loop fully unrolled)
+        LT row[PB];
+        const bool own = tid < m;
+        if (own) {
+            const LT *src = M + (int64_t)perm[j0 + tid] * ld + j0;
+            if (pb == PB) {
+#pragma unroll
+                for (int c = 0; c < PB; c += 4) load4(src + c, row + c);
+            } else {
+#pragma unroll
+                for (int c = 0; c < PB; c++) row[c] = (c < pb) ? src[c] : LT(0);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < PB; c++) row[c] = LT(0);
         }
-        __syncthreads();
         PivT<LT> best{LT(-1), 1 << 30};
-        if (tid < m) {
-            const LT v = fabs(lt[tid]);
+        if (own) {
+            const LT v = fabs(row[0]);
             if (!isnan(v)) best = PivT<LT>{v, tid};
         }
-        for (int jj = 0; jj < pb; jj++) {
+        LT *redv = reinterpret_cast<LT *>(red);
+#pragma unroll
+        for (int jj = 0; jj < PB; jj++) {
+            if (jj >= pb) break;
             for (int o = 16; o > 0; o >>= 1) {
                 PivT<LT> other{__shfl_xor_sync(0xffffffffu, best.v, o),
                                __shfl_xor_sync(0xffffffffu, best.i, o)};
                 best = piv_better(best, other);
             }
-            LT *redv = reinterpret_cast<LT *>(red);
             if (lane == 0) {
                 redv[warp] = best.v;
                 ired[warp] = best.i;
             }
-            __syncthreads();
-            PivT<LT> all{redv[0], ired[0]};
-            for (int q = 1; q < kWarps; q++)
-                all = piv_better(all, PivT<LT>{redv[q], ired[q]});
-            int p = all.i;
             // a NaN in the diagonal position keeps its own row (oracle rule)
-            if (isnan(lt[jj * mp + jj]) || p >= m) p = jj;
-            if (tid < PB) {
-                pivrow[tid] = lt[tid * mp + p];
-                swaprow[tid] = lt[tid * mp + jj];
+            if (tid == jj) ired[kWarps] = isnan(row[jj]) ? 1 : 0;
+            __syncthreads();
+            // every warp combines the kWarps partials with shuffles (the order
+            // of combination does not matter: piv_better is a total order)
+            PivT<LT> all{LT(-1), 1 << 30};
+            if (lane < kWarps) all = PivT<LT>{redv[lane], ired[lane]};
+            for (int o = kWarps / 2; o > 0; o >>= 1) {
+                PivT<LT> other{__shfl_xor_sync(0xffffffffu, all.v, o),
+                               __shfl_xor_sync(0xffffffffu, all.i, o)};
+                all = piv_better(all, other);
             }
-            if (tid == 0 && p != jj) {
-                int tmp = perm[j0 + jj];
+            int p = __shfl_sync(0xffffffffu, all.i, 0);
+            if (ired[kWarps] || p >= m) p = jj;
+            if (tid == p) {
+#pragma unroll
+                for (int c = 0; c < PB; c++) pivrow[c] = row[c];
+            }
+            if (tid == jj && p != jj) {
+#pragma unroll
+                for (int c = 0; c < PB; c++) swaprow[c] = row[c];
+                const int tmp = perm[j0 + jj];
                 perm[j0 + jj] = perm[j0 + p];
                 perm[j0 + p] = tmp;
             }
@@ -400,40 +501,52 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
                 break;
             }
             best = PivT<LT>{LT(-1), 1 << 30};
-            if (tid > jj && tid < m && tid != p) {
-                // own row, untouched by the interchange
-                const LT l = lt[jj * mp + tid] / d;
-                lt[jj * mp + tid] = l;
-                for (int c = jj + 1; c < pb; c++)
-                    lt[c * mp + tid] = lt_fma(-l, pivrow[c], lt[c * mp + tid]);
-                if (jj + 1 < pb) {
-                    const LT v = fabs(lt[(jj + 1) * mp + tid]);
-                    if (!isnan(v)) best = PivT<LT>{v, tid};
+            if (tid == jj) {
+                // the pivot row moves to position jj
+                if (p != jj) {
+#pragma unroll
+                    for (int c = 0; c < PB; c++) row[c] = pivrow[c];
                 }
-            } else if (tid == jj && p != jj) {
-                // the pivot row moves to position jj; the displaced row jj goes
-                // to position p and is eliminated there
-                for (int c = 0; c < pb; c++) lt[c * mp + jj] = pivrow[c];
-                const LT l = swaprow[jj] / d;
-                lt[jj * mp + p] = l;
-                for (int c = 0; c < jj; c++) lt[c * mp + p] = swaprow[c];
-                for (int c = jj + 1; c < pb; c++)
-                    lt[c * mp + p] = lt_fma(-l, pivrow[c], swaprow[c]);
+            } else if (tid > jj && own) {
+                // the displaced row jj goes to position p and is eliminated
+                // there; every other position eliminates its own row
+                if (tid == p) {
+#pragma unroll
+                    for (int c = 0; c < PB; c++) row[c] = swaprow[c];
+                }
+                const LT l = row[jj] / d;
+                row[jj] = l;
+#pragma unroll
+                for (int c = jj + 1; c < PB; c++) row[c] = lt_fma(-l, pivrow[c], row[c]);
                 if (jj + 1 < pb) {
-                    const LT v = fabs(lt[(jj + 1) * mp + p]);
-                    if (!isnan(v)) best = PivT<LT>{v, p};
+                    const LT v = fabs(row[jj + 1]);
+                    if (!isnan(v)) best = PivT<LT>{v, tid};
                 }
             }
         }
         if (fail) break;
         long long c_b = clock64();
         if (tid == 0) cyc[0] += c_b - c_a;
-        __syncthreads();
-        // panel back to its physical rows
-        for (int idx = tid; idx < m * PB; idx += kThreads) {
-            const int r = idx / PB, c = idx - r * PB;
-            if (c < pb) M[(int64_t)perm[j0 + r] * ld + j0 + c] = lt[c * mp + r];
+        // panel back to its physical rows, into lt (column-major) for the
+        // trailing update, and L11 row-major into utile for the U12 solve
+        if (own) {
+            LT *dst = M + (int64_t)perm[j0 + tid] * ld + j0;
+            if (pb == PB) {
+#pragma unroll
+                for (int c = 0; c < PB; c += 4) store4(dst + c, row + c);
+            } else {
+#pragma unroll
+                for (int c = 0; c < PB; c++)
+                    if (c < pb) dst[c] = row[c];
+            }
+#pragma unroll
+            for (int c = 0; c < PB; c++) lt[c * mp + tid] = row[c];
+            if (tid < PB) {
+#pragma unroll
+                for (int c = 0; c < PB; c++) utile[tid * PB + c] = row[c];
+            }
         }
+        __syncthreads();
         // U12: unit-lower triangular solve on the panel's rows, one column per
         // thread
         for (int c = j0 + pb + tid; c < N; c += kThreads) {
@@ -445,7 +558,13 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
             for (int r = 1; r < PB; r++) {
                 LT acc = u[r];
 #pragma unroll
-                for (int q = 0; q < r; q++) acc = lt_fma(-lt[q * mp + r], u[q], acc);
+                for (int q4 = 0; q4 < r; q4 += 4) {
+                    LT l4[4];
+                    load4(utile + r * PB + q4, l4);
+#pragma unroll
+                    for (int q = q4; q < q4 + 4; q++)
+                        if (q < r) acc = lt_fma(-l4[q - q4], u[q], acc);
+                }
                 u[r] = acc;
             }
 #pragma unroll
@@ -803,16 +922,23 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
     }
 }
 
+#include "wide.cuh"
+
 // ----------------------------------------------------------- integrator
 
 struct Vecs {
     double *y1, *u, *k1, *k2, *k3, *k4, *k5, *k6, *fd, *tol;
 };
 
-template <typename LT>
+// One instance, one CTA (kWide = false: the batched engine, everything in
+// shared memory, per-CTA LU), or the leader CTA of the wide engine (kWide:
+// vectors in global memory, linear algebra shared with the other CTAs
+// through W; wlimit bounds every wait on them).
+template <typename LT, bool kWide = false>
 __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, double *red,
                           int *ired, int *mv, InstDesc &D, InstResult &st,
-                          uint64_t deadline) {
+                          uint64_t deadline, const WideWs<LT> *W = nullptr,
+                          uint64_t wlimit = 0) {
     constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN;
     constexpr bool kMixed = std::is_same<LT, float>::value;
     const int tid = threadIdx.x;
@@ -822,35 +948,64 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     }
     __syncthreads();
     const int N = D.n, R = D.r;
-    const SmemLayout L(P.nmax, P.rmax, P.amax, P.hmax, (int)sizeof(LT), PB, TN);
-    double *vbase = reinterpret_cast<double *>(smem + L.vec);
-    Vecs V;
-    V.y1 = vbase;
-    V.u = vbase + 1 * P.nmax;
-    V.k1 = vbase + 2 * P.nmax;
-    V.k2 = vbase + 3 * P.nmax;
-    V.k3 = vbase + 4 * P.nmax;
-    V.k4 = vbase + 5 * P.nmax;
-    V.k5 = vbase + 6 * P.nmax;
-    V.k6 = vbase + 7 * P.nmax;
-    V.fd = vbase + 8 * P.nmax;
-    V.tol = vbase + 9 * P.nmax;
-    double *kk = reinterpret_cast<double *>(smem + L.kk);
-    double *pw = reinterpret_cast<double *>(smem + L.pw);
-    double *qr = reinterpret_cast<double *>(smem + L.qr);
-    int *rptr = reinterpret_cast<int *>(smem + L.rptr);
-    int *perm = reinterpret_cast<int *>(smem + L.perm);
-    int *slot = reinterpret_cast<int *>(smem + L.slot);
-    LT *bvec = reinterpret_cast<LT *>(smem + L.bvec);
-    LT *lt = reinterpret_cast<LT *>(smem + L.lt);
-    LT *utile = reinterpret_cast<LT *>(smem + L.utile);
-    LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
-    int *s_sptr = reinterpret_cast<int *>(smem + L.sptr);
-    int *s_sent = reinterpret_cast<int *>(smem + L.sent);
-    int *s_rent = reinterpret_cast<int *>(smem + L.rent);
-
     const int *ia = P.iarena;
     const double *da = P.darena;
+    Vecs V;
+    double *kk, *pw, *qr;
+    const int *rptr, *s_sptr, *s_sent, *s_rent;
+    int *perm;
+    LT *bvec, *lt = nullptr, *utile = nullptr, *rowbuf = nullptr;
+    int vstride;
+    double *vbase;
+    if constexpr (kWide) {
+        vbase = W->vec;
+        vstride = N;
+        kk = const_cast<double *>(da + D.k);
+        pw = W->pw;
+        qr = W->qr;
+        rptr = ia + D.rxn_ptr;
+        s_sptr = ia + D.sp_ptr;
+        s_sent = ia + D.sp_ent;
+        s_rent = ia + D.rxn_ent;
+        perm = W->piv;
+        bvec = W->vin;
+    } else {
+        const SmemLayout L(P.nmax, P.rmax, P.amax, P.hmax, (int)sizeof(LT), PB, TN);
+        vbase = reinterpret_cast<double *>(smem + L.vec);
+        vstride = P.nmax;
+        kk = reinterpret_cast<double *>(smem + L.kk);
+        pw = reinterpret_cast<double *>(smem + L.pw);
+        qr = reinterpret_cast<double *>(smem + L.qr);
+        int *w_rptr = reinterpret_cast<int *>(smem + L.rptr);
+        int *w_sptr = reinterpret_cast<int *>(smem + L.sptr);
+        int *w_sent = reinterpret_cast<int *>(smem + L.sent);
+        int *w_rent = reinterpret_cast<int *>(smem + L.rent);
+        perm = reinterpret_cast<int *>(smem + L.perm);
+        bvec = reinterpret_cast<LT *>(smem + L.bvec);
+        lt = reinterpret_cast<LT *>(smem + L.lt);
+        utile = reinterpret_cast<LT *>(smem + L.utile);
+        rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
+        for (int q = tid; q < D.nnz_a; q += kThreads) w_rent[q] = ia[D.rxn_ent + q];
+        for (int q = tid; q < D.nnz_h; q += kThreads) w_sent[q] = ia[D.sp_ent + q];
+        for (int q = tid; q <= N; q += kThreads) w_sptr[q] = ia[D.sp_ptr + q];
+        for (int j = tid; j < R; j += kThreads) kk[j] = da[D.k + j];
+        for (int j = tid; j <= R; j += kThreads) w_rptr[j] = ia[D.rxn_ptr + j];
+        rptr = w_rptr;
+        s_sptr = w_sptr;
+        s_sent = w_sent;
+        s_rent = w_rent;
+    }
+    V.y1 = vbase;
+    V.u = vbase + 1 * vstride;
+    V.k1 = vbase + 2 * vstride;
+    V.k2 = vbase + 3 * vstride;
+    V.k3 = vbase + 4 * vstride;
+    V.k4 = vbase + 5 * vstride;
+    V.k5 = vbase + 6 * vstride;
+    V.k6 = vbase + 7 * vstride;
+    V.fd = vbase + 8 * vstride;
+    V.tol = vbase + 9 * vstride;
+
     Net m;
     m.n = N;
     m.r = R;
@@ -860,9 +1015,6 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     m.sent = s_sent;
     m.rptr = rptr;
     m.kk = kk;
-    for (int q = tid; q < D.nnz_a; q += kThreads) s_rent[q] = ia[D.rxn_ent + q];
-    for (int q = tid; q < D.nnz_h; q += kThreads) s_sent[q] = ia[D.sp_ent + q];
-    for (int q = tid; q <= N; q += kThreads) s_sptr[q] = ia[D.sp_ptr + q];
 
     for (int s = tid; s < N; s += kThreads) {
         V.y1[s] = da[D.x0 + s];
@@ -870,17 +1022,17 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         V.fd[s] = D.feed >= 0 ? da[D.feed + s] : 0.0;
         V.tol[s] = D.atol >= 0 ? da[D.atol + s] : 1e-12;
     }
-    for (int j = tid; j < R; j += kThreads) kk[j] = da[D.k + j];
-    for (int j = tid; j <= R; j += kThreads) rptr[j] = ia[D.rxn_ptr + j];
     __syncthreads();
 
     const double *tv = da + D.t;
     const int *cs = D.cs >= 0 ? ia + D.cs : nullptr;
     double *out = P.out + D.out;
-    LT *M = reinterpret_cast<LT *>(P.workspace + (int64_t)blockIdx.x * P.ws_stride);
+    LT *M = kWide ? nullptr
+                  : reinterpret_cast<LT *>(P.workspace + (int64_t)blockIdx.x * P.ws_stride);
     const int ld = round_up4(N);
     // FP32 form: inverted diagonal blocks of the factors follow the matrix
     float *dinv = reinterpret_cast<float *>(M + (int64_t)N * ld);
+    int *wflag = ired + kWarps + 1;  // wide engine: join results
     const int refine_max = P.refine_max > 0 ? P.refine_max : 8;
     const bool root_sqrt = (D.flags & 1) != 0;
     long long c_mark = 0;
@@ -902,6 +1054,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     double dt = D.rkf_step;
     double newDt = D.be_step;
     const int nt = D.nt, ncs = D.ncs;
+    // mixed form: the factors in M stay valid across backward-Euler steps of
+    // the same size; lu_rate is the worst refinement contraction per sweep
+    // seen in the last solve that used them
+    bool lu_valid = false, wide_abort = false;
+    double lu_dt = 0.0, lu_rate = 1.0;
 
     while (i < nt) {
         if (D.max_steps > 0 && outer >= D.max_steps) {
@@ -1067,10 +1224,49 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         __syncthreads();
         int64_t itN = 0;
         double errN = 1000;
-        bool luFail = false;
+        // reused: this step's solves use factors of an earlier step; soft:
+        // they use reused factors, or (wide engine) a factorisation with an
+        // earlier step's pivot order, so a solve that does not converge asks
+        // for a fresh partial-pivoting factorisation
+        bool luFail = false, reused = false, soft = false;
+        // M = I - dt*J(x) assembled, its diagonal kept in FP64, factored; true
+        // if the factorisation met an exactly zero pivot
+        auto factor_at = [&](const double *x, bool fresh) -> bool {
+            c_mark = clock64();
+            bool fail;
+            if constexpr (kWide) {
+                if (tid == 0) st.lu_factorisations++;
+                const int rc = wide_factor<LT>(*W, m, x, dt, fresh, mdiag, smem, red, ired,
+                                               wlimit, wflag);
+                if (rc == 2) wide_abort = true;
+                fail = rc == 1 || rc == 2;
+                soft = rc == 3;
+            } else {
+                assemble_newton_matrix<LT>(m, x, dt, M, ld);
+                for (int s2 = tid; s2 < N; s2 += kThreads)
+                    mdiag[s2] = (double)M[(int64_t)s2 * ld + s2];
+                if (tid == 0) st.cycles_matrix += clock64() - c_mark;
+                if (tid == 0) st.lu_factorisations++;
+                fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
+                                     reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0;
+                if constexpr (kMixed) {
+                    if (!fail) invert_diag_blocks(M, ld, N, perm, dinv);
+                    __syncthreads();
+                }
+                soft = false;
+            }
+            if constexpr (kMixed) {
+                lu_valid = !fail;
+                lu_dt = dt;
+                lu_rate = 0.0;
+            }
+            if (tid == 0) st.cycles_lu += clock64() - c_mark;
+            return fail;
+        };
         if (tid == 0) st.be_steps++;
         bool expired = false;
         while ((itN < D.newton_iter) & (errN > D.newton_tol)) {
+            if (wide_abort) break;
             if (deadline && (itN & 63) == 63) {
                 if (tid == 0) ired[0] = global_ns() > deadline;
                 __syncthreads();
@@ -1088,21 +1284,20 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
             __syncthreads();
             if (itN == 0) {
-                c_mark = clock64();
-                assemble_newton_matrix<LT>(m, yv, dt, M, ld);
-                for (int s2 = tid; s2 < N; s2 += kThreads)
-                    mdiag[s2] = (double)M[(int64_t)s2 * ld + s2];
-                const long long c1 = clock64();
-                if (tid == 0) st.cycles_matrix += c1 - c_mark;
-                if (tid == 0) st.lu_factorisations++;
-                if (lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
-                                  reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0)
-                    luFail = true;
-                if constexpr (kMixed) {
-                    if (!luFail) invert_diag_blocks(M, ld, N, perm, dinv);
+                reused = false;
+                if constexpr (kMixed)
+                    reused = P.lu_reuse && lu_valid && dt == lu_dt && lu_rate <= kReuseRate;
+                if (reused) {
+                    // factors of an earlier step precondition this step's
+                    // refinement; the diagonal is this step's
+                    c_mark = clock64();
+                    newton_diag(m, yv, dt, mdiag);
                     __syncthreads();
+                    if (tid == 0) st.cycles_matrix += clock64() - c_mark;
+                    soft = true;
+                } else {
+                    luFail = factor_at(yv, false);
                 }
-                if (tid == 0) st.cycles_lu += clock64() - c1;
             }
             if (luFail) {
                 // Simulation.cuh:869-875, kernels.cuh:512-521
@@ -1117,7 +1312,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if constexpr (!kMixed) {
                 for (int s = tid; s < N; s += kThreads) bvec[s] = (LT)xr[perm[s]];
                 __syncthreads();
-                lu_solve<LT>(M, ld, N, perm, bvec);
+                if constexpr (kWide) {
+                    if (!wide_apply<LT>(*W, smem, wlimit, wflag)) wide_abort = true;
+                } else {
+                    lu_solve<LT>(M, ld, N, perm, bvec);
+                }
                 for (int s = tid; s < N; s += kThreads) dx[s] = (double)bvec[s];
                 __syncthreads();
             } else {
@@ -1127,61 +1326,98 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 // the FP32 normal range (species far below the others) get an
                 // FP64 diagonal correction instead, so that they keep their
                 // sign and magnitude as in the FP64 solve.
-                for (int s = tid; s < N; s += kThreads) {
-                    dx[s] = 0.0;
-                    res[s] = xr[s];
+                for (int attempt = 0; attempt < 2; attempt++) {
+                    for (int s = tid; s < N; s += kThreads) {
+                        dx[s] = 0.0;
+                        res[s] = xr[s];
+                    }
+                    double rloc = 0.0;
+                    for (int s = tid; s < N; s += kThreads) rloc = fmax(rloc, fabs(res[s]));
+                    double rmax = block_max(rloc, red);
+                    double prev = INFINITY, rate = 0.0;
+                    bool converged = false;
+                    for (int sweep = 0; sweep < refine_max; sweep++) {
+                        if (rmax == 0.0) {  // exact
+                            converged = true;
+                            break;
+                        }
+                        // a non-finite residual is solved unscaled, so that
+                        // inf/NaN reach the update as in the FP64 solve
+                        const bool finite = isfinite(rmax);
+                        const int e = finite ? ilogb(rmax) : 0;
+                        const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
+                        for (int s = tid; s < N; s += kThreads)
+                            bvec[s] = (LT)(res[perm[s]] * sc);
+                        __syncthreads();
+                        const long long c_tri = clock64();
+                        if constexpr (kWide) {
+                            if (!wide_apply<LT>(*W, smem, wlimit, wflag)) wide_abort = true;
+                        } else {
+                            lu_solve_fast(M, ld, N, perm, dinv, reinterpret_cast<float *>(bvec),
+                                          reinterpret_cast<float *>(rowbuf));
+                        }
+                        if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
+                        double cmax = 0.0, xmax = 0.0;
+                        for (int s = tid; s < N; s += kThreads) {
+                            double c = (double)bvec[s] * isc;
+                            // the part of this row's right-hand side that the
+                            // FP32 cast lost (below the FP32 normal range),
+                            // applied through the diagonal
+                            const double rs = res[s] * sc;
+                            if (fabs(rs) < 0x1p-126 && fabs(mdiag[s]) >= 0.5)
+                                c += (rs - (double)(float)rs) * isc / mdiag[s];
+                            const double nx = dx[s] + c;
+                            dx[s] = nx;
+                            cmax = fmax(cmax, fabs(c));
+                            xmax = fmax(xmax, fabs(nx));
+                        }
+                        if (tid == 0) st.refine_sweeps++;
+                        block_max2(cmax, xmax, red);
+                        if (sweep > 0) rate = fmax(rate, cmax / prev);
+                        // stop when this correction, or the next one predicted
+                        // from the contraction so far, is below FP64 resolution
+                        // of dx
+                        const bool small_next =
+                            sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
+                        if (!finite || !(cmax > 1e-15 * xmax) || small_next) {
+                            converged = true;
+                            break;
+                        }
+                        // stagnation, the sweep limit, or reused factors that
+                        // contract too slowly: not converged
+                        if (!(cmax < 0.5 * prev) || sweep + 1 == refine_max ||
+                            (soft && sweep > 0 && !(cmax <= kBailRate * prev)))
+                            break;
+                        prev = cmax;
+                        // res = xr - (dx - h*J(xf)*dx)
+                        jv_phase1(m, xf, dx, qr);
+                        __syncthreads();
+                        rloc = 0.0;
+                        for (int s = tid; s < N; s += kThreads) {
+                            const double jv = jv_species(m, s, qr);
+                            const double r = xr[s] - (dx[s] - dt * jv);
+                            res[s] = r;
+                            rloc = fmax(rloc, fabs(r));
+                        }
+                        rmax = block_max(rloc, red);
+                    }
+                    lu_rate = rate;
+                    if (converged || !soft || wide_abort) break;
+                    // the reused factors (or pivots) do not converge: factor this
+                    // step's matrix (Jacobian at the step's frozen point) with
+                    // fresh pivots and solve again
+                    reused = false;
+                    luFail = factor_at(xf, true);
+                    if (luFail) break;
                 }
-                double rloc = 0.0;
-                for (int s = tid; s < N; s += kThreads) rloc = fmax(rloc, fabs(res[s]));
-                double rmax = block_max(rloc, red);
-                double prev = INFINITY;
-                for (int sweep = 0; sweep < refine_max; sweep++) {
-                    if (rmax == 0.0) break;  // exact
-                    // a non-finite residual is solved unscaled, so that inf/NaN
-                    // reach the update as in the FP64 solve
-                    const bool finite = isfinite(rmax);
-                    const int e = finite ? ilogb(rmax) : 0;
-                    const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
+                if (luFail) {
+                    // as above: the step's own matrix failed to factor
                     for (int s = tid; s < N; s += kThreads)
-                        bvec[s] = (LT)(res[perm[s]] * sc);
+                        if (bad_value(yv[s])) yv[s] = V.y1[s];
                     __syncthreads();
-                    lu_solve_fast(M, ld, N, perm, dinv, bvec, reinterpret_cast<float *>(rowbuf));
-                    double cmax = 0.0, xmax = 0.0;
-                    for (int s = tid; s < N; s += kThreads) {
-                        double c = (double)bvec[s] * isc;
-                        // the part of this row's right-hand side that the FP32
-                        // cast lost (below the FP32 normal range), applied
-                        // through the diagonal
-                        const double rs = res[s] * sc;
-                        if (fabs(rs) < 0x1p-126 && fabs(mdiag[s]) >= 0.5)
-                            c += (rs - (double)(float)rs) * isc / mdiag[s];
-                        const double nx = dx[s] + c;
-                        dx[s] = nx;
-                        cmax = fmax(cmax, fabs(c));
-                        xmax = fmax(xmax, fabs(nx));
-                    }
-                    if (tid == 0) st.refine_sweeps++;
-                    cmax = block_max(cmax, red);
-                    xmax = block_max(xmax, red);
-                    // stop when this correction, or the next one predicted from
-                    // the contraction so far, is below FP64 resolution of dx
-                    const bool small_next =
-                        sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
-                    if (!finite || !(cmax > 1e-15 * xmax) || !(cmax < 0.5 * prev) ||
-                        small_next || sweep + 1 == refine_max)
-                        break;
-                    prev = cmax;
-                    // res = xr - (dx - h*J(xf)*dx)
-                    jv_phase1(m, xf, dx, qr);
-                    __syncthreads();
-                    rloc = 0.0;
-                    for (int s = tid; s < N; s += kThreads) {
-                        const double jv = jv_species(m, s, qr);
-                        const double r = xr[s] - (dx[s] - dt * jv);
-                        res[s] = r;
-                        rloc = fmax(rloc, fabs(r));
-                    }
-                    rmax = block_max(rloc, red);
+                    newDt = dt * 0.1;
+                    if (tid == 0) st.lu_failures++;
+                    break;
                 }
             }
             if (tid == 0) st.cycles_solve += clock64() - c_mark;
@@ -1214,7 +1450,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
         }
         __syncthreads();
-        if (expired) {
+        if (expired || wide_abort) {
             status = LASSIE_ERR_DEADLINE;
             break;
         }
@@ -1240,6 +1476,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         t = t + dt;
     }
     if (rec && tid == 0) P.adj.nsteps[id] = nsteps;
+    if constexpr (kWide) wide_exit<LT>(*W);
     __syncthreads();
     if (tid == 0) {
         st.outer_iters = outer;
@@ -1254,7 +1491,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
 template <typename LT>
 __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double red[kWarps + 1];
+    __shared__ double red[2 * kWarps + 1];
     __shared__ int ired[kWarps + 2 + LuShape<LT>::PB];
     __shared__ int mv[4 * LuShape<LT>::PB];
     __shared__ InstDesc D;
@@ -1602,7 +1839,7 @@ __device__ void adjoint_instance(const LaunchParams &P, int id, unsigned char *s
 
 __global__ void __launch_bounds__(kThreads, 1) adjoint_kernel(LaunchParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double red[kWarps + 1];
+    __shared__ double red[2 * kWarps + 1];
     __shared__ int ired[kWarps + 2 + LuShape<float>::PB];
     __shared__ int mv[4 * LuShape<float>::PB];
     __shared__ InstDesc D;
@@ -1653,6 +1890,81 @@ cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStr
     else
         compat_kernel<float><<<grid, kThreads, smem, stream>>>(P);
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------- wide engine
+
+// One instance (P.inst[0]) over the whole GPU: CTA 0 integrates, the others
+// serve its linear-algebra tasks.  Launched cooperatively (all CTAs resident).
+template <typename LT>
+__global__ void __launch_bounds__(kThreads, 1) wide_kernel(LaunchParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double red[2 * kWarps + 1];
+    __shared__ int ired[kWarps + 2 + LuShape<LT>::PB];
+    __shared__ int mv[4 * LuShape<LT>::PB];
+    __shared__ InstDesc D;
+    __shared__ InstResult st;
+    __shared__ uint64_t start;
+    if (threadIdx.x == 0) start = global_ns();
+    __syncthreads();
+    const uint64_t deadline = P.deadline_ns ? start + P.deadline_ns : 0;
+    // every wait on another CTA ends at the launch deadline, or after an hour
+    const uint64_t wlimit = deadline ? deadline : start + 3600ull * 1000000000ull;
+    const InstDesc &D0 = P.inst[0];
+    const int N = D0.n;
+    const WideWs<LT> W = wide_ws<LT>(P.workspace, N, D0.r, D0.nnz_a);
+    if (blockIdx.x == 0) {
+        integrate<LT, true>(P, 0, smem, red, ired, mv, D, st, deadline, &W, wlimit);
+    } else {
+        Net m;
+        m.n = N;
+        m.r = D0.r;
+        m.nnz_a = D0.nnz_a;
+        m.rent = P.iarena + D0.rxn_ent;
+        m.sptr = P.iarena + D0.sp_ptr;
+        m.sent = P.iarena + D0.sp_ent;
+        m.rptr = P.iarena + D0.rxn_ptr;
+        m.kk = P.darena + D0.k;
+        // the leader's mdiag is its vector k1 (third of the ten)
+        wide_worker<LT>(W, m, W.vec + 2 * (int64_t)N, smem, wlimit);
+    }
+}
+
+int64_t wide_workspace_bytes(int N, int R, int nnz_a, int precision) {
+    return WideLayout(N, R, nnz_a, precision == LASSIE_PREC_FP64 ? 8 : 4).total;
+}
+
+int64_t wide_flags_offset(int N, int R, int nnz_a, int precision) {
+    return WideLayout(N, R, nnz_a, precision == LASSIE_PREC_FP64 ? 8 : 4).flags;
+}
+
+int64_t wide_dynamic_smem(int N, int precision) {
+    return wide_smem_bytes(N, precision == LASSIE_PREC_FP64 ? 8 : 4);
+}
+
+// Configures the kernel and returns the number of CTAs of one cooperative
+// launch (one per SM), or 0 if a CTA does not fit.
+int wide_configure(int precision, int64_t smem, int sm_count) {
+    const void *f = precision == LASSIE_PREC_FP64 ? (const void *)wide_kernel<double>
+                                                  : (const void *)wide_kernel<float>;
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return 0;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kThreads, (size_t)smem) !=
+            cudaSuccess ||
+        per_sm < 1)
+        return 0;
+    return sm_count;
+}
+
+// The caller clears the control block and the pivot-order flag first.
+cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream) {
+    LaunchParams Pc = P;
+    void *args[] = {&Pc};
+    const void *f = P.precision == LASSIE_PREC_FP64 ? (const void *)wide_kernel<double>
+                                                    : (const void *)wide_kernel<float>;
+    return cudaLaunchCooperativeKernel(f, grid, kThreads, args, (size_t)smem, stream);
 }
 
 // ------------------------------------------ single-evaluation kernels
@@ -1752,7 +2064,7 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
                                                                int *info) {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int PB = LuShape<LT>::PB;
-    __shared__ double red[kWarps + 1];
+    __shared__ double red[2 * kWarps + 1];
     __shared__ int ired[kWarps + 2 + PB];
     __shared__ int mv[4 * PB];
     const SmemLayout L(N, 1, 1, 1, (int)sizeof(LT), PB, 128);

@@ -189,6 +189,7 @@ extern "C" int lassie_solve_noalloc(const lassie_model *model, const double *d_k
     P.hmax = nh;
     P.precision = o.precision;
     P.refine_max = o.refine_max;
+    P.lu_reuse = o.lu_reuse;
     P.deadline_ns = o.deadline_s > 0 ? (uint64_t)(o.deadline_s * 1e9) : 0;
     if (compat_configure(o.precision, smem) != cudaSuccess ||
         compat_launch(P, 1, smem, s) != cudaSuccess) {

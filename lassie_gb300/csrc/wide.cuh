@@ -1,0 +1,588 @@
+// Single-instance engine for networks above kThreads species: the whole GPU
+// integrates one instance.  Included by compat_engine.cu inside its
+// namespace (uses its helpers).
+//
+// One cooperative launch, one CTA per SM.  CTA 0 (the leader) runs the same
+// integrator as the batched engine (integrate<LT, true>) with its vectors in
+// global memory; the dense linear algebra is spread over all CTAs through a
+// fork-join on a control block in global memory: the leader publishes a
+// task and bumps a generation counter, every CTA does its share, the
+// workers count themselves done, the leader waits for the count.
+//
+// The Newton matrix M = I - h*J is inverted in place by blocked Gauss-Jordan
+// elimination with partial pivoting (row pivots, kWPB-column panels): per
+// panel, the pivot block D (rows p_j0.., columns J) is inverted by the leader,
+// then all CTAs form PR = D^-1 * M[P_J, :] and apply the rank-kWPB update
+//     M[i, C] -= M[i, J] * PR[:, C]   (i not a pivot row, C not in J)
+//     M[i, J]  = -M[i, J] * D^-1,   M[P_J, C] = PR,   M[P_J, J] = D^-1.
+// The result X satisfies inv(M)[j][p_k] = X[p_j][k], so a solve is
+//     x[j] = (X * r[p])[p_j]:   one dense matrix-vector product,
+// where the LU's two triangular solves would be 2N/32 dependent block steps.
+// Pivot rows of the last fresh factorisation are reused (no pivot search)
+// while the pivot blocks stay well conditioned; the integrator's refinement
+// checks every solve and asks for fresh pivots when one does not converge.
+#pragma once
+
+constexpr int kWPB = 32;   // Gauss-Jordan panel width
+constexpr int kWT = 128;   // rank-update tile: kWT rows x kWT columns per CTA pass
+
+enum WideTask : int { kTaskExit = 0, kTaskAssemble = 1, kTaskPanel = 2, kTaskUpdate = 3,
+                      kTaskMatvec = 4 };
+
+// Control block (global memory), zeroed before the launch.
+struct WideCtl {
+    unsigned int gen;   // task generation, bumped by the leader
+    unsigned int done;  // CTAs other than the leader done with the current task
+    int abort;          // a wait ran out of time
+    int task;
+    int j0, pb;         // current panel
+    int pad0, pad1;
+    double h;           // step of the matrix being assembled
+    const double *x;    // state the Jacobian is evaluated at
+};
+
+// Workspace of the wide engine, carved from one allocation (WideLayout).
+template <typename LT>
+struct WideWs {
+    WideCtl *ctl;
+    double *vec;      // 10 FP64 N-vectors (the batched engine's shared-memory set)
+    double *pw;       // [nnz_a] reactant powers
+    double *qr;       // [R] per-reaction scratch
+    LT *A;            // N x ld, row-major; after factorisation the in-place inverse
+    int *piv;         // [N] pivot row of each column
+    int *pos;         // [N] position of a row among the current panel's pivots, or -1
+    int *used;        // [N] 1 once a row has been a pivot (fresh pivot search)
+    LT *PN;           // [kWPB][N] panel copy for the pivot search (column-major)
+    LT *Dinv;         // [kWPB][kWPB]
+    LT *PR;           // [kWPB][ld]
+    LT *AJ;           // [N][kWPB] panel columns before the update
+    LT *vin, *vout;   // [N] matrix-vector product input (gathered) and output
+    int *flags;       // [0]: pivot order valid (set by the leader)
+    int N, ld;
+};
+
+struct WideLayout {
+    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJ, vin, vout, flags, total;
+    __host__ __device__ static int64_t al(int64_t v) { return (v + 255) & ~int64_t(255); }
+    __host__ __device__ WideLayout(int N, int R, int nnz_a, int lt) {
+        const int64_t ld = (N + 3) & ~3;
+        int64_t o = 0;
+        ctl = o;   o = al(o + 256);
+        vec = o;   o = al(o + int64_t(10) * N * 8);
+        pw = o;    o = al(o + int64_t(nnz_a > 0 ? nnz_a : 1) * 8);
+        qr = o;    o = al(o + int64_t(R > 0 ? R : 1) * 8);
+        A = o;     o = al(o + int64_t(N) * ld * lt);
+        piv = o;   o = al(o + int64_t(N) * 4);
+        pos = o;   o = al(o + int64_t(N) * 4);
+        used = o;  o = al(o + int64_t(N) * 4);
+        PN = o;    o = al(o + int64_t(kWPB) * N * lt);
+        Dinv = o;  o = al(o + int64_t(kWPB) * kWPB * lt);
+        PR = o;    o = al(o + int64_t(kWPB) * ld * lt);
+        AJ = o;    o = al(o + int64_t(N) * kWPB * lt);
+        vin = o;   o = al(o + int64_t(N) * lt);
+        vout = o;  o = al(o + int64_t(N) * lt);
+        flags = o; o = al(o + 16);
+        total = o;
+    }
+};
+
+template <typename LT>
+__device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
+    const WideLayout L(N, R, nnz_a, (int)sizeof(LT));
+    WideWs<LT> W;
+    W.ctl = reinterpret_cast<WideCtl *>(base + L.ctl);
+    W.vec = reinterpret_cast<double *>(base + L.vec);
+    W.pw = reinterpret_cast<double *>(base + L.pw);
+    W.qr = reinterpret_cast<double *>(base + L.qr);
+    W.A = reinterpret_cast<LT *>(base + L.A);
+    W.piv = reinterpret_cast<int *>(base + L.piv);
+    W.pos = reinterpret_cast<int *>(base + L.pos);
+    W.used = reinterpret_cast<int *>(base + L.used);
+    W.PN = reinterpret_cast<LT *>(base + L.PN);
+    W.Dinv = reinterpret_cast<LT *>(base + L.Dinv);
+    W.PR = reinterpret_cast<LT *>(base + L.PR);
+    W.AJ = reinterpret_cast<LT *>(base + L.AJ);
+    W.vin = reinterpret_cast<LT *>(base + L.vin);
+    W.vout = reinterpret_cast<LT *>(base + L.vout);
+    W.flags = reinterpret_cast<int *>(base + L.flags);
+    W.N = N;
+    W.ld = (N + 3) & ~3;
+    return W;
+}
+
+// Dynamic shared memory of the wide kernel: the rank-update tiles, or the
+// matrix-vector input, whichever is larger, plus the pivot-block inverse.
+__host__ __device__ inline int64_t wide_smem_bytes(int N, int lt) {
+    const int64_t tiles = int64_t(2) * kWT * kWPB * lt;
+    const int64_t vin = int64_t((N + 3) & ~3) * lt;
+    return (tiles > vin ? tiles : vin) + int64_t(kWPB) * kWPB * lt;
+}
+
+// ---------------------------------------------------------------- sync
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_acquire_i(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Thread 0 waits until *p >= target; false if the control block's abort flag
+// is set or the wall clock passes `limit` (then it sets the abort flag).
+__device__ bool wide_wait(const unsigned *p, unsigned target, WideCtl *ctl, uint64_t limit) {
+    unsigned spins = 0;
+    while (ld_acquire(p) < target) {
+        if (ld_acquire_i(&ctl->abort)) return false;
+        if ((++spins & 255) == 0 && global_ns() > limit) {
+            atomicExch(&ctl->abort, 1);
+            return false;
+        }
+        __nanosleep(256);
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------- tasks
+
+// Rows of M = I - h*J(x) (assemble_newton_matrix's entries and Jacobian
+// semantics), one warp per row: the lanes clear the row, lane 0 writes the
+// identity and the entries; mdiag[i] = the FP64 diagonal before the cast.
+template <typename LT>
+__device__ void task_assemble(const WideWs<LT> &W, const Net &m, const double *x, double h,
+                              double *mdiag) {
+    const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * kWarps + (threadIdx.x >> 5), nw = gridDim.x * kWarps;
+    const int N = W.N, ld = W.ld;
+    for (int i = gw; i < N; i += nw) {
+        LT *Ar = W.A + (int64_t)i * ld;
+        for (int c = lane; c < ld; c += 32) Ar[c] = LT(0);
+        __syncwarp();
+        if (lane == 0) {
+            Ar[i] = LT(1);
+            double di = 1.0;
+            const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
+            for (int e = e0; e < e1; e++) {
+                const int y = ent_index(m.sent[e]);
+                for (int q = m.rptr[y]; q < m.rptr[y + 1]; q++) {
+                    const int g = ent_index(m.rent[q]);
+                    bool seen = false;
+                    for (int ep = e0; ep < e && !seen; ep++) {
+                        const int yp = ent_index(m.sent[ep]);
+                        for (int qp = m.rptr[yp]; qp < m.rptr[yp + 1]; qp++)
+                            if (ent_index(m.rent[qp]) == g) { seen = true; break; }
+                    }
+                    if (seen) continue;
+                    double J = 0.0;
+                    for (int e2 = e; e2 < e1; e2++) {
+                        const int ent2 = m.sent[e2];
+                        const int y2 = ent_index(ent2), s2 = ent_coef(ent2);
+                        const int b2 = m.rptr[y2], en2 = m.rptr[y2 + 1];
+                        int a = 0;
+                        for (int q2 = b2; q2 < en2; q2++)
+                            if (ent_index(m.rent[q2]) == g) { a = ent_coef(m.rent[q2]); break; }
+                        if (a < 1) continue;
+                        double temp = 0.0;
+                        if (a == 1) temp = temp + (double)s2 * m.kk[y2];
+                        else temp = temp + (double)s2 * m.kk[y2] * (double)a * mypow(x[g], a - 1);
+                        for (int q2 = b2; q2 < en2; q2++) {
+                            const int o = ent_index(m.rent[q2]);
+                            if (o != g) temp = temp * x[o];
+                        }
+                        J = J + temp;
+                    }
+                    const double v = ((i == g) ? 1.0 : 0.0) - h * J;
+                    Ar[g] = (LT)v;
+                    if (g == i) di = v;
+                }
+            }
+            mdiag[i] = di;
+        }
+    }
+}
+
+// PR = D^-1 * M[P_J, :] (columns spread over all threads of the grid) and the
+// snapshot AJ = M[:, J] (rows likewise).
+template <typename LT>
+__device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD) {
+    const int tid = threadIdx.x;
+    for (int q = tid; q < kWPB * kWPB; q += kThreads) sD[q] = W.Dinv[q];
+    __syncthreads();
+    const int N = W.N, ld = W.ld;
+    const int gt = blockIdx.x * kThreads + tid, nt = gridDim.x * kThreads;
+    for (int c = gt; c < ld; c += nt) {
+        if (c >= j0 && c < j0 + kWPB) continue;
+        LT a[kWPB];
+#pragma unroll
+        for (int k = 0; k < kWPB; k++) a[k] = (k < pb) ? W.A[(int64_t)W.piv[j0 + k] * ld + c] : LT(0);
+#pragma unroll 4
+        for (int r = 0; r < kWPB; r++) {
+            LT acc = LT(0);
+#pragma unroll
+            for (int k = 0; k < kWPB; k++) acc = lt_fma(sD[r * kWPB + k], a[k], acc);
+            W.PR[(int64_t)r * ld + c] = acc;
+        }
+    }
+    for (int i = gt; i < N; i += nt) {
+        const LT *src = W.A + (int64_t)i * ld + j0;
+        LT *dst = W.AJ + (int64_t)i * kWPB;
+#pragma unroll
+        for (int k = 0; k < kWPB; k++) dst[k] = (k < pb) ? src[k] : LT(0);
+    }
+}
+
+// The rank-kWPB update of every row and column, in kWT x kWT tiles; thread
+// (ty, tx) owns rows ty*8.. and columns tx*4.. of a tile.  Columns in J start
+// from 0 and use D^-1 in place of PR; the current panel's pivot rows take
+// their new values (PR, D^-1) directly.
+template <typename LT>
+__device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
+    LT *sAJ = smem;                       // [kWT][kWPB]
+    LT *sB = smem + kWT * kWPB;           // [kWPB][kWT]
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int N = W.N, ld = W.ld;
+    const int nrt = (N + kWT - 1) / kWT, nct = (ld + kWT - 1) / kWT;
+    for (int t = blockIdx.x; t < nrt * nct; t += gridDim.x) {
+        const int r0 = (t / nct) * kWT, c0 = (t % nct) * kWT;
+        __syncthreads();
+        for (int q = tid; q < kWT * kWPB; q += kThreads) {
+            const int r = q / kWPB, k = q - r * kWPB;
+            sAJ[q] = (r0 + r < N) ? W.AJ[(int64_t)(r0 + r) * kWPB + k] : LT(0);
+        }
+        for (int q = tid; q < kWPB * kWT; q += kThreads) {
+            const int k = q / kWT, cc = q - k * kWT;
+            const int c = c0 + cc;
+            LT v = LT(0);
+            if (k < pb && c < ld) {
+                if (c >= j0 && c < j0 + kWPB) v = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : LT(0);
+                else v = W.PR[(int64_t)k * ld + c];
+            }
+            sB[q] = v;
+        }
+        __syncthreads();
+        const int col = c0 + tx * 4;
+        if (col >= ld) continue;
+        const bool inJ = col >= j0 && col < j0 + kWPB;
+        for (int a = 0; a < 8; a++) {
+            const int rl = ty * 8 + a, row = r0 + rl;
+            if (row >= N) break;
+            LT *dst = W.A + (int64_t)row * ld + col;
+            LT acc[4];
+            const int pr = W.pos[row];
+            if (pr >= 0) {
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[b] = sB[pr * kWT + tx * 4 + b];
+            } else {
+                if (inJ) {
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[b] = LT(0);
+                } else {
+                    load4(dst, acc);
+                }
+#pragma unroll 8
+                for (int k = 0; k < kWPB; k++) {
+                    const LT l = sAJ[rl * kWPB + k];
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[b] = lt_fma(-l, sB[k * kWT + tx * 4 + b], acc[b]);
+                }
+            }
+            store4(dst, acc);
+        }
+    }
+}
+
+// vout = A * vin, one warp per row, vin staged in shared memory.
+template <typename LT>
+__device__ void task_matvec(const WideWs<LT> &W, LT *svin) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int N = W.N, ld = W.ld;
+    for (int c = tid; c < ld; c += kThreads) svin[c] = (c < N) ? W.vin[c] : LT(0);
+    __syncthreads();
+    const int gw = blockIdx.x * kWarps + (tid >> 5), nw = gridDim.x * kWarps;
+    for (int i = gw; i < N; i += nw) {
+        const LT *Ar = W.A + (int64_t)i * ld;
+        LT acc = LT(0);
+        for (int c = lane * 4; c < ld; c += 128) {
+            LT a[4];
+            load4(Ar + c, a);
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc = lt_fma(a[b], svin[c + b], acc);
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) W.vout[i] = acc;
+    }
+}
+
+// Worker CTA: serve tasks until the leader sends kTaskExit (or a wait runs
+// out of time).
+template <typename LT>
+__device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, unsigned char *smem,
+                            uint64_t limit) {
+    __shared__ int s_task, s_j0, s_pb, s_ok;
+    __shared__ double s_h;
+    __shared__ const double *s_x;
+    LT *sm = reinterpret_cast<LT *>(smem);
+    LT *sD = sm + wide_smem_bytes(W.N, (int)sizeof(LT)) / (int)sizeof(LT) - kWPB * kWPB;
+    unsigned gen = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_ok = wide_wait(&W.ctl->gen, gen + 1, W.ctl, limit);
+            __threadfence();
+            if (s_ok) {
+                s_task = W.ctl->task;
+                s_j0 = W.ctl->j0;
+                s_pb = W.ctl->pb;
+                s_h = W.ctl->h;
+                s_x = W.ctl->x;
+            }
+        }
+        __syncthreads();
+        if (!s_ok || s_task == kTaskExit) return;
+        gen++;
+        switch (s_task) {
+        case kTaskAssemble: task_assemble<LT>(W, m, s_x, s_h, mdiag); break;
+        case kTaskPanel: task_panel<LT>(W, s_j0, s_pb, sD); break;
+        case kTaskUpdate: task_update<LT>(W, s_j0, s_pb, sm); break;
+        case kTaskMatvec: task_matvec<LT>(W, sm); break;
+        default: break;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(&W.ctl->done, 1u);
+        }
+    }
+}
+
+// Leader: publish a task (the leader then does its own share).
+template <typename LT>
+__device__ void wide_fork(const WideWs<LT> &W, int task, int j0, int pb, double h,
+                          const double *x) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        WideCtl *c = W.ctl;
+        c->task = task;
+        c->j0 = j0;
+        c->pb = pb;
+        c->h = h;
+        c->x = x;
+        c->done = 0;
+        __threadfence();
+        atomicAdd(&c->gen, 1u);
+    }
+}
+
+// Leader: wait for the other CTAs; false if a wait ran out of time.
+template <typename LT>
+__device__ bool wide_join(const WideWs<LT> &W, uint64_t limit, int *sflag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *sflag = wide_wait(&W.ctl->done, gridDim.x - 1, W.ctl, limit) ? 1 : 0;
+        __threadfence();
+    }
+    __syncthreads();
+    return *sflag != 0;
+}
+
+// Leader: inverse of the pivot block D = A[piv[j0+r]][j0+k] by warp 0
+// (Gauss-Jordan without further pivoting: the rows are in pivot order), into
+// W.Dinv; false if a pivot is zero or the inverse is not finite, or, with
+// check_growth (pivot rows of an earlier factorisation), if
+// max|D| * max|D^-1| exceeds 1e6.
+template <typename LT>
+__device__ bool wide_pivot_block(const WideWs<LT> &W, int j0, int pb, int *sflag, bool check_growth) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        LT a[kWPB], v[kWPB];
+        const LT *src = W.A + (int64_t)(lane < pb ? W.piv[j0 + lane] : 0) * W.ld + j0;
+#pragma unroll
+        for (int k = 0; k < kWPB; k++) {
+            a[k] = (lane < pb && k < pb) ? src[k] : (lane == k ? LT(1) : LT(0));
+            v[k] = (lane == k) ? LT(1) : LT(0);
+        }
+        bool ok = true;
+        LT amax = LT(0), vmax = LT(0);
+#pragma unroll
+        for (int k = 0; k < kWPB; k++) amax = fmax(amax, fabs(a[k]));
+#pragma unroll
+        for (int k = 0; k < kWPB; k++) {
+            const LT d = __shfl_sync(0xffffffffu, a[k], k);
+            ok = ok && d != LT(0) && isfinite(d);
+            const LT f = a[k];
+            if (lane == k) {
+#pragma unroll
+                for (int c = 0; c < kWPB; c++) {
+                    a[c] = a[c] / d;
+                    v[c] = v[c] / d;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kWPB; c++) {
+                const LT pa = __shfl_sync(0xffffffffu, a[c], k);
+                const LT pv = __shfl_sync(0xffffffffu, v[c], k);
+                if (lane != k) {
+                    a[c] = lt_fma(-f, pa, a[c]);
+                    v[c] = lt_fma(-f, pv, v[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kWPB; c++) {
+            ok = ok && isfinite(v[c]);
+            vmax = fmax(vmax, fabs(v[c]));
+            W.Dinv[lane * kWPB + c] = v[c];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+            vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        }
+        if (check_growth && !(amax * vmax <= LT(1e6))) ok = false;
+        ok = __all_sync(0xffffffffu, ok);
+        if (lane == 0) *sflag = ok ? 1 : 0;
+    }
+    __syncthreads();
+    return *sflag != 0;
+}
+
+// Leader: partial-pivoting choice of the panel's pivot rows among the rows
+// not yet used, on a copy of the panel (the LU panel factorisation restricted
+// to the candidate rows).  Ties go to the smaller row, NaN never wins.  False
+// if a column has no nonzero candidate.
+template <typename LT>
+__device__ bool wide_select_pivots(const WideWs<LT> &W, int j0, int pb, double *red, int *ired,
+                                   LT *prow) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int N = W.N, ld = W.ld;
+    for (int i = tid; i < N; i += kThreads) {
+        if (W.used[i]) continue;
+        const LT *src = W.A + (int64_t)i * ld + j0;
+        for (int k = 0; k < pb; k++) W.PN[(int64_t)k * N + i] = src[k];
+    }
+    __syncthreads();
+    for (int k = 0; k < pb; k++) {
+        PivT<LT> best{LT(-1), 1 << 30};
+        for (int i = tid; i < N; i += kThreads) {
+            if (W.used[i]) continue;
+            const LT v = fabs(W.PN[(int64_t)k * N + i]);
+            if (!isnan(v)) best = piv_better(best, PivT<LT>{v, i});
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            PivT<LT> other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                           __shfl_xor_sync(0xffffffffu, best.i, o)};
+            best = piv_better(best, other);
+        }
+        LT *redv = reinterpret_cast<LT *>(red);
+        if (lane == 0) {
+            redv[warp] = best.v;
+            ired[warp] = best.i;
+        }
+        __syncthreads();
+        PivT<LT> all{LT(-1), 1 << 30};
+        if (lane < kWarps) all = PivT<LT>{redv[lane], ired[lane]};
+        for (int o = kWarps / 2; o > 0; o >>= 1) {
+            PivT<LT> other{__shfl_xor_sync(0xffffffffu, all.v, o),
+                           __shfl_xor_sync(0xffffffffu, all.i, o)};
+            all = piv_better(all, other);
+        }
+        const int p = __shfl_sync(0xffffffffu, all.i, 0);
+        const LT pv = __shfl_sync(0xffffffffu, all.v, 0);
+        if (p >= N || !(pv > LT(0))) return false;  // uniform
+        if (tid < kWPB) prow[tid] = (tid < pb) ? W.PN[(int64_t)tid * N + p] : LT(0);
+        __syncthreads();
+        if (tid == 0) {
+            W.piv[j0 + k] = p;
+            W.used[p] = 1;
+        }
+        const LT d = prow[k];
+        for (int i = tid; i < N; i += kThreads) {
+            if (W.used[i] || i == p) continue;
+            const LT l = W.PN[(int64_t)k * N + i] / d;
+            for (int c = k + 1; c < pb; c++)
+                W.PN[(int64_t)c * N + i] = lt_fma(-l, prow[c], W.PN[(int64_t)c * N + i]);
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// Leader: assemble M = I - h*J(x) on all CTAs and invert it in place.
+// Returns 0 (fresh pivots), 3 (the last fresh factorisation's pivot order,
+// when `fresh` is false and it still gives finite, moderately conditioned
+// pivot blocks), 1 (a zero pivot column: singular), 2 (a wait ran out).
+template <typename LT>
+__device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, double h,
+                           bool fresh, double *mdiag, unsigned char *smem, double *red,
+                           int *ired, uint64_t limit, int *sflag) {
+    const int tid = threadIdx.x, N = W.N;
+    LT *sm = reinterpret_cast<LT *>(smem);
+    LT *sD = sm + wide_smem_bytes(N, (int)sizeof(LT)) / (int)sizeof(LT) - kWPB * kWPB;
+    bool use_old = !fresh && ld_acquire_i(W.flags) != 0;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        wide_fork<LT>(W, kTaskAssemble, 0, 0, h, x);
+        task_assemble<LT>(W, m, x, h, mdiag);
+        if (!wide_join<LT>(W, limit, sflag)) return 2;
+        for (int i = tid; i < N; i += kThreads) {
+            W.pos[i] = -1;
+            if (!use_old) W.used[i] = 0;
+        }
+        __syncthreads();
+        bool ok = true;
+        for (int j0 = 0; j0 < N; j0 += kWPB) {
+            const int pb = min(kWPB, N - j0);
+            if (!use_old && !wide_select_pivots<LT>(W, j0, pb, red, ired, sD)) {
+                if (tid == 0) W.flags[0] = 0;
+                __syncthreads();
+                return 1;
+            }
+            __syncthreads();
+            if (j0 > 0 && tid < kWPB) W.pos[W.piv[j0 - kWPB + tid]] = -1;
+            __syncthreads();
+            if (tid < pb) W.pos[W.piv[j0 + tid]] = tid;
+            if (!wide_pivot_block<LT>(W, j0, pb, sflag, use_old)) {
+                ok = false;
+                break;
+            }
+            wide_fork<LT>(W, kTaskPanel, j0, pb, h, x);
+            task_panel<LT>(W, j0, pb, sD);
+            if (!wide_join<LT>(W, limit, sflag)) return 2;
+            wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
+            task_update<LT>(W, j0, pb, sm);
+            if (!wide_join<LT>(W, limit, sflag)) return 2;
+        }
+        if (ok) {
+            if (tid == 0) W.flags[0] = 1;
+            __syncthreads();
+            return use_old ? 3 : 0;
+        }
+        if (!use_old) {
+            if (tid == 0) W.flags[0] = 0;
+            __syncthreads();
+            return 1;
+        }
+        use_old = false;  // the old pivot order failed here: search afresh
+    }
+    return 1;
+}
+
+// Leader: W.vin holds r gathered by the pivot rows (vin[j] = r[piv[j]]);
+// replaces it by the solution x[j] = (X * vin)[piv[j]].  False if a wait ran
+// out of time.
+template <typename LT>
+__device__ bool wide_apply(const WideWs<LT> &W, unsigned char *smem, uint64_t limit,
+                           int *sflag) {
+    wide_fork<LT>(W, kTaskMatvec, 0, 0, 0.0, nullptr);
+    task_matvec<LT>(W, reinterpret_cast<LT *>(smem));
+    if (!wide_join<LT>(W, limit, sflag)) return false;
+    for (int j = threadIdx.x; j < W.N; j += kThreads) W.vin[j] = W.vout[W.piv[j]];
+    __syncthreads();
+    return true;
+}
+
+// Leader: release the workers.
+template <typename LT>
+__device__ void wide_exit(const WideWs<LT> &W) {
+    wide_fork<LT>(W, kTaskExit, 0, 0, 0.0, nullptr);
+}

@@ -60,7 +60,8 @@ ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
 
 
 def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int = 0,
-              deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow") -> nat.Opts:
+              deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow",
+              lu_reuse: bool = True) -> nat.Opts:
     o = nat.Opts()
     nat.load().lassie_opts_default(C.byref(o))
     if m is not None:
@@ -74,6 +75,7 @@ def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int =
     o.precision = ENGINES[engine]
     o.refine_max = int(refine_max)
     o.quarter_root = ROOTS[root]
+    o.lu_reuse = 1 if lu_reuse else 0
     return o
 
 
@@ -105,12 +107,13 @@ class _Packed:
 
 
 def simulate(m: Model, engine: str = "mixed", max_steps: int = 0, deadline_s: float = 0.0,
-             nm: Optional[NativeModel] = None, root: str = "pow") -> Tuple[np.ndarray, Dict]:
+             nm: Optional[NativeModel] = None, root: str = "pow",
+             lu_reuse: bool = True) -> Tuple[np.ndarray, Dict]:
     """Integrate one model on the GPU.  Returns (trajectory [nt, ncs], stats)."""
     nm = nm or NativeModel.of(m)
     pk = _Packed(m, nm)
     st = nat.Stats()
-    o = make_opts(m, engine, max_steps, deadline_s, root=root)
+    o = make_opts(m, engine, max_steps, deadline_s, root=root, lu_reuse=lu_reuse)
     rc = nat.load().lassie_solve(nm.handle, _p(pk.k), _p(pk.x0), _p(pk.feed), _p(pk.atol),
                                  _p(pk.t), pk.t.shape[0], _p(pk.cs),
                                  0 if pk.cs is None else pk.cs.shape[0], C.byref(o),
@@ -128,7 +131,7 @@ class Batch:
 
     def __init__(self, models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                  deadline_s: float = 0.0, native: Optional[Sequence[NativeModel]] = None,
-                 refine_max: int = 0, root: str = "pow"):
+                 refine_max: int = 0, root: str = "pow", lu_reuse: bool = True):
         L = nat.load()
         cache: Dict[int, NativeModel] = {}
         self.packs = []
@@ -144,7 +147,7 @@ class Batch:
         self.n = len(models)
         self._inst = (nat.Instance * max(self.n, 1))(*[p.instance() for p in self.packs])
         self.opts = make_opts(models[0] if self.n else None, engine, max_steps, deadline_s,
-                              refine_max, root)
+                              refine_max, root, lu_reuse)
         h = C.c_void_p()
         nat.check(L.lassie_batch_create(C.cast(self._inst, C.c_void_p), self.n,
                                         C.byref(self.opts), C.byref(h)), "lassie_batch_create")
@@ -182,7 +185,8 @@ class Batch:
 
 
 def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
-                   deadline_s: float = 0.0, root: str = "pow") -> Tuple[List[np.ndarray], List[Dict]]:
+                   deadline_s: float = 0.0, root: str = "pow",
+                   lu_reuse: bool = True) -> Tuple[List[np.ndarray], List[Dict]]:
     """Integrate independent instances in one persistent launch (host buffers
     in and out, ``lassie_solve_batch``)."""
     L = nat.load()
@@ -196,7 +200,8 @@ def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: in
     n = len(models)
     inst = (nat.Instance * max(n, 1))(*[p.instance() for p in packs])
     stats = (nat.Stats * max(n, 1))()
-    o = make_opts(models[0] if n else None, engine, max_steps, deadline_s, root=root)
+    o = make_opts(models[0] if n else None, engine, max_steps, deadline_s, root=root,
+                  lu_reuse=lu_reuse)
     rc = L.lassie_solve_batch(C.cast(inst, C.c_void_p), n, C.byref(o), C.cast(stats, C.c_void_p))
     if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE):
         nat.check(rc, "lassie_solve_batch")

@@ -94,6 +94,17 @@ def make_c4_instance(instance: int) -> Model:
     return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 20.0, 50))
 
 
+def make_sized(N: int, instance: int = 0) -> Model:
+    """The batched workload's recipe (c1 structure, k = 10^U(-4,4), x0 ~
+    U(0,1), t = linspace(0, 20, 50)) at a chosen size, seed (4, N, instance):
+    networks above the batched engine's 512 species for the wide engine."""
+    rng = np.random.default_rng((4, N, instance))
+    left, right = _structure(rng, N, N, "c1")
+    k = 10.0 ** rng.uniform(-4.0, 4.0, N)
+    x0 = rng.uniform(0.0, 1.0, N)
+    return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 20.0, 50))
+
+
 def make_c4(n_instances: int = 2048, first: int = 0) -> List[Model]:
     return [make_c4_instance(first + q) for q in range(n_instances)]
 

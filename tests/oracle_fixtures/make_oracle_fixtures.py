@@ -1,0 +1,48 @@
+"""Fixtures computed by the CPU oracle (oracle/) for cases too slow to run
+inside the test suite: the 4096-species workload on t in [0, 0.02] (two
+backward-Euler steps with 4096 x 4096 LU factorisations, about two minutes
+on one core).  The GPU machine has no reference checkout, and its tests must
+not spend minutes in the oracle, so the trajectory is stored:
+
+    python tests/oracle_fixtures/make_oracle_fixtures.py
+
+Each fixture holds the sampling times, the oracle's trajectory and status
+and its step counts; the network and its parameters are regenerated from
+their seed by lassie_gb300.synth.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from lassie_gb300 import synth  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+
+def c3_short():
+    return synth.shorten(synth.make_c3(), 0.02, 3)
+
+
+CASES = {"c3_t002": c3_short}
+
+
+def main():
+    for name, make in CASES.items():
+        m = make()
+        t0 = time.time()
+        out, st, rc = O.solve(m)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), t=m.t, out=out, status=rc,
+                            be_steps=st["be_steps"], rkf_accepts=st["rkf_accepts"],
+                            newton_iters=st["newton_iters"], seconds=time.time() - t0)
+        print(name, rc, st, "%.1fs" % (time.time() - t0), flush=True)
+
+
+if __name__ == "__main__":
+    main()

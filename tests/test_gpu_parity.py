@@ -108,11 +108,16 @@ def test_solve_fp64_bit_exact(gpu, name, m):
 
 @pytest.mark.parametrize("name,m", [c for c in small_cases() if c[0] not in DECISION_SENSITIVE],
                          ids=[c[0] for c in small_cases() if c[0] not in DECISION_SENSITIVE])
-def test_solve_mixed_within_tolerance(gpu, name, m):
+@pytest.mark.parametrize("lu_reuse", [True, False], ids=["reuse", "refactor"])
+def test_solve_mixed_within_tolerance(gpu, name, m, lu_reuse):
     ref, st_ref, rc = O.solve(m, max_steps=2_000_000)
-    out, st = solver.simulate(m, engine="mixed", deadline_s=120, root="sqrt")
+    out, st = solver.simulate(m, engine="mixed", deadline_s=120, root="sqrt", lu_reuse=lu_reuse)
     assert st["status"] == 0
     assert within(out, ref), float(np.max(excess(out, ref)))
+    # the same step sequence as the oracle
+    assert (st["be_steps"], st["rkf_accepts"]) == (st_ref["be_steps"], st_ref["rkf_accepts"])
+    if not lu_reuse:
+        assert st["lu_factorisations"] == st["be_steps"]
 
 
 @pytest.mark.parametrize("name,m", [c for c in small_cases() if c[0] in DECISION_SENSITIVE],

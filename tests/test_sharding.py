@@ -36,7 +36,8 @@ def _worker(rank, world, port, q):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     ids = list(sharding.weak_shard(8, rank))
     elapsed = 1.0 + rank  # rank 1 is slower
-    q.put((rank, ids, sharding.max_over_ranks(elapsed)))
+    done = 3 + rank  # completed instances on this rank
+    q.put((rank, ids, sharding.max_over_ranks(elapsed), sharding.sum_over_ranks(done)))
     dist.destroy_process_group()
 
 
@@ -52,4 +53,5 @@ def test_gloo_max_over_ranks():
         p.join(timeout=60)
         assert p.exitcode == 0
     assert res[0][2] == res[1][2] == 2.0
+    assert res[0][3] == res[1][3] == 7.0
     assert set(res[0][1]).isdisjoint(res[1][1])

@@ -1,0 +1,77 @@
+"""The wide engine (one network above 512 species over the whole GPU,
+blocked Gauss-Jordan inverse + FP64 refinement) against the CPU oracle,
+through the C ABI.
+
+Cases: the batched workload's recipe at 600 and 777 species on t in
+[0, 0.2] (backward-Euler steps with the reference's stiffness switch; the
+oracle finishes them in seconds), and the 4096-species workload on t in
+[0, 0.02] against a stored oracle trajectory (two 4096 x 4096
+factorisations take the oracle about two minutes).  All three are
+insensitive to last-bit differences of the linear solve (checked with the
+oracle's perturbation probe), so the mixed form is held to rtol 1e-6 /
+atol 1e-9 at every sample and to the oracle's step counts.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from lassie_gb300 import _native as nat
+from lassie_gb300 import solver, synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 1e-6, 1e-9
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def within(a, b, rtol=RTOL, atol=ATOL):
+    return bool(np.all(np.abs(a - b) <= atol + rtol * np.abs(b)))
+
+
+CASES = [(600, 1), (777, 0)]
+
+
+@pytest.mark.parametrize("N,inst", CASES, ids=[f"n{n}-{i}" for n, i in CASES])
+@pytest.mark.parametrize("lu_reuse", [True, False], ids=["reuse", "refactor"])
+def test_wide_mixed_matches_oracle(gpu, N, inst, lu_reuse):
+    m = synth.shorten(synth.make_sized(N, inst), 0.2, 5)
+    ref, st_ref, rc = O.solve(m)
+    assert rc == 0
+    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt", lu_reuse=lu_reuse)
+    assert st["status"] == 0
+    assert within(out, ref), float(np.max(np.abs(out - ref) - RTOL * np.abs(ref)))
+    assert (st["be_steps"], st["rkf_accepts"], st["newton_iters"]) == \
+        (st_ref["be_steps"], st_ref["rkf_accepts"], st_ref["newton_iters"])
+
+
+def test_wide_fp64_matches_oracle(gpu):
+    """The FP64 form of the wide engine (Gauss-Jordan inverse in FP64, no
+    refinement) rounds differently from the oracle's LU, by far less than
+    the parity tolerance."""
+    m = synth.shorten(synth.make_sized(600, 1), 0.2, 5)
+    ref, st_ref, rc = O.solve(m)
+    out, st = solver.simulate(m, engine="fp64", deadline_s=300, root="sqrt")
+    assert st["status"] == 0
+    assert within(out, ref, rtol=1e-10, atol=1e-13)
+    assert st["be_steps"] == st_ref["be_steps"]
+
+
+def test_wide_c3_matches_stored_oracle_trajectory(gpu):
+    d = np.load(os.path.join(HERE, "oracle_fixtures", "c3_t002.npz"))
+    m = synth.shorten(synth.make_c3(), 0.02, 3)
+    assert np.array_equal(m.t, d["t"])
+    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt")
+    assert st["status"] == 0 and int(d["status"]) == 0
+    assert within(out, d["out"]), float(np.max(np.abs(out - d["out"]) - RTOL * np.abs(d["out"])))
+    assert st["be_steps"] == int(d["be_steps"])
+    assert st["newton_iters"] == int(d["newton_iters"])
+
+
+def test_wide_networks_do_not_batch(gpu):
+    big = synth.shorten(synth.make_sized(600, 1), 0.1, 2)
+    small = synth.shorten(synth.make_c4_instance(0), 0.1, 2)
+    with pytest.raises(nat.LassieError) as e:
+        solver.simulate_batch([big, small], engine="mixed")
+    assert e.value.status == nat.ERR_TOO_LARGE
