@@ -240,6 +240,31 @@ def rhs_bandwidth(torch, stream, n_inst=65536, reps=20):
             "network": "256 species x 256 reactions", "instances": n_inst}
 
 
+def parity_table():
+    """Max relative error (|a-b| / max(|b|, atol/rtol)) of the mixed form
+    against the plain FP64 GPU form, which equals the CPU oracle bit for bit
+    for N <= 512 (tests/test_gpu_parity.py), per configuration on horizons
+    the FP64 form finishes in seconds, with both forms' step counts."""
+    import numpy as np
+    from lassie_gb300 import synth, solver
+    cases = {
+        "c1 (64 x 64, t in [0,10])": synth.make_c1(),
+        "c2 (512 x 512 stiff, t in [0,0.004])": synth.shorten(synth.make_c2(), 0.004, 3),
+        "c3 (4096 x 4096, t in [0,0.02])": synth.shorten(synth.make_c3(), 0.02, 3),
+        "c5 (256 x 256, t in [0,1])": synth.shorten(synth.make_c5(1)[0][0], 1.0, 9),
+    }
+    out = {}
+    for name, m in cases.items():
+        a, sa = solver.simulate(m, engine="mixed", deadline_s=600)
+        b, sb = solver.simulate(m, engine="fp64", deadline_s=600)
+        rel = np.abs(a - b) / np.maximum(np.abs(b), ATOL / RTOL)
+        out[name] = {"max_rel_err": float(rel.max()),
+                     "within_rtol1e-6_atol1e-9": bool(np.all(np.abs(a - b) <= ATOL + RTOL * np.abs(b))),
+                     "steps_mixed": [sa["be_steps"], sa["rkf_accepts"], sa["newton_iters"]],
+                     "steps_fp64": [sb["be_steps"], sb["rkf_accepts"], sb["newton_iters"]]}
+    return out
+
+
 def adjoint_measure(n_copies=64):
     """Differentiation workload: 64 copies of a 256 x 256 network,
     k = 10^U(-3,3), loss = sum of squares over 40 samples in (0,10] against
@@ -404,11 +429,22 @@ def main():
             o, st = b.read()
             res[eng] = (e0.elapsed_time(e1), o, st)
         worst, nbad = max_rel_err(res["mixed"][1], res["fp64"][1])
+        # instances whose two forms took the same step sequence, and the rest
+        # (a rounding-driven step decision went the other way)
+        key = lambda st: (st["be_steps"], st["rkf_accepts"], st["newton_iters"])  # noqa: E731
+        same = [q for q, (a, b) in enumerate(zip(res["mixed"][2], res["fp64"][2]))
+                if key(a) == key(b)]
+        w_same, n_same = max_rel_err([res["mixed"][1][q] for q in same],
+                                     [res["fp64"][1][q] for q in same])
         line["fp64_form"] = {
             "sample": f"{len(sample)} instances (every 13th), t in [0,2] (0.1 of horizon)",
             "fp64_ms": res["fp64"][0], "mixed_ms": res["mixed"][0],
             "speedup_mixed_vs_fp64": res["fp64"][0] / res["mixed"][0],
-            "max_rel_err_vs_fp64": worst, "points_outside_rtol1e-6_atol1e-9": nbad}
+            "max_rel_err_vs_fp64": worst, "points_outside_rtol1e-6_atol1e-9": nbad,
+            "instances_same_step_sequence": len(same),
+            "max_rel_err_same_step_sequence": w_same,
+            "points_outside_same_step_sequence": n_same}
+        line["parity_vs_fp64_form"] = parity_table()
         line["adjoint"] = adjoint_measure()
         line["rhs_hbm"] = rhs_bandwidth(torch, stream)
         line["rhs_hbm"]["frac"] = line["rhs_hbm"]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))

@@ -25,7 +25,7 @@ int64_t wide_flags_offset(int N, int R, int nnz_a, int precision);
 int64_t wide_dynamic_smem(int N, int precision);
 int wide_configure(int precision, int64_t smem, int sm_count);
 cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
-cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, const int *rptr,
+cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, int nnz_h, const int *rptr,
                              const int *rent, const int *sptr, const int *sent,
                              const double *k, const double *x, double *dx, int sm_count,
                              cudaStream_t stream);
@@ -804,7 +804,8 @@ extern "C" int lassie_rhs_device(const lassie_model *cm, int32_t n_inst, const d
     int dev = 0, sms = 0;
     CU(cudaGetDevice(&dev));
     CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    CU(rhs_batch_launch(n_inst, m->N, m->R, (int)m->rxn_ent.size(), d, d + m->off_rent(),
+    CU(rhs_batch_launch(n_inst, m->N, m->R, (int)m->rxn_ent.size(), (int)m->sp_ent.size(), d,
+                        d + m->off_rent(),
                         d + m->off_sptr(), d + m->off_sent(), k, x, dx, sms,
                         (cudaStream_t)stream));
     return LASSIE_OK;

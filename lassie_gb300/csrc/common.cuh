@@ -99,7 +99,7 @@ struct LaunchParams {
 // (PB x (round_up32(N) + 4), plus slack for the 8-row tile reads past its end),
 // utile one PB x 128 tile of U12, rowbuf the pivot and swap rows.
 struct SmemLayout {
-    int64_t vec, kk, pw, qr, rptr, sptr, sent, rent, perm, slot, bvec, lt, utile, rowbuf, total;
+    int64_t vec, kk, pw, qr, rptr, sptr, sent, rent, perm, slot, bvec, lt, utile, rowbuf, dblk, total;
     __host__ __device__ static int64_t align(int64_t v) { return (v + 15) & ~int64_t(15); }
     __host__ __device__ SmemLayout(int nmax, int rmax, int amax, int hmax, int lt_bytes, int pb,
                                    int tn) {
@@ -118,6 +118,7 @@ struct SmemLayout {
         lt = o;     o = align(o + (int64_t(pb) * (((nmax + 31) & ~31) + 4) + 160) * lt_bytes);
         utile = o;  o = align(o + int64_t(pb) * tn * lt_bytes);
         rowbuf = o; o = align(o + int64_t(2 * pb) * lt_bytes);
+        dblk = o;   o = align(o + int64_t(pb) * pb * lt_bytes);
         total = o;
     }
 };

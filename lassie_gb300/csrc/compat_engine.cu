@@ -32,6 +32,7 @@ __device__ __forceinline__ uint64_t global_ns() {
 
 // kernels.cuh:52-63 (myPow): repeated multiplication, 1 for ex <= 0.
 __device__ __forceinline__ double mypow(double b, int e) {
+    if (e == 1) return b;  // 1.0 * b == b exactly
     double p = 1.0;
     while (e > 0) {
         p = p * b;
@@ -177,6 +178,45 @@ __device__ __forceinline__ double rhs_species(const Net &m, int i, const double 
         double v = (double)ent_coef(ent) * m.kk[y];
         const int b = m.rptr[y], en = m.rptr[y + 1];
         for (int q = b; q < en; q++) v = v * pw[q];
+        acc = acc + v;
+    }
+    return acc;
+}
+
+// The same RHS with the reaction products formed once per reaction:
+// rate[y] = ((k_y * pw_0) * pw_1) ... in reactant order, and pw[q] as above.
+// A net coefficient of +-1 contributes +-rate[y], which equals the per-entry
+// product ((+-1 * k_y) * pw_0) * ... bit for bit (negation commutes with
+// rounding); other coefficients use the per-entry product.  On this GPU the
+// FP64 pipe, not HBM, bounds the RHS, so the per-entry FP64 work matters.
+__device__ __forceinline__ void rhs_rates(const Net &m, const double *x, double *pw,
+                                          double *rate) {
+    for (int y = threadIdx.x; y < m.r; y += kThreads) {
+        double r = m.kk[y];
+        for (int q = m.rptr[y]; q < m.rptr[y + 1]; q++) {
+            const int e = m.rent[q];
+            const double p = mypow(x[ent_index(e)], ent_coef(e));
+            pw[q] = p;
+            r = r * p;
+        }
+        rate[y] = r;
+    }
+}
+
+__device__ __forceinline__ double rhs_species_r(const Net &m, int i, const double *pw,
+                                                const double *rate) {
+    double acc = 0.0;
+    const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
+    for (int e = e0; e < e1; e++) {
+        const int ent = m.sent[e];
+        const int y = ent_index(ent), c = ent_coef(ent);
+        double v;
+        if (c == 1) v = rate[y];
+        else if (c == -1) v = -rate[y];
+        else {
+            v = (double)c * m.kk[y];
+            for (int q = m.rptr[y]; q < m.rptr[y + 1]; q++) v = v * pw[q];
+        }
         acc = acc + v;
     }
     return acc;
@@ -496,6 +536,7 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
             }
             __syncthreads();
             const LT d = pivrow[jj];
+            const LT rd = LT(1) / d;
             if (d == LT(0)) {
                 fail = j0 + jj + 1;
                 break;
@@ -514,7 +555,10 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
 #pragma unroll
                     for (int c = 0; c < PB; c++) row[c] = swaprow[c];
                 }
-                const LT l = row[jj] / d;
+                // a zero multiplier needs no division: 0 * (1/d) is the same
+                // signed zero as 0 / d, and most entries of M are zero
+                const LT num = row[jj];
+                const LT l = (num == LT(0)) ? num * rd : num / d;
                 row[jj] = l;
 #pragma unroll
                 for (int c = jj + 1; c < PB; c++) row[c] = lt_fma(-l, pivrow[c], row[c]);
@@ -632,6 +676,274 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
     return fail;
 }
 
+// FP32 form: in-place Gauss-Jordan inverse of M (row-major, N <= kThreads)
+// with partial pivoting by rows, in kPB-column panels J:
+//   pivot rows P_J: per column, the largest |value| among the rows that are
+//     not yet pivots, after the panel's earlier columns are eliminated from
+//     them (ties to the smaller row, NaN never wins); each candidate keeps
+//     its row of the panel in registers;
+//   D^-1 of the pivot block D = M[P_J, J] by warp 0 (shuffles);
+//   every 128 x 128 tile:  M[i, C] -= M[i, J] * B[:, C]  (i not in P_J),
+//     M[i, J] = -M[i, J] * D^-1,  M[P_J, :] = B,  with B = D^-1 M[P_J, C]
+//     outside J and D^-1 inside J (M[:, J] is read from a snapshot in lt).
+// perm[j] = pivot row of column j; the result X satisfies
+// inv(M)[j][perm[k]] = X[perm[j]][k] (gje_apply).  pos: N ints of scratch.
+// Returns 0, or j+1 if column j has no nonzero candidate.
+__device__ __noinline__ int gje_factor(float *M, int ld, int N, int *perm, int *pos, float *lt,
+                                       float *utile, float *dblk, float *rowbuf, double *red,
+                                       int *ired, long long *cyc) {
+    constexpr int PB = 32, TN = 128, TM = 128;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int mp = ((N + 31) & ~31) + 4;  // lt: panel snapshot, column-major
+    float *pivrow = rowbuf;
+    float *redv = reinterpret_cast<float *>(red);
+    for (int i = tid; i < N; i += kThreads) pos[i] = -1;  // -1 candidate, -2 used
+    __syncthreads();
+    int fail = 0;
+    long long c_a = clock64();
+    for (int j0 = 0; j0 < N; j0 += PB) {
+        const int pb = min(PB, N - j0);
+        float row[PB];
+        const bool own = tid < N;
+        if (own) {
+            const float *src = M + (int64_t)tid * ld + j0;
+            if (pb == PB) {
+#pragma unroll
+                for (int c = 0; c < PB; c += 4) load4(src + c, row + c);
+            } else {
+#pragma unroll
+                for (int c = 0; c < PB; c++) row[c] = (c < pb) ? src[c] : 0.f;
+            }
+#pragma unroll
+            for (int c = 0; c < PB; c++) lt[c * mp + tid] = row[c];
+        }
+        bool cand = own && pos[tid] == -1;
+        PivT<float> best{-1.f, 1 << 30};
+        if (cand) {
+            const float v = fabsf(row[0]);
+            if (!isnan(v)) best = PivT<float>{v, tid};
+        }
+#pragma unroll
+        for (int jj = 0; jj < PB; jj++) {
+            if (jj >= pb) break;
+            for (int o = 16; o > 0; o >>= 1) {
+                PivT<float> other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                                  __shfl_xor_sync(0xffffffffu, best.i, o)};
+                best = piv_better(best, other);
+            }
+            if (lane == 0) {
+                redv[warp] = best.v;
+                ired[warp] = best.i;
+            }
+            __syncthreads();
+            PivT<float> all{-1.f, 1 << 30};
+            if (lane < kWarps) all = PivT<float>{redv[lane], ired[lane]};
+            for (int o = kWarps / 2; o > 0; o >>= 1) {
+                PivT<float> other{__shfl_xor_sync(0xffffffffu, all.v, o),
+                                  __shfl_xor_sync(0xffffffffu, all.i, o)};
+                all = piv_better(all, other);
+            }
+            const int p = __shfl_sync(0xffffffffu, all.i, 0);
+            const float pv = __shfl_sync(0xffffffffu, all.v, 0);
+            if (p >= N || !(pv > 0.f)) {  // uniform
+                fail = j0 + jj + 1;
+                break;
+            }
+            if (tid == p) {
+#pragma unroll
+                for (int c = 0; c < PB; c++) pivrow[c] = row[c];
+                perm[j0 + jj] = p;
+                pos[p] = jj;
+                cand = false;
+            }
+            __syncthreads();
+            best = PivT<float>{-1.f, 1 << 30};
+            const float rd = 1.f / pivrow[jj];
+            if (cand) {
+                const float l = row[jj] * rd;
+#pragma unroll
+                for (int c = jj + 1; c < PB; c++) row[c] = __fmaf_rn(-l, pivrow[c], row[c]);
+                if (jj + 1 < pb) {
+                    const float v = fabsf(row[jj + 1]);
+                    if (!isnan(v)) best = PivT<float>{v, tid};
+                }
+            }
+        }
+        if (fail) break;
+        // D^-1 by warp 0: lane r holds row r of D (original values) and of I
+        if (warp == 0) {
+            float a[PB], v[PB];
+            const float *src = M + (int64_t)(lane < pb ? perm[j0 + lane] : 0) * ld + j0;
+#pragma unroll
+            for (int k = 0; k < PB; k++) {
+                a[k] = (lane < pb && k < pb) ? src[k] : (lane == k ? 1.f : 0.f);
+                v[k] = (lane == k) ? 1.f : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < PB; k++) {
+                const float rd = 1.f / __shfl_sync(0xffffffffu, a[k], k);
+                const float f = a[k];
+                if (lane == k) {
+#pragma unroll
+                    for (int c = 0; c < PB; c++) {
+                        a[c] = a[c] * rd;
+                        v[c] = v[c] * rd;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < PB; c++) {
+                    const float pa = __shfl_sync(0xffffffffu, a[c], k);
+                    const float pvv = __shfl_sync(0xffffffffu, v[c], k);
+                    if (lane != k) {
+                        a[c] = __fmaf_rn(-f, pa, a[c]);
+                        v[c] = __fmaf_rn(-f, pvv, v[c]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < PB; c++) dblk[lane * PB + c] = v[c];
+        }
+        __syncthreads();
+        long long c_b = clock64();
+        if (tid == 0) cyc[0] += c_b - c_a;
+        // all rows and columns, 128 x 128 tiles
+        const int tx = tid & 31, ty = tid >> 5;
+        for (int tn0 = 0; tn0 < ld; tn0 += TN) {
+            // B tile: stage the pivot rows' tile, then D^-1 times it (columns
+            // outside J), D^-1 itself inside J
+            for (int idx = tid; idx < PB * TN; idx += kThreads) {
+                const int q = idx / TN, cc = idx - q * TN;
+                const int col = tn0 + cc;
+                utile[idx] = (q < pb && col < ld) ? M[(int64_t)perm[j0 + q] * ld + col] : 0.f;
+            }
+            __syncthreads();
+            {
+                const int cc = tid & (TN - 1), k0 = (tid >> 7) * 8;  // 128 columns x 4 groups of 8
+                const int col = tn0 + cc;
+                const bool inJ = col >= j0 && col < j0 + PB;
+                float b[8];
+#pragma unroll
+                for (int kk = 0; kk < 8; kk++) {
+                    const int k = k0 + kk;
+                    float acc = 0.f;
+                    if (inJ) {
+                        acc = (k < pb && col - j0 < pb) ? dblk[k * PB + (col - j0)] : 0.f;
+                    } else if (k < pb) {
+#pragma unroll 8
+                        for (int r = 0; r < PB; r++)
+                            acc = __fmaf_rn(dblk[k * PB + r], utile[r * TN + cc], acc);
+                    }
+                    b[kk] = acc;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int kk = 0; kk < 8; kk++) utile[(k0 + kk) * TN + cc] = b[kk];
+            }
+            __syncthreads();
+            const int col0 = tn0 + tx * 4;
+            const bool inJ = col0 >= j0 && col0 < j0 + PB;
+            for (int tm0 = 0; tm0 < N; tm0 += TM) {
+                const int rl = tm0 + ty * 8;
+                float acc[8][4];
+#pragma unroll
+                for (int a = 0; a < 8; a++) {
+                    const int r = rl + a;
+                    if (r < N && col0 < ld && !inJ) {
+                        load4(M + (int64_t)r * ld + col0, acc[a]);
+                    } else {
+#pragma unroll
+                        for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+                    }
+                }
+#pragma unroll 4
+                for (int q = 0; q < PB; q++) {
+                    float av[8], bv[4];
+                    load8(lt + q * mp + rl, av);
+                    load4(utile + q * TN + tx * 4, bv);
+#pragma unroll
+                    for (int a = 0; a < 8; a++)
+#pragma unroll
+                        for (int b = 0; b < 4; b++) acc[a][b] = __fmaf_rn(-av[a], bv[b], acc[a][b]);
+                }
+#pragma unroll
+                for (int a = 0; a < 8; a++) {
+                    const int r = rl + a;
+                    if (r < N && col0 < ld) {
+                        const int pr = pos[r];
+                        if (pr >= 0) load4(utile + pr * TN + tx * 4, acc[a]);
+                        store4(M + (int64_t)r * ld + col0, acc[a]);
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        if (tid < pb) pos[perm[j0 + tid]] = -2;
+        __syncthreads();
+        c_a = clock64();
+        if (tid == 0) cyc[2] += c_a - c_b;
+    }
+    __syncthreads();
+    return fail;
+}
+
+// FP32 form: x = inv(M) b with the Gauss-Jordan result X in M: bvec holds
+// b[perm[j]] on entry and x on exit; y = X * bvec (ybuf: N floats of
+// scratch), then x[j] = y[perm[j]].  Each warp takes 4 rows at a time and
+// issues all of their 16-byte loads (N <= 512: at most 4 per row and lane)
+// before the first multiply, so a sweep waits for few L2 round trips.
+__device__ __noinline__ void gje_apply(const float *M, int ld, int N, const int *perm,
+                                       float *bvec, float *ybuf) {
+    constexpr int RW = 4, CH = kThreads / 128;  // rows per warp pass, 128-column chunks
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float b[CH][4];
+#pragma unroll
+    for (int ch = 0; ch < CH; ch++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int c = ch * 128 + lane * 4 + q;
+            b[ch][q] = (c < N) ? bvec[c] : 0.f;
+        }
+    for (int i0 = warp * RW; i0 < N; i0 += kWarps * RW) {
+        float4 a[RW][CH];
+#pragma unroll
+        for (int r = 0; r < RW; r++)
+#pragma unroll
+            for (int ch = 0; ch < CH; ch++) {
+                const int c = ch * 128 + lane * 4;
+                a[r][ch] = (i0 + r < N && c < N)
+                               ? *reinterpret_cast<const float4 *>(M + (int64_t)(i0 + r) * ld + c)
+                               : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        float acc[RW];
+#pragma unroll
+        for (int r = 0; r < RW; r++) {
+            float s = 0.f;
+#pragma unroll
+            for (int ch = 0; ch < CH; ch++) {
+                s = __fmaf_rn(a[r][ch].x, b[ch][0], s);
+                s = __fmaf_rn(a[r][ch].y, b[ch][1], s);
+                s = __fmaf_rn(a[r][ch].z, b[ch][2], s);
+                s = __fmaf_rn(a[r][ch].w, b[ch][3], s);
+            }
+            acc[r] = s;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int r = 0; r < RW; r++) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+        if (lane < RW && i0 + lane < N) {
+            float v = acc[0];
+#pragma unroll
+            for (int r = 1; r < RW; r++)
+                if (lane == r) v = acc[r];
+            ybuf[i0 + lane] = v;
+        }
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < N; j += kThreads) bvec[j] = ybuf[perm[j]];
+    __syncthreads();
+}
+
 // Solve (P A) x = P b with the factors in M; b is in bvec (already permuted),
 // overwritten by x.  Forward: ascending accumulation; backward: descending
 // accumulation then one division (the oracle's order).  Used by the FP64
@@ -744,7 +1056,7 @@ __device__ __noinline__ void invert_diag_blocks(const float *M, int ld, int N, c
 #pragma unroll
             for (int k = i + 1; k < 32; k++)
                 acc = __fmaf_rn(-__shfl_sync(0xffffffffu, row[k], i), x[k], acc);
-            x[i] = acc / __shfl_sync(0xffffffffu, row[i], i);
+            x[i] = acc * (1.f / __shfl_sync(0xffffffffu, row[i], i));
         }
         float *Ui = Li + 1024;
 #pragma unroll
@@ -953,8 +1265,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     Vecs V;
     double *kk, *pw, *qr;
     const int *rptr, *s_sptr, *s_sent, *s_rent;
-    int *perm;
-    LT *bvec, *lt = nullptr, *utile = nullptr, *rowbuf = nullptr;
+    int *perm, *pos = nullptr;
+    LT *bvec, *lt = nullptr, *utile = nullptr, *rowbuf = nullptr, *dblk = nullptr;
     int vstride;
     double *vbase;
     if constexpr (kWide) {
@@ -985,6 +1297,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         lt = reinterpret_cast<LT *>(smem + L.lt);
         utile = reinterpret_cast<LT *>(smem + L.utile);
         rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
+        dblk = reinterpret_cast<LT *>(smem + L.dblk);
+        pos = reinterpret_cast<int *>(smem + L.slot);
         for (int q = tid; q < D.nnz_a; q += kThreads) w_rent[q] = ia[D.rxn_ent + q];
         for (int q = tid; q < D.nnz_h; q += kThreads) w_sent[q] = ia[D.sp_ent + q];
         for (int q = tid; q <= N; q += kThreads) w_sptr[q] = ia[D.sp_ptr + q];
@@ -1087,10 +1401,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         }
         // ---- RKF45 attempt (Simulation.cuh:692-735, kernels.cuh:68-199)
         c_mark = clock64();
-        rhs_phase1(m, V.y1, pw);
+        rhs_rates(m, V.y1, pw, qr);
         __syncthreads();
         for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species(m, s, pw);
+            const double f = rhs_species_r(m, s, pw, qr);
             if (V.fd[s] != 0.0) V.k1[s] = V.fd[s];
             else {
                 V.k1[s] = f * dt;
@@ -1098,10 +1412,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
         }
         __syncthreads();
-        rhs_phase1(m, V.u, pw);
+        rhs_rates(m, V.u, pw, qr);
         __syncthreads();
         for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species(m, s, pw);
+            const double f = rhs_species_r(m, s, pw, qr);
             if (V.fd[s] != 0.0) V.k2[s] = V.fd[s];
             else {
                 V.k2[s] = f * dt;
@@ -1109,10 +1423,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
         }
         __syncthreads();
-        rhs_phase1(m, V.u, pw);
+        rhs_rates(m, V.u, pw, qr);
         __syncthreads();
         for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species(m, s, pw);
+            const double f = rhs_species_r(m, s, pw, qr);
             if (V.fd[s] != 0.0) V.k3[s] = V.fd[s];
             else {
                 V.k3[s] = f * dt;
@@ -1121,10 +1435,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
         }
         __syncthreads();
-        rhs_phase1(m, V.u, pw);
+        rhs_rates(m, V.u, pw, qr);
         __syncthreads();
         for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species(m, s, pw);
+            const double f = rhs_species_r(m, s, pw, qr);
             if (V.fd[s] != 0.0) V.k4[s] = V.fd[s];
             else {
                 V.k4[s] = f * dt;
@@ -1133,10 +1447,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
         }
         __syncthreads();
-        rhs_phase1(m, V.u, pw);
+        rhs_rates(m, V.u, pw, qr);
         __syncthreads();
         for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species(m, s, pw);
+            const double f = rhs_species_r(m, s, pw, qr);
             if (V.fd[s] != 0.0) V.k5[s] = V.fd[s];
             else {
                 V.k5[s] = f * dt;
@@ -1146,13 +1460,13 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             }
         }
         __syncthreads();
-        rhs_phase1(m, V.u, pw);
+        rhs_rates(m, V.u, pw, qr);
         __syncthreads();
         bool ok = true;
         double dloc = INFINITY;
         bool d0nan = false;
         for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species(m, s, pw);
+            const double f = rhs_species_r(m, s, pw, qr);
             const double fdv = V.fd[s];
             double k6 = (fdv != 0.0) ? fdv : f * dt;
             V.k6[s] = k6;
@@ -1237,7 +1551,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if constexpr (kWide) {
                 if (tid == 0) st.lu_factorisations++;
                 const int rc = wide_factor<LT>(*W, m, x, dt, fresh, mdiag, smem, red, ired,
-                                               wlimit, wflag);
+                                               wlimit, wflag,
+                                               reinterpret_cast<long long *>(&st.cycles_lu_panel));
                 if (rc == 2) wide_abort = true;
                 fail = rc == 1 || rc == 2;
                 soft = rc == 3;
@@ -1247,11 +1562,13 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     mdiag[s2] = (double)M[(int64_t)s2 * ld + s2];
                 if (tid == 0) st.cycles_matrix += clock64() - c_mark;
                 if (tid == 0) st.lu_factorisations++;
-                fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
-                                     reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0;
                 if constexpr (kMixed) {
-                    if (!fail) invert_diag_blocks(M, ld, N, perm, dinv);
-                    __syncthreads();
+                    // FP32: Gauss-Jordan inverse (each solve is a matrix-vector product)
+                    fail = gje_factor(M, ld, N, perm, pos, lt, utile, dblk, rowbuf, red, ired,
+                                      reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0;
+                } else {
+                    fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
+                                         reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0;
                 }
                 soft = false;
             }
@@ -1275,10 +1592,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 if (expired) break;
             }
             // x = f(y_v); x = -(y_v - y1 - h*x)   (kernels.cuh:289-300)
-            rhs_phase1(m, yv, pw);
+            rhs_rates(m, yv, pw, qr);
             __syncthreads();
             for (int s = tid; s < N; s += kThreads) {
-                const double f = rhs_species(m, s, pw);
+                const double f = rhs_species_r(m, s, pw, qr);
                 xr[s] = -(yv[s] - V.y1[s] - dt * f);
                 if (itN == 0) xf[s] = yv[s];
             }
@@ -1326,7 +1643,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 // the FP32 normal range (species far below the others) get an
                 // FP64 diagonal correction instead, so that they keep their
                 // sign and magnitude as in the FP64 solve.
-                for (int attempt = 0; attempt < 2; attempt++) {
+                for (int attempt = 0; attempt < 3; attempt++) {
                     for (int s = tid; s < N; s += kThreads) {
                         dx[s] = 0.0;
                         res[s] = xr[s];
@@ -1353,8 +1670,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                         if constexpr (kWide) {
                             if (!wide_apply<LT>(*W, smem, wlimit, wflag)) wide_abort = true;
                         } else {
-                            lu_solve_fast(M, ld, N, perm, dinv, reinterpret_cast<float *>(bvec),
-                                          reinterpret_cast<float *>(rowbuf));
+                            gje_apply(reinterpret_cast<const float *>(M), ld, N, perm,
+                                      reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt));
                         }
                         if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
                         double cmax = 0.0, xmax = 0.0;
@@ -1403,11 +1720,13 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                     }
                     lu_rate = rate;
                     if (converged || !soft || wide_abort) break;
-                    // the reused factors (or pivots) do not converge: factor this
-                    // step's matrix (Jacobian at the step's frozen point) with
-                    // fresh pivots and solve again
+                    // the reused factors do not converge: factor this step's
+                    // matrix (Jacobian at the step's frozen point) and solve
+                    // again -- in the wide engine first with the earlier pivot
+                    // order, then with a fresh pivot search if that fails too
+                    const bool fresh = !reused;
                     reused = false;
-                    luFail = factor_at(xf, true);
+                    luFail = factor_at(xf, fresh);
                     if (luFail) break;
                 }
                 if (luFail) {
@@ -1969,53 +2288,105 @@ cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStrea
 
 // ------------------------------------------ single-evaluation kernels
 
-// dx = f(x) for a batch of parameterisations of one network; one CTA per
-// instance chunk, x/k staged through shared memory with coalesced loads.
-__global__ void __launch_bounds__(kThreads) rhs_batch_kernel(
-    int n_inst, int N, int R, int nnz_a, const int *__restrict__ rptr_g,
-    const int *__restrict__ rent, const int *__restrict__ sptr, const int *__restrict__ sent,
-    const double *__restrict__ k, const double *__restrict__ x, double *__restrict__ dx) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    double *xs = reinterpret_cast<double *>(smem);
-    double *kk = xs + N;
-    double *pw = kk + R;
-    int *rptr = reinterpret_cast<int *>(pw + (nnz_a > 0 ? nnz_a : 1));
-    for (int j = threadIdx.x; j <= R; j += kThreads) rptr[j] = rptr_g[j];
-    Net m;
-    m.n = N;
-    m.r = R;
-    m.nnz_a = nnz_a;
-    m.rent = rent;
-    m.sptr = sptr;
-    m.sent = sent;
-    m.rptr = rptr;
-    m.kk = kk;
-    for (int b = blockIdx.x; b < n_inst; b += gridDim.x) {
-        __syncthreads();
-        const double *xb = x + (int64_t)b * N;
-        const double *kb = k + (int64_t)b * R;
-        for (int s = threadIdx.x; s < N; s += kThreads) xs[s] = xb[s];
-        for (int j = threadIdx.x; j < R; j += kThreads) kk[j] = kb[j];
-        __syncthreads();
-        rhs_phase1(m, xs, pw);
-        __syncthreads();
-        double *db = dx + (int64_t)b * N;
-        for (int s = threadIdx.x; s < N; s += kThreads) db[s] = rhs_species(m, s, pw);
+// dx = f(x) for a batch of parameterisations of one network: one warp per
+// instance (no CTA barrier on the data path).  The network structure is
+// staged once per CTA; each warp copies its instance's x and k into its own
+// shared-memory slice with 16-byte loads, forms the reactant powers, then the
+// species sums in the oracle's order (rhs_species), and stores dx coalesced.
+constexpr int kRhsThreads = 256;
+constexpr int kRhsWarps = kRhsThreads / 32;
+
+__device__ __forceinline__ void warp_copy_f64(double *dst, const double *src, int n) {
+    const int lane = threadIdx.x & 31;
+    if ((((uintptr_t)src) & 15) == 0 && (n & 1) == 0) {
+        const double2 *s2 = reinterpret_cast<const double2 *>(src);
+        double2 *d2 = reinterpret_cast<double2 *>(dst);
+        for (int i = lane; i < n / 2; i += 32) d2[i] = __ldcs(s2 + i);
+    } else {
+        for (int i = lane; i < n; i += 32) dst[i] = __ldcs(src + i);
     }
 }
 
-cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, const int *rptr,
+__global__ void __launch_bounds__(kRhsThreads) rhs_batch_kernel(
+    int n_inst, int N, int R, int nnz_a, int nnz_h, const int *__restrict__ rptr_g,
+    const int *__restrict__ rent_g, const int *__restrict__ sptr_g, const int *__restrict__ sent_g,
+    const double *__restrict__ k, const double *__restrict__ x, double *__restrict__ dx) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    int *rptr = reinterpret_cast<int *>(smem);
+    int *sptr = rptr + (R + 1);
+    int *rent = sptr + (N + 1);
+    int *sent = rent + (nnz_a > 0 ? nnz_a : 1);
+    const int64_t ints = (int64_t)(R + 1) + (N + 1) + (nnz_a > 0 ? nnz_a : 1) + (nnz_h > 0 ? nnz_h : 1);
+    double *wbase = reinterpret_cast<double *>(smem + ((ints * 4 + 15) & ~int64_t(15)));
+    const int per_warp = ((N + 1) & ~1) + 2 * ((R + 1) & ~1) + ((nnz_a + 1) & ~1);
+    for (int j = threadIdx.x; j <= R; j += kRhsThreads) rptr[j] = rptr_g[j];
+    for (int j = threadIdx.x; j <= N; j += kRhsThreads) sptr[j] = sptr_g[j];
+    for (int j = threadIdx.x; j < nnz_a; j += kRhsThreads) rent[j] = rent_g[j];
+    for (int j = threadIdx.x; j < nnz_h; j += kRhsThreads) sent[j] = sent_g[j];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double *xs = wbase + (int64_t)warp * per_warp;
+    double *kk = xs + ((N + 1) & ~1);
+    double *rate = kk + ((R + 1) & ~1);
+    double *pw = rate + ((R + 1) & ~1);
+    for (int b = blockIdx.x * kRhsWarps + warp; b < n_inst; b += gridDim.x * kRhsWarps) {
+        warp_copy_f64(xs, x + (int64_t)b * N, N);
+        warp_copy_f64(kk, k + (int64_t)b * R, R);
+        __syncwarp();
+        // reaction products once per reaction (rhs_rates), then the species
+        // sums (rhs_species_r): bit-identical to the per-entry products
+        for (int y = lane; y < R; y += 32) {
+            double r = kk[y];
+            for (int q = rptr[y]; q < rptr[y + 1]; q++) {
+                const int e = rent[q];
+                const double p = mypow(xs[ent_index(e)], ent_coef(e));
+                pw[q] = p;
+                r = r * p;
+            }
+            rate[y] = r;
+        }
+        __syncwarp();
+        double *db = dx + (int64_t)b * N;
+        for (int s = lane; s < N; s += 32) {
+            double acc = 0.0;
+            for (int e = sptr[s]; e < sptr[s + 1]; e++) {
+                const int ent = sent[e];
+                const int y = ent_index(ent), c = ent_coef(ent);
+                double v;
+                if (c == 1) v = rate[y];
+                else if (c == -1) v = -rate[y];
+                else {
+                    v = (double)c * kk[y];
+                    for (int q = rptr[y]; q < rptr[y + 1]; q++) v = v * pw[q];
+                }
+                acc = acc + v;
+            }
+            __stcs(db + s, acc);
+        }
+        __syncwarp();
+    }
+}
+
+cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, int nnz_h, const int *rptr,
                              const int *rent, const int *sptr, const int *sent,
                              const double *k, const double *x, double *dx, int sm_count,
                              cudaStream_t stream) {
-    const int64_t smem = int64_t(N + R + (nnz_a > 0 ? nnz_a : 1)) * 8 + int64_t(R + 1) * 4;
+    const int64_t ints = (int64_t)(R + 1) + (N + 1) + (nnz_a > 0 ? nnz_a : 1) + (nnz_h > 0 ? nnz_h : 1);
+    const int64_t per_warp = ((N + 1) & ~1) + 2 * ((R + 1) & ~1) + ((nnz_a + 1) & ~1);
+    const int64_t smem = ((ints * 4 + 15) & ~int64_t(15)) + per_warp * 8 * kRhsWarps;
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(rhs_batch_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int grid = n_inst < sm_count * 4 ? n_inst : sm_count * 4;
-    rhs_batch_kernel<<<grid, kThreads, smem, stream>>>(n_inst, N, R, nnz_a, rptr, rent, sptr,
-                                                       sent, k, x, dx);
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rhs_batch_kernel, kRhsThreads,
+                                                      (size_t)smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const int64_t want = ((int64_t)n_inst + kRhsWarps - 1) / kRhsWarps;
+    const int grid = (int)std::min<int64_t>(want, (int64_t)sm_count * per_sm);
+    rhs_batch_kernel<<<grid, kRhsThreads, smem, stream>>>(n_inst, N, R, nnz_a, nnz_h, rptr, rent,
+                                                          sptr, sent, k, x, dx);
     return cudaGetLastError();
 }
 

@@ -113,7 +113,7 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
 // Dynamic shared memory of the wide kernel: the rank-update tiles, or the
 // matrix-vector input, whichever is larger, plus the pivot-block inverse.
 __host__ __device__ inline int64_t wide_smem_bytes(int N, int lt) {
-    const int64_t tiles = int64_t(2) * kWT * kWPB * lt;
+    const int64_t tiles = (int64_t(kWPB) * (kWT + 4) + int64_t(kWPB) * kWT) * lt;
     const int64_t vin = int64_t((N + 3) & ~3) * lt;
     return (tiles > vin ? tiles : vin) + int64_t(kWPB) * kWPB * lt;
 }
@@ -240,8 +240,9 @@ __device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD) {
 // their new values (PR, D^-1) directly.
 template <typename LT>
 __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
-    LT *sAJ = smem;                       // [kWT][kWPB]
-    LT *sB = smem + kWT * kWPB;           // [kWPB][kWT]
+    constexpr int AS = kWT + 4;           // sAJ row stride (16-byte rows)
+    LT *sAJ = smem;                       // [kWPB][AS]: panel columns, column-major
+    LT *sB = smem + kWPB * AS;            // [kWPB][kWT]
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const int N = W.N, ld = W.ld;
     const int nrt = (N + kWT - 1) / kWT, nct = (ld + kWT - 1) / kWT;
@@ -250,7 +251,7 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
         __syncthreads();
         for (int q = tid; q < kWT * kWPB; q += kThreads) {
             const int r = q / kWPB, k = q - r * kWPB;
-            sAJ[q] = (r0 + r < N) ? W.AJ[(int64_t)(r0 + r) * kWPB + k] : LT(0);
+            sAJ[k * AS + r] = (r0 + r < N) ? W.AJ[(int64_t)(r0 + r) * kWPB + k] : LT(0);
         }
         for (int q = tid; q < kWPB * kWT; q += kThreads) {
             const int k = q / kWT, cc = q - k * kWT;
@@ -266,30 +267,35 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
         const int col = c0 + tx * 4;
         if (col >= ld) continue;
         const bool inJ = col >= j0 && col < j0 + kWPB;
+        const int rl0 = ty * 8;
+        LT acc[8][4];
+#pragma unroll
         for (int a = 0; a < 8; a++) {
-            const int rl = ty * 8 + a, row = r0 + rl;
-            if (row >= N) break;
-            LT *dst = W.A + (int64_t)row * ld + col;
-            LT acc[4];
-            const int pr = W.pos[row];
-            if (pr >= 0) {
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[b] = sB[pr * kWT + tx * 4 + b];
+            const int row = r0 + rl0 + a;
+            if (row < N && !inJ) {
+                load4(W.A + (int64_t)row * ld + col, acc[a]);
             } else {
-                if (inJ) {
 #pragma unroll
-                    for (int b = 0; b < 4; b++) acc[b] = LT(0);
-                } else {
-                    load4(dst, acc);
-                }
-#pragma unroll 8
-                for (int k = 0; k < kWPB; k++) {
-                    const LT l = sAJ[rl * kWPB + k];
-#pragma unroll
-                    for (int b = 0; b < 4; b++) acc[b] = lt_fma(-l, sB[k * kWT + tx * 4 + b], acc[b]);
-                }
+                for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
             }
-            store4(dst, acc);
+        }
+#pragma unroll 4
+        for (int k = 0; k < kWPB; k++) {
+            LT av[8], bv[4];
+            load8(sAJ + k * AS + rl0, av);
+            load4(sB + k * kWT + tx * 4, bv);
+#pragma unroll
+            for (int a = 0; a < 8; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = lt_fma(-av[a], bv[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            const int row = r0 + rl0 + a;
+            if (row >= N) break;
+            const int pr = W.pos[row];
+            if (pr >= 0) load4(sB + pr * kWT + tx * 4, acc[a]);
+            store4(W.A + (int64_t)row * ld + col, acc[a]);
         }
     }
 }
@@ -411,12 +417,13 @@ __device__ bool wide_pivot_block(const WideWs<LT> &W, int j0, int pb, int *sflag
         for (int k = 0; k < kWPB; k++) {
             const LT d = __shfl_sync(0xffffffffu, a[k], k);
             ok = ok && d != LT(0) && isfinite(d);
+            const LT rd = LT(1) / d;
             const LT f = a[k];
             if (lane == k) {
 #pragma unroll
                 for (int c = 0; c < kWPB; c++) {
-                    a[c] = a[c] / d;
-                    v[c] = v[c] / d;
+                    a[c] = a[c] * rd;
+                    v[c] = v[c] * rd;
                 }
             }
 #pragma unroll
@@ -496,10 +503,10 @@ __device__ bool wide_select_pivots(const WideWs<LT> &W, int j0, int pb, double *
             W.piv[j0 + k] = p;
             W.used[p] = 1;
         }
-        const LT d = prow[k];
+        const LT rd = LT(1) / prow[k];
         for (int i = tid; i < N; i += kThreads) {
             if (W.used[i] || i == p) continue;
-            const LT l = W.PN[(int64_t)k * N + i] / d;
+            const LT l = W.PN[(int64_t)k * N + i] * rd;
             for (int c = k + 1; c < pb; c++)
                 W.PN[(int64_t)c * N + i] = lt_fma(-l, prow[c], W.PN[(int64_t)c * N + i]);
         }
@@ -512,18 +519,28 @@ __device__ bool wide_select_pivots(const WideWs<LT> &W, int j0, int pb, double *
 // Returns 0 (fresh pivots), 3 (the last fresh factorisation's pivot order,
 // when `fresh` is false and it still gives finite, moderately conditioned
 // pivot blocks), 1 (a zero pivot column: singular), 2 (a wait ran out).
+// cyc (thread 0): [0] += leader-only work (pivot searches, pivot-block
+// inverses), [1] += panel-product tasks, [2] += assembly and rank-update tasks
+// (each from fork to join).
 template <typename LT>
 __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, double h,
                            bool fresh, double *mdiag, unsigned char *smem, double *red,
-                           int *ired, uint64_t limit, int *sflag) {
+                           int *ired, uint64_t limit, int *sflag, long long *cyc) {
     const int tid = threadIdx.x, N = W.N;
     LT *sm = reinterpret_cast<LT *>(smem);
     LT *sD = sm + wide_smem_bytes(N, (int)sizeof(LT)) / (int)sizeof(LT) - kWPB * kWPB;
     bool use_old = !fresh && ld_acquire_i(W.flags) != 0;
+    long long c0 = clock64(), c1;
+    auto tick = [&](int slot) {
+        c1 = clock64();
+        if (tid == 0) cyc[slot] += c1 - c0;
+        c0 = c1;
+    };
     for (int attempt = 0; attempt < 2; attempt++) {
         wide_fork<LT>(W, kTaskAssemble, 0, 0, h, x);
         task_assemble<LT>(W, m, x, h, mdiag);
         if (!wide_join<LT>(W, limit, sflag)) return 2;
+        tick(2);
         for (int i = tid; i < N; i += kThreads) {
             W.pos[i] = -1;
             if (!use_old) W.used[i] = 0;
@@ -538,6 +555,7 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
                 return 1;
             }
             __syncthreads();
+            tick(0);
             if (j0 > 0 && tid < kWPB) W.pos[W.piv[j0 - kWPB + tid]] = -1;
             __syncthreads();
             if (tid < pb) W.pos[W.piv[j0 + tid]] = tid;
@@ -545,12 +563,15 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
                 ok = false;
                 break;
             }
+            tick(0);
             wide_fork<LT>(W, kTaskPanel, j0, pb, h, x);
             task_panel<LT>(W, j0, pb, sD);
             if (!wide_join<LT>(W, limit, sflag)) return 2;
+            tick(1);
             wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
             task_update<LT>(W, j0, pb, sm);
             if (!wide_join<LT>(W, limit, sflag)) return 2;
+            tick(2);
         }
         if (ok) {
             if (tid == 0) W.flags[0] = 1;
