@@ -130,7 +130,9 @@ def load_traffic():
 
 def lu_flops(stats, models, engine):
     """Algorithmic FLOPs of the dense linear algebra the integration did:
-    (2/3)N^3 per factorisation + 2N^2 per triangular-solve pair."""
+    (2/3)N^3 per factorisation + 2N^2 per solve (an LU's triangular-solve
+    pair).  The mixed form's Gauss-Jordan inverse does 2N^3 per
+    factorisation; the roofline counts the LU's algorithmic figure."""
     tot = 0.0
     for s, m in zip(stats, models):
         n = float(m.n_species)

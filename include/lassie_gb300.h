@@ -71,7 +71,7 @@ typedef struct {
     int32_t lu_reuse;     /* mixed form: 1 (default) lets a backward-Euler step
                              precondition its refinement with the FP32 factors
                              of an earlier step of the same step size while they
-                             contract the residual by 1e-3 or better per sweep
+                             contract the residual by 2e-3 or better per sweep
                              (the refinement still converges to the FP64 solve of
                              the current matrix); 0 factors at every step */
 } lassie_opts;

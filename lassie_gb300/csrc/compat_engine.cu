@@ -676,6 +676,62 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
     return fail;
 }
 
+// Inverse of a 32 x 32 block by the whole CTA: Gauss-Jordan without pivoting
+// (the rows arrive in pivot order) on [D | I].  Thread t owns row t / 16 and
+// four of the 64 columns in registers; per pivot the pivot value, the scaled
+// pivot row and the pivot column pass through shared memory (two buffers,
+// alternating), two barriers per pivot.  D is read from Dsrc[r * ds + c]
+// (rows/columns at or past nb are the identity), the inverse goes to
+// Dinv[r * 32 + c].  xs: 2 * 97 T of scratch.  Returns false (uniformly) if
+// a pivot is zero or not finite, or the inverse is not finite.
+template <typename T>
+__device__ bool cta_block_inverse(const T *Dsrc, int ds, int nb, T *Dinv, T *xs) {
+    static_assert(kThreads == 512, "one thread per 4 of the 32 x 64 entries");
+    const int t = threadIdx.x, r = t >> 4, c0 = (t & 15) * 4;
+    T v[4];
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+        const int c = c0 + b;
+        if (c < 32) v[b] = (r < nb && c < nb) ? Dsrc[r * ds + c] : (r == c ? T(1) : T(0));
+        else v[b] = (c - 32 == r) ? T(1) : T(0);
+    }
+    bool ok = true;
+    for (int k = 0; k < 32; k++) {
+        T *P = xs + (k & 1) * 97, *F = P + 64, *dd = P + 96;
+        const int own = k - c0;
+        if (own >= 0 && own < 4) {
+            const T x = own == 0 ? v[0] : own == 1 ? v[1] : own == 2 ? v[2] : v[3];
+            F[r] = x;
+            if (r == k) *dd = x;
+        }
+        __syncthreads();
+        const T d = *dd;
+        ok = ok && d != T(0) && isfinite(d);
+        if (r == k) {
+            const T rd = T(1) / d;
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                v[b] = v[b] * rd;
+                P[c0 + b] = v[b];
+            }
+        }
+        __syncthreads();
+        if (r != k) {
+            const T f = F[r];
+#pragma unroll
+            for (int b = 0; b < 4; b++) v[b] = lt_fma(-f, P[c0 + b], v[b]);
+        }
+    }
+    if (c0 >= 32) {
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            ok = ok && isfinite(v[b]);
+            Dinv[r * 32 + (c0 - 32) + b] = v[b];
+        }
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
 // FP32 form: in-place Gauss-Jordan inverse of M (row-major, N <= kThreads)
 // with partial pivoting by rows, in kPB-column panels J:
 //   pivot rows P_J: per column, the largest |value| among the rows that are
@@ -770,40 +826,14 @@ __device__ __noinline__ int gje_factor(float *M, int ld, int N, int *perm, int *
             }
         }
         if (fail) break;
-        // D^-1 by warp 0: lane r holds row r of D (original values) and of I
-        if (warp == 0) {
-            float a[PB], v[PB];
-            const float *src = M + (int64_t)(lane < pb ? perm[j0 + lane] : 0) * ld + j0;
-#pragma unroll
-            for (int k = 0; k < PB; k++) {
-                a[k] = (lane < pb && k < pb) ? src[k] : (lane == k ? 1.f : 0.f);
-                v[k] = (lane == k) ? 1.f : 0.f;
-            }
-#pragma unroll
-            for (int k = 0; k < PB; k++) {
-                const float rd = 1.f / __shfl_sync(0xffffffffu, a[k], k);
-                const float f = a[k];
-                if (lane == k) {
-#pragma unroll
-                    for (int c = 0; c < PB; c++) {
-                        a[c] = a[c] * rd;
-                        v[c] = v[c] * rd;
-                    }
-                }
-#pragma unroll
-                for (int c = 0; c < PB; c++) {
-                    const float pa = __shfl_sync(0xffffffffu, a[c], k);
-                    const float pvv = __shfl_sync(0xffffffffu, v[c], k);
-                    if (lane != k) {
-                        a[c] = __fmaf_rn(-f, pa, a[c]);
-                        v[c] = __fmaf_rn(-f, pvv, v[c]);
-                    }
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < PB; c++) dblk[lane * PB + c] = v[c];
+        // D^-1 (D = M[P_J, J] with its original values) by the whole CTA; the
+        // pivot rows' panel values are staged in utile, free until the B tiles
+        for (int q = tid; q < PB * PB; q += kThreads) {
+            const int r = q / PB, c = q - r * PB;
+            utile[r * PB + c] = (r < pb && c < pb) ? M[(int64_t)perm[j0 + r] * ld + j0 + c] : 0.f;
         }
         __syncthreads();
+        cta_block_inverse<float>(utile, PB, pb, dblk, utile + PB * PB);
         long long c_b = clock64();
         if (tid == 0) cyc[0] += c_b - c_a;
         // all rows and columns, 128 x 128 tiles

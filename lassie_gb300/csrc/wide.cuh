@@ -19,8 +19,8 @@
 //     x[j] = (X * r[p])[p_j]:   one dense matrix-vector product,
 // where the LU's two triangular solves would be 2N/32 dependent block steps.
 // Pivot rows of the last fresh factorisation are reused (no pivot search)
-// while the pivot blocks stay well conditioned; the integrator's refinement
-// checks every solve and asks for fresh pivots when one does not converge.
+// while the pivot blocks stay invertible; the integrator's refinement checks
+// every solve and asks for fresh pivots when one does not converge.
 #pragma once
 
 constexpr int kWPB = 32;   // Gauss-Jordan panel width
@@ -204,8 +204,9 @@ __device__ void task_assemble(const WideWs<LT> &W, const Net &m, const double *x
     }
 }
 
-// PR = D^-1 * M[P_J, :] (columns spread over all threads of the grid) and the
-// snapshot AJ = M[:, J] (rows likewise).
+// PR = D^-1 * M[P_J, :] and the snapshot AJ = M[:, J], spread over every
+// thread of the grid: PR by (group of 4 pivot rows, column), AJ by (row,
+// 4 panel columns).
 template <typename LT>
 __device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD) {
     const int tid = threadIdx.x;
@@ -213,24 +214,32 @@ __device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD) {
     __syncthreads();
     const int N = W.N, ld = W.ld;
     const int gt = blockIdx.x * kThreads + tid, nt = gridDim.x * kThreads;
-    for (int c = gt; c < ld; c += nt) {
+    for (int q = gt; q < (kWPB / 4) * ld; q += nt) {
+        const int g = q / ld, c = q - g * ld;
         if (c >= j0 && c < j0 + kWPB) continue;
         LT a[kWPB];
 #pragma unroll
         for (int k = 0; k < kWPB; k++) a[k] = (k < pb) ? W.A[(int64_t)W.piv[j0 + k] * ld + c] : LT(0);
-#pragma unroll 4
-        for (int r = 0; r < kWPB; r++) {
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) {
+            const int r = g * 4 + rr;
             LT acc = LT(0);
 #pragma unroll
             for (int k = 0; k < kWPB; k++) acc = lt_fma(sD[r * kWPB + k], a[k], acc);
             W.PR[(int64_t)r * ld + c] = acc;
         }
     }
-    for (int i = gt; i < N; i += nt) {
-        const LT *src = W.A + (int64_t)i * ld + j0;
-        LT *dst = W.AJ + (int64_t)i * kWPB;
+    for (int q = gt; q < N * (kWPB / 4); q += nt) {
+        const int i = q / (kWPB / 4), k4 = (q - i * (kWPB / 4)) * 4;
+        const LT *src = W.A + (int64_t)i * ld + j0 + k4;
+        LT v[4];
+        if (k4 + 4 <= pb) {
+            load4(src, v);
+        } else {
 #pragma unroll
-        for (int k = 0; k < kWPB; k++) dst[k] = (k < pb) ? src[k] : LT(0);
+            for (int b = 0; b < 4; b++) v[b] = (k4 + b < pb) ? src[b] : LT(0);
+        }
+        store4(W.AJ + (int64_t)i * kWPB + k4, v);
     }
 }
 
@@ -393,65 +402,17 @@ __device__ bool wide_join(const WideWs<LT> &W, uint64_t limit, int *sflag) {
     return *sflag != 0;
 }
 
-// Leader: inverse of the pivot block D = A[piv[j0+r]][j0+k] by warp 0
-// (Gauss-Jordan without further pivoting: the rows are in pivot order), into
-// W.Dinv; false if a pivot is zero or the inverse is not finite, or, with
-// check_growth (pivot rows of an earlier factorisation), if
-// max|D| * max|D^-1| exceeds 1e6.
+// Leader: inverse of the pivot block D = A[piv[j0+r]][j0+k] into W.Dinv by
+// the whole leader CTA (cta_block_inverse; scratch: 32 * 32 + 194 LT); false
+// if a pivot is zero or the inverse is not finite.
 template <typename LT>
-__device__ bool wide_pivot_block(const WideWs<LT> &W, int j0, int pb, int *sflag, bool check_growth) {
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        LT a[kWPB], v[kWPB];
-        const LT *src = W.A + (int64_t)(lane < pb ? W.piv[j0 + lane] : 0) * W.ld + j0;
-#pragma unroll
-        for (int k = 0; k < kWPB; k++) {
-            a[k] = (lane < pb && k < pb) ? src[k] : (lane == k ? LT(1) : LT(0));
-            v[k] = (lane == k) ? LT(1) : LT(0);
-        }
-        bool ok = true;
-        LT amax = LT(0), vmax = LT(0);
-#pragma unroll
-        for (int k = 0; k < kWPB; k++) amax = fmax(amax, fabs(a[k]));
-#pragma unroll
-        for (int k = 0; k < kWPB; k++) {
-            const LT d = __shfl_sync(0xffffffffu, a[k], k);
-            ok = ok && d != LT(0) && isfinite(d);
-            const LT rd = LT(1) / d;
-            const LT f = a[k];
-            if (lane == k) {
-#pragma unroll
-                for (int c = 0; c < kWPB; c++) {
-                    a[c] = a[c] * rd;
-                    v[c] = v[c] * rd;
-                }
-            }
-#pragma unroll
-            for (int c = 0; c < kWPB; c++) {
-                const LT pa = __shfl_sync(0xffffffffu, a[c], k);
-                const LT pv = __shfl_sync(0xffffffffu, v[c], k);
-                if (lane != k) {
-                    a[c] = lt_fma(-f, pa, a[c]);
-                    v[c] = lt_fma(-f, pv, v[c]);
-                }
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < kWPB; c++) {
-            ok = ok && isfinite(v[c]);
-            vmax = fmax(vmax, fabs(v[c]));
-            W.Dinv[lane * kWPB + c] = v[c];
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-            vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-        }
-        if (check_growth && !(amax * vmax <= LT(1e6))) ok = false;
-        ok = __all_sync(0xffffffffu, ok);
-        if (lane == 0) *sflag = ok ? 1 : 0;
+__device__ bool wide_pivot_block(const WideWs<LT> &W, int j0, int pb, LT *scratch) {
+    for (int q = threadIdx.x; q < kWPB * kWPB; q += kThreads) {
+        const int r = q / kWPB, c = q - r * kWPB;
+        scratch[q] = (r < pb && c < pb) ? W.A[(int64_t)W.piv[j0 + r] * W.ld + j0 + c] : LT(0);
     }
     __syncthreads();
-    return *sflag != 0;
+    return cta_block_inverse<LT>(scratch, kWPB, pb, W.Dinv, scratch + kWPB * kWPB);
 }
 
 // Leader: partial-pivoting choice of the panel's pivot rows among the rows
@@ -517,8 +478,8 @@ __device__ bool wide_select_pivots(const WideWs<LT> &W, int j0, int pb, double *
 
 // Leader: assemble M = I - h*J(x) on all CTAs and invert it in place.
 // Returns 0 (fresh pivots), 3 (the last fresh factorisation's pivot order,
-// when `fresh` is false and it still gives finite, moderately conditioned
-// pivot blocks), 1 (a zero pivot column: singular), 2 (a wait ran out).
+// when `fresh` is false and it still gives invertible pivot blocks),
+// 1 (a zero pivot column: singular), 2 (a wait ran out).
 // cyc (thread 0): [0] += leader-only work (pivot searches, pivot-block
 // inverses), [1] += panel-product tasks, [2] += assembly and rank-update tasks
 // (each from fork to join).
@@ -559,7 +520,7 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
             if (j0 > 0 && tid < kWPB) W.pos[W.piv[j0 - kWPB + tid]] = -1;
             __syncthreads();
             if (tid < pb) W.pos[W.piv[j0 + tid]] = tid;
-            if (!wide_pivot_block<LT>(W, j0, pb, sflag, use_old)) {
+            if (!wide_pivot_block<LT>(W, j0, pb, sm)) {
                 ok = false;
                 break;
             }
