@@ -74,6 +74,12 @@ typedef struct {
                              contract the residual by 2e-3 or better per sweep
                              (the refinement still converges to the FP64 solve of
                              the current matrix); 0 factors at every step */
+    int32_t tensor_cores; /* wide engine (networks above 512 species), mixed
+                             form: 1 runs the rank-32 updates of the
+                             factorisation on the tensor cores (tcgen05, TF32
+                             products of split operands), 0 (default) on the
+                             FP32 pipes */
+    int32_t pad;
 } lassie_opts;
 
 #define LASSIE_ROOT_POW 0
@@ -197,6 +203,15 @@ int lassie_adjoint_batch(const lassie_instance *inst, int32_t n, const double *c
                          const lassie_opts *opts, int32_t ckpt_every, int32_t max_record,
                          double *loss, double *const *grad_logk, double *const *grad_x0,
                          lassie_stats *stats);
+
+/* Self-test of the tensor-core (tcgen05) tile product used by the wide
+   engine's rank-32 updates (no reference counterpart): on device buffers,
+   D[128 x 128] = A[128 x 32] * B[32 x 128], row-major FP32, computed as three
+   TF32 products of the operands split into TF32 high and low parts; status[0]
+   becomes 1, or 2 if the tensor core did not complete.  Launches one CTA on
+   `stream`. */
+int lassie_tc_selftest(const float *d_a, const float *d_b, float *d_d, int *d_status,
+                       void *stream);
 
 /* One integration that allocates no device memory (no counterpart in the
    reference, which allocates in every solve).  For callers that cannot call

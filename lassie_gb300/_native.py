@@ -31,7 +31,7 @@ EXPORTS = (
     "lassie_model_info", "lassie_solve", "lassie_solve_batch", "lassie_batch_create",
     "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
     "lassie_batch_bytes", "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
-    "lassie_lu_solve", "lassie_adjoint_batch", "lassie_solve_noalloc",
+    "lassie_lu_solve", "lassie_adjoint_batch", "lassie_solve_noalloc", "lassie_tc_selftest",
 )
 
 
@@ -40,7 +40,8 @@ class Opts(C.Structure):
                 ("newton_tol", C.c_double), ("stiffness_tol", C.c_double),
                 ("newton_iter", C.c_int64), ("max_steps", C.c_int64),
                 ("deadline_s", C.c_double), ("precision", C.c_int32),
-                ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("lu_reuse", C.c_int32)]
+                ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("lu_reuse", C.c_int32),
+                ("tensor_cores", C.c_int32), ("pad", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -126,6 +127,7 @@ def load():
         L.lassie_adjoint_batch.argtypes = [vp, i32, vp, C.POINTER(Opts), i32, i32, vp, vp, vp, vp]
         L.lassie_solve_noalloc.argtypes = [vp, vp, vp, vp, i32, C.POINTER(Opts), vp,
                                            C.POINTER(Stats), vp]
+        L.lassie_tc_selftest.argtypes = [vp, vp, vp, vp, vp]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int and name not in ("lassie_device_ok",):

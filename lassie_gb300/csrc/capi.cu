@@ -272,6 +272,8 @@ extern "C" void lassie_opts_default(lassie_opts *o) {
     o->refine_max = 0;
     o->quarter_root = LASSIE_ROOT_POW;
     o->lu_reuse = 1;
+    o->tensor_cores = 0;
+    o->pad = 0;
 }
 
 extern "C" const char *lassie_status_string(int s) {
@@ -565,6 +567,7 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     P.precision = o.precision;
     P.refine_max = o.refine_max;
     P.lu_reuse = o.lu_reuse;
+    P.tensor_cores = o.tensor_cores;
     P.deadline_ns = o.deadline_s > 0 ? (uint64_t)(o.deadline_s * 1e9) : 0;
     *out = b;
     return LASSIE_OK;

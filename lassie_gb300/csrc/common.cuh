@@ -88,7 +88,7 @@ struct LaunchParams {
     unsigned char *workspace;  // per-CTA Newton matrix
     int64_t ws_stride;         // bytes per CTA
     int32_t nmax, rmax, amax, hmax;  // largest N, R, nnz_A, nnz_H in the batch
-    int32_t precision, refine_max, lu_reuse, pad_;
+    int32_t precision, refine_max, lu_reuse, tensor_cores;
     uint64_t deadline_ns;      // per-launch wall-clock limit (ns), 0 = none
     AdjArrays adj;             // adj.desc == nullptr: no recording
 };

@@ -95,6 +95,14 @@ __device__ double block_max(double v, double *red) {
     return __longlong_as_double(__shfl_sync(0xffffffffu, s, 0));
 }
 
+// |v| as an IEEE bit pattern, NaN as 0: running maxima of these integers
+// equal fmax(acc, fabs(v)) (which ignores a NaN operand) without FP64
+// instructions, the slow pipe on this GPU.
+__device__ __forceinline__ long long absbits_nonan(double v) {
+    const long long b = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+    return b > 0x7ff0000000000000LL ? 0 : b;
+}
+
 // Block max of two non-negative values at once (same rules as block_max).
 __device__ void block_max2(double &a, double &b, double *red) {
     long long x = __double_as_longlong(fabs(a)), y = __double_as_longlong(fabs(b));
@@ -922,7 +930,7 @@ __device__ __noinline__ int gje_factor(float *M, int ld, int N, int *perm, int *
 // issues all of their 16-byte loads (N <= 512: at most 4 per row and lane)
 // before the first multiply, so a sweep waits for few L2 round trips.
 __device__ __noinline__ void gje_apply(const float *M, int ld, int N, const int *perm,
-                                       float *bvec, float *ybuf) {
+                                       float *bvec, float *ybuf, bool gather = true) {
     constexpr int RW = 4, CH = kThreads / 128;  // rows per warp pass, 128-column chunks
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float b[CH][4];
@@ -970,6 +978,7 @@ __device__ __noinline__ void gje_apply(const float *M, int ld, int N, const int 
         }
     }
     __syncthreads();
+    if (!gather) return;  // the caller reads x[j] = ybuf[perm[j]] itself
     for (int j = threadIdx.x; j < N; j += kThreads) bvec[j] = ybuf[perm[j]];
     __syncthreads();
 }
@@ -1264,6 +1273,7 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
     }
 }
 
+#include "tc.cuh"
 #include "wide.cuh"
 
 // ----------------------------------------------------------- integrator
@@ -1678,9 +1688,9 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                         dx[s] = 0.0;
                         res[s] = xr[s];
                     }
-                    double rloc = 0.0;
-                    for (int s = tid; s < N; s += kThreads) rloc = fmax(rloc, fabs(res[s]));
-                    double rmax = block_max(rloc, red);
+                    long long rlb = 0;
+                    for (int s = tid; s < N; s += kThreads) rlb = max(rlb, absbits_nonan(res[s]));
+                    double rmax = block_max(__longlong_as_double(rlb), red);
                     double prev = INFINITY, rate = 0.0;
                     bool converged = false;
                     for (int sweep = 0; sweep < refine_max; sweep++) {
@@ -1693,6 +1703,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                         const bool finite = isfinite(rmax);
                         const int e = finite ? ilogb(rmax) : 0;
                         const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
+                        // |res| * sc < 2^-126  <=>  |res| < 2^(e-126): bit-pattern bound
+                        const int le = e - 126;
+                        const long long lost_lim =
+                            le >= -1022 ? (long long)(le + 1023) << 52
+                                        : (le >= -1074 ? 1LL << (le + 1074) : 0LL);
                         for (int s = tid; s < N; s += kThreads)
                             bvec[s] = (LT)(res[perm[s]] * sc);
                         __syncthreads();
@@ -1701,24 +1716,30 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                             if (!wide_apply<LT>(*W, smem, wlimit, wflag)) wide_abort = true;
                         } else {
                             gje_apply(reinterpret_cast<const float *>(M), ld, N, perm,
-                                      reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt));
+                                      reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt),
+                                      false);
                         }
                         if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
-                        double cmax = 0.0, xmax = 0.0;
+                        long long cmb = 0, xmb = 0;
                         for (int s = tid; s < N; s += kThreads) {
-                            double c = (double)bvec[s] * isc;
+                            double c;
+                            if constexpr (kWide) c = (double)bvec[s] * isc;
+                            else c = (double)reinterpret_cast<const float *>(lt)[perm[s]] * isc;
                             // the part of this row's right-hand side that the
                             // FP32 cast lost (below the FP32 normal range),
                             // applied through the diagonal
-                            const double rs = res[s] * sc;
-                            if (fabs(rs) < 0x1p-126 && fabs(mdiag[s]) >= 0.5)
-                                c += (rs - (double)(float)rs) * isc / mdiag[s];
+                            if ((__double_as_longlong(res[s]) & 0x7fffffffffffffffLL) < lost_lim) {
+                                const double rs = res[s] * sc;
+                                if (fabs(mdiag[s]) >= 0.5)
+                                    c += (rs - (double)(float)rs) * isc / mdiag[s];
+                            }
                             const double nx = dx[s] + c;
                             dx[s] = nx;
-                            cmax = fmax(cmax, fabs(c));
-                            xmax = fmax(xmax, fabs(nx));
+                            cmb = max(cmb, absbits_nonan(c));
+                            xmb = max(xmb, absbits_nonan(nx));
                         }
                         if (tid == 0) st.refine_sweeps++;
+                        double cmax = __longlong_as_double(cmb), xmax = __longlong_as_double(xmb);
                         block_max2(cmax, xmax, red);
                         if (sweep > 0) rate = fmax(rate, cmax / prev);
                         // stop when this correction, or the next one predicted
@@ -1739,14 +1760,14 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                         // res = xr - (dx - h*J(xf)*dx)
                         jv_phase1(m, xf, dx, qr);
                         __syncthreads();
-                        rloc = 0.0;
+                        rlb = 0;
                         for (int s = tid; s < N; s += kThreads) {
                             const double jv = jv_species(m, s, qr);
                             const double r = xr[s] - (dx[s] - dt * jv);
                             res[s] = r;
-                            rloc = fmax(rloc, fabs(r));
+                            rlb = max(rlb, absbits_nonan(r));
                         }
-                        rmax = block_max(rloc, red);
+                        rmax = block_max(__longlong_as_double(rlb), red);
                     }
                     lu_rate = rate;
                     if (converged || !soft || wide_abort) break;
@@ -2261,7 +2282,26 @@ __global__ void __launch_bounds__(kThreads, 1) wide_kernel(LaunchParams P) {
     const uint64_t wlimit = deadline ? deadline : start + 3600ull * 1000000000ull;
     const InstDesc &D0 = P.inst[0];
     const int N = D0.n;
-    const WideWs<LT> W = wide_ws<LT>(P.workspace, N, D0.r, D0.nnz_a);
+    WideWs<LT> W = wide_ws<LT>(P.workspace, N, D0.r, D0.nnz_a);
+    // tensor-core rank updates: each CTA holds kTcN TMEM columns and an
+    // mbarrier for the whole launch
+    __shared__ uint64_t tc_bar;
+    __shared__ uint32_t tc_slot, tc_phase;
+    const bool tc = std::is_same<LT, float>::value && P.tensor_cores != 0;
+    if (tc) {
+        if (threadIdx.x < 32) tc_alloc(&tc_slot, kTcN);
+        if (threadIdx.x == 0) {
+            tc_mbar_init(&tc_bar);
+            tc_phase = 0;
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        W.tc_on = 1;
+        W.tc_bar = &tc_bar;
+        W.tc_phase = &tc_phase;
+        W.tc_tmem = tc_slot;
+    }
     if (blockIdx.x == 0) {
         integrate<LT, true>(P, 0, smem, red, ired, mv, D, st, deadline, &W, wlimit);
     } else {
@@ -2276,6 +2316,12 @@ __global__ void __launch_bounds__(kThreads, 1) wide_kernel(LaunchParams P) {
         m.kk = P.darena + D0.k;
         // the leader's mdiag is its vector k1 (third of the ten)
         wide_worker<LT>(W, m, W.vec + 2 * (int64_t)N, smem, wlimit);
+    }
+    if (tc) {
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (threadIdx.x < 32) tc_dealloc(W.tc_tmem, kTcN);
     }
 }
 
@@ -2314,6 +2360,65 @@ cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStrea
     const void *f = P.precision == LASSIE_PREC_FP64 ? (const void *)wide_kernel<double>
                                                     : (const void *)wide_kernel<float>;
     return cudaLaunchCooperativeKernel(f, grid, kThreads, args, (size_t)smem, stream);
+}
+
+// ------------------------------------------------ tensor-core self-test
+
+// D = A * B (A: 128 x 32, B: 32 x kTcN, D: 128 x kTcN, row-major FP32) through
+// tc_tile_product on one CTA; status[0] = 1 on success, 2 if the MMA wait
+// ran out.
+__global__ void __launch_bounds__(kThreads, 1) tc_selftest_kernel(const float *A, const float *B,
+                                                                  float *D, int *status) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    float *sAh = reinterpret_cast<float *>(smem);
+    float *sAl = sAh + kTcM * kTcK;
+    float *sBh = sAl + kTcM * kTcK;
+    float *sBl = sBh + kTcN * kTcK;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sBl + kTcN * kTcK);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x;
+    if (tid < 32) tc_alloc(slot, kTcN);
+    if (tid == 0) tc_mbar_init(bar);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *slot;
+    for (int q = tid; q < kTcM * kTcK; q += kThreads) {
+        const int r = q / kTcK, k = q - r * kTcK;
+        const float x = A[q], hi = tf32_hi(x);
+        const int o = tc_off(r, k) / 4;
+        sAh[o] = hi;
+        sAl[o] = x - hi;
+    }
+    for (int q = tid; q < kTcN * kTcK; q += kThreads) {
+        const int n = q / kTcK, k = q - n * kTcK;
+        const float x = B[k * kTcN + n], hi = tf32_hi(x);
+        const int o = tc_off(n, k) / 4;
+        sBh[o] = hi;
+        sBl[o] = x - hi;
+    }
+    tc_proxy_fence();
+    __syncthreads();
+    uint32_t phase = 0;
+    float out[32];
+    const bool ok = tc_tile_product(sAh, sAl, sBh, sBl, bar, tmem, phase, out);
+    if (ok) {
+        const int w = tid >> 5, row = (w & 3) * 32 + (tid & 31), c0 = (w >> 2) * 32;
+        for (int i = 0; i < 32; i++) D[row * kTcN + c0 + i] = out[i];
+    }
+    __syncthreads();
+    if (tid < 32) tc_dealloc(tmem, kTcN);
+    if (tid == 0) status[0] = ok ? 1 : 2;
+}
+
+extern "C" int lassie_tc_selftest(const float *dA, const float *dB, float *dD, int *dstatus,
+                                  void *stream) {
+    const int smem = kTcSmemBytes;
+    if (cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return LASSIE_ERR_CUDA;
+    tc_selftest_kernel<<<1, kThreads, smem, (cudaStream_t)stream>>>(dA, dB, dD, dstatus);
+    return cudaGetLastError() == cudaSuccess ? LASSIE_OK : LASSIE_ERR_CUDA;
 }
 
 // ------------------------------------------ single-evaluation kernels

@@ -59,6 +59,11 @@ struct WideWs {
     LT *vin, *vout;   // [N] matrix-vector product input (gathered) and output
     int *flags;       // [0]: pivot order valid (set by the leader)
     int N, ld;
+    // this CTA's tensor-core state (rank updates on tcgen05 when tc_on)
+    int tc_on;
+    uint64_t *tc_bar;     // mbarrier (shared)
+    uint32_t *tc_phase;   // its parity (shared)
+    uint32_t tc_tmem;     // kTcN TMEM columns
 };
 
 struct WideLayout {
@@ -107,13 +112,18 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
     W.flags = reinterpret_cast<int *>(base + L.flags);
     W.N = N;
     W.ld = (N + 3) & ~3;
+    W.tc_on = 0;
+    W.tc_bar = nullptr;
+    W.tc_phase = nullptr;
+    W.tc_tmem = 0;
     return W;
 }
 
 // Dynamic shared memory of the wide kernel: the rank-update tiles, or the
 // matrix-vector input, whichever is larger, plus the pivot-block inverse.
 __host__ __device__ inline int64_t wide_smem_bytes(int N, int lt) {
-    const int64_t tiles = (int64_t(kWPB) * (kWT + 4) + int64_t(kWPB) * kWT) * lt;
+    int64_t tiles = (int64_t(kWPB) * (kWT + 4) + int64_t(kWPB) * kWT) * lt;
+    if (lt == 4 && tiles < 4 * kWT * kWPB * 4) tiles = 4 * kWT * kWPB * 4;  // tensor-core operands
     const int64_t vin = int64_t((N + 3) & ~3) * lt;
     return (tiles > vin ? tiles : vin) + int64_t(kWPB) * kWPB * lt;
 }
@@ -309,6 +319,102 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
     }
 }
 
+// task_update on the tensor cores (FP32 form): per 128 x 128 tile the
+// panel columns (A = AJ rows) and B = [PR | D^-1] are split into TF32 high
+// and low parts in the canonical K-major layout, tc_tile_product forms
+// AJ * B in tensor memory, and each thread finishes 32 entries of its row:
+// pivot rows take B, columns in J start from 0, the rest subtract from M.
+// False if a tensor-core wait ran out (the control block's abort flag is
+// then set).
+__device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *smem) {
+    float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
+    const int tid = threadIdx.x;
+    const int N = W.N, ld = W.ld;
+    const int nrt = (N + kTcM - 1) / kTcM, nct = (ld + kTcN - 1) / kTcN;
+    uint32_t phase = *W.tc_phase;
+    bool ok = true;
+    for (int t = blockIdx.x; t < nrt * nct && ok; t += gridDim.x) {
+        const int r0 = (t / nct) * kTcM, c0 = (t % nct) * kTcN;
+        __syncthreads();
+        for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
+            const int r = q >> 3, k4 = (q & 7) * 4;
+            float v[4] = {0.f, 0.f, 0.f, 0.f};
+            if (r0 + r < N) load4(W.AJ + (int64_t)(r0 + r) * kWPB + k4, v);
+            float h[4], l[4];
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                h[b] = tf32_hi(v[b]);
+                l[b] = v[b] - h[b];
+            }
+            const int o = tc_off(r, k4) / 4;
+            store4(sAh + o, h);
+            store4(sAl + o, l);
+        }
+        for (int q = tid; q < kTcN * (kTcK / 4); q += kThreads) {
+            const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
+            const int c = c0 + n;
+            const bool inJ = c >= j0 && c < j0 + kWPB;
+            float v[4], h[4], l[4];
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const int k = k4 + b;
+                float x = 0.f;
+                if (k < pb && c < ld) {
+                    if (inJ) x = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : 0.f;
+                    else x = W.PR[(int64_t)k * ld + c];
+                }
+                v[b] = x;
+                h[b] = tf32_hi(x);
+                l[b] = x - h[b];
+            }
+            const int o = tc_off(n, k4) / 4;
+            store4(sBh + o, h);
+            store4(sBl + o, l);
+        }
+        tc_proxy_fence();
+        __syncthreads();
+        float out[32];
+        ok = tc_tile_product(sAh, sAl, sBh, sBl, W.tc_bar, W.tc_tmem, phase, out);
+        if (!ok) break;
+        const int w = tid >> 5;
+        const int row = r0 + (w & 3) * 32 + (tid & 31), cb = c0 + (w >> 2) * 32;
+        if (row < N && cb < ld) {
+            const int pr = W.pos[row];
+            float *dst = W.A + (int64_t)row * ld;
+#pragma unroll
+            for (int g = 0; g < 8; g++) {
+                const int c = cb + 4 * g;
+                if (c >= ld) break;
+                const bool inJ = c >= j0 && c < j0 + kWPB;
+                float v[4];
+                if (pr >= 0) {
+#pragma unroll
+                    for (int b = 0; b < 4; b++)
+                        v[b] = inJ ? ((c + b - j0 < pb) ? W.Dinv[pr * kWPB + (c + b - j0)] : 0.f)
+                                   : W.PR[(int64_t)pr * ld + c + b];
+                } else {
+                    if (inJ) {
+#pragma unroll
+                        for (int b = 0; b < 4; b++) v[b] = 0.f;
+                    } else {
+                        load4(dst + c, v);
+                    }
+#pragma unroll
+                    for (int b = 0; b < 4; b++) v[b] -= out[4 * g + b];
+                }
+                store4(dst + c, v);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        *W.tc_phase = phase;
+        if (!ok) atomicExch(&W.ctl->abort, 1);
+    }
+    __syncthreads();
+    return ok;
+}
+
 // vout = A * vin, one warp per row, vin staged in shared memory.
 template <typename LT>
 __device__ void task_matvec(const WideWs<LT> &W, LT *svin) {
@@ -360,7 +466,15 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
         switch (s_task) {
         case kTaskAssemble: task_assemble<LT>(W, m, s_x, s_h, mdiag); break;
         case kTaskPanel: task_panel<LT>(W, s_j0, s_pb, sD); break;
-        case kTaskUpdate: task_update<LT>(W, s_j0, s_pb, sm); break;
+        case kTaskUpdate:
+            if constexpr (std::is_same<LT, float>::value) {
+                if (W.tc_on) {
+                    task_update_tc(W, s_j0, s_pb, sm);
+                    break;
+                }
+            }
+            task_update<LT>(W, s_j0, s_pb, sm);
+            break;
         case kTaskMatvec: task_matvec<LT>(W, sm); break;
         default: break;
         }
@@ -530,7 +644,14 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
             if (!wide_join<LT>(W, limit, sflag)) return 2;
             tick(1);
             wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
-            task_update<LT>(W, j0, pb, sm);
+            bool tc_done = false;
+            if constexpr (std::is_same<LT, float>::value) {
+                if (W.tc_on) {
+                    task_update_tc(W, j0, pb, sm);
+                    tc_done = true;
+                }
+            }
+            if (!tc_done) task_update<LT>(W, j0, pb, sm);
             if (!wide_join<LT>(W, limit, sflag)) return 2;
             tick(2);
         }

@@ -61,7 +61,7 @@ ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
 
 def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int = 0,
               deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow",
-              lu_reuse: bool = True) -> nat.Opts:
+              lu_reuse: bool = True, tensor_cores: bool = False) -> nat.Opts:
     o = nat.Opts()
     nat.load().lassie_opts_default(C.byref(o))
     if m is not None:
@@ -76,6 +76,7 @@ def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int =
     o.refine_max = int(refine_max)
     o.quarter_root = ROOTS[root]
     o.lu_reuse = 1 if lu_reuse else 0
+    o.tensor_cores = 1 if tensor_cores else 0
     return o
 
 
@@ -108,12 +109,13 @@ class _Packed:
 
 def simulate(m: Model, engine: str = "mixed", max_steps: int = 0, deadline_s: float = 0.0,
              nm: Optional[NativeModel] = None, root: str = "pow",
-             lu_reuse: bool = True) -> Tuple[np.ndarray, Dict]:
+             lu_reuse: bool = True, tensor_cores: bool = False) -> Tuple[np.ndarray, Dict]:
     """Integrate one model on the GPU.  Returns (trajectory [nt, ncs], stats)."""
     nm = nm or NativeModel.of(m)
     pk = _Packed(m, nm)
     st = nat.Stats()
-    o = make_opts(m, engine, max_steps, deadline_s, root=root, lu_reuse=lu_reuse)
+    o = make_opts(m, engine, max_steps, deadline_s, root=root, lu_reuse=lu_reuse,
+                  tensor_cores=tensor_cores)
     rc = nat.load().lassie_solve(nm.handle, _p(pk.k), _p(pk.x0), _p(pk.feed), _p(pk.atol),
                                  _p(pk.t), pk.t.shape[0], _p(pk.cs),
                                  0 if pk.cs is None else pk.cs.shape[0], C.byref(o),
@@ -131,7 +133,8 @@ class Batch:
 
     def __init__(self, models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                  deadline_s: float = 0.0, native: Optional[Sequence[NativeModel]] = None,
-                 refine_max: int = 0, root: str = "pow", lu_reuse: bool = True):
+                 refine_max: int = 0, root: str = "pow", lu_reuse: bool = True,
+                 tensor_cores: bool = False):
         L = nat.load()
         cache: Dict[int, NativeModel] = {}
         self.packs = []
@@ -147,7 +150,7 @@ class Batch:
         self.n = len(models)
         self._inst = (nat.Instance * max(self.n, 1))(*[p.instance() for p in self.packs])
         self.opts = make_opts(models[0] if self.n else None, engine, max_steps, deadline_s,
-                              refine_max, root, lu_reuse)
+                              refine_max, root, lu_reuse, tensor_cores)
         h = C.c_void_p()
         nat.check(L.lassie_batch_create(C.cast(self._inst, C.c_void_p), self.n,
                                         C.byref(self.opts), C.byref(h)), "lassie_batch_create")
