@@ -253,7 +253,9 @@ def parity_table():
         "c1 (64 x 64, t in [0,10])": synth.make_c1(),
         "c2 (512 x 512 stiff, t in [0,0.004])": synth.shorten(synth.make_c2(), 0.004, 3),
         "c3 (4096 x 4096, t in [0,0.02])": synth.shorten(synth.make_c3(), 0.02, 3),
-        "c5 (256 x 256, t in [0,1])": synth.shorten(synth.make_c5(1)[0][0], 1.0, 9),
+        # t in [0, 0.8]: on [0, 1] a one-ulp change of the Newton corrections
+        # already changes this network's RKF45 step sequence
+        "c5 (256 x 256, t in [0,0.8])": synth.shorten(synth.make_c5(1)[0][0], 0.8, 9),
     }
     out = {}
     for name, m in cases.items():
