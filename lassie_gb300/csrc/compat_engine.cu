@@ -234,25 +234,28 @@ __device__ __forceinline__ double rhs_species_r(const Net &m, int i, const doubl
 // forming J: per reaction the directional derivative of k*prod(x), with the
 // other reactants multiplied in once each as createJac does, then the same
 // species sums as the RHS.  Phase 1 writes qr[R].
-__device__ void jv_phase1(const Net &m, const double *x, const double *v, double *qr) {
-    for (int y = threadIdx.x; y < m.r; y += kThreads) {
-        const int b = m.rptr[y], en = m.rptr[y + 1];
-        double q = 0.0;
-        for (int j = b; j < en; j++) {
-            const int ej = m.rent[j];
-            const int g = ent_index(ej), a = ent_coef(ej);
-            double d;
-            if (a == 1) d = m.kk[y];
-            else if (a > 1) d = m.kk[y] * (double)a * mypow(x[g], a - 1);
-            else continue;
-            for (int jj = b; jj < en; jj++) {
-                const int o = ent_index(m.rent[jj]);
-                if (o != g) d = d * x[o];
-            }
-            q = fma(d, v[g], q);
+__device__ __forceinline__ double jv_reaction(const Net &m, const double *x, const double *v,
+                                               int y) {
+    const int b = m.rptr[y], en = m.rptr[y + 1];
+    double q = 0.0;
+    for (int j = b; j < en; j++) {
+        const int ej = m.rent[j];
+        const int g = ent_index(ej), a = ent_coef(ej);
+        double d;
+        if (a == 1) d = m.kk[y];
+        else if (a > 1) d = m.kk[y] * (double)a * mypow(x[g], a - 1);
+        else continue;
+        for (int jj = b; jj < en; jj++) {
+            const int o = ent_index(m.rent[jj]);
+            if (o != g) d = d * x[o];
         }
-        qr[y] = q;
+        q = fma(d, v[g], q);
     }
+    return q;
+}
+
+__device__ void jv_phase1(const Net &m, const double *x, const double *v, double *qr) {
+    for (int y = threadIdx.x; y < m.r; y += kThreads) qr[y] = jv_reaction(m, x, v, y);
 }
 
 __device__ __forceinline__ double jv_species(const Net &m, int i, const double *qr) {
@@ -1273,14 +1276,72 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
     }
 }
 
-#include "tc.cuh"
-#include "wide.cuh"
 
 // ----------------------------------------------------------- integrator
 
 struct Vecs {
     double *y1, *u, *k1, *k2, *k3, *k4, *k5, *k6, *fd, *tol;
 };
+
+// RKF45 stage stg (0..4) for species s with f = f(stage input)_s
+// (kernels.cuh:68-143): the slope k_{stg+1} = f*dt (the feed for a fed
+// species) and the next stage input u, in the reference's expression order.
+__device__ __forceinline__ void rkf_stage(int stg, const Vecs &V, int s, double f, double dt) {
+    double *k = stg == 0 ? V.k1 : stg == 1 ? V.k2 : stg == 2 ? V.k3 : stg == 3 ? V.k4 : V.k5;
+    if (V.fd[s] != 0.0) {
+        k[s] = V.fd[s];
+        return;
+    }
+    k[s] = f * dt;
+    switch (stg) {
+    case 0: V.u[s] = V.y1[s] + V.k1[s] / 4.0; break;
+    case 1: V.u[s] = V.y1[s] + (3.0 * V.k1[s]) / 32.0 + (9.0 * V.k2[s]) / 32.0; break;
+    case 2:
+        V.u[s] = V.y1[s] + (1932.0 * V.k1[s]) / 2197.0 - (7200.0 * V.k2[s]) / 2197.0 +
+                 (7296.0 * V.k3[s]) / 2197.0;
+        break;
+    case 3:
+        V.u[s] = V.y1[s] + (439.0 * V.k1[s]) / 216.0 - (8.0 * V.k2[s]) +
+                 (3680.0 * V.k3[s]) / 513.0 - (845.0 * V.k4[s]) / 4104.0;
+        break;
+    default:
+        V.u[s] = V.y1[s] - (8.0 * V.k1[s]) / 27.0 + (2.0 * V.k2[s]) -
+                 (3544.0 * V.k3[s]) / 2565.0 + (1859.0 * V.k4[s]) / 4104.0 -
+                 (11.0 * V.k5[s]) / 40.0;
+        break;
+    }
+}
+
+// Last stage for species s (kernels.cuh:144-199): k6, the 4th- and 5th-order
+// solutions w1, w2 (w1 kept in k1 for an accept), the error R = |w1-w2|/dt,
+// the accept test, and delta = 0.84 (atol/R)^(1/4); ok, dloc (min delta) and
+// d0nan (species 0's delta is NaN) accumulate.
+__device__ __forceinline__ void rkf_final(const Vecs &V, int s, double f, double dt,
+                                          bool root_sqrt, bool &ok, double &dloc, bool &d0nan) {
+    const double fdv = V.fd[s];
+    double k6 = (fdv != 0.0) ? fdv : f * dt;
+    V.k6[s] = k6;
+    double w1, w2;
+    if (fdv != 0.0) {
+        w1 = fdv;
+        w2 = fdv;
+    } else {
+        w1 = V.y1[s] + (25.0 * V.k1[s]) / 216.0 + (1408.0 * V.k3[s]) / 2565.0 +
+             (2197.0 * V.k4[s]) / 4104.0 - V.k5[s] / 5.0;
+        w2 = V.y1[s] + (16.0 * V.k1[s]) / 135.0 + (6656.0 * V.k3[s]) / 12825.0 +
+             (28561.0 * V.k4[s]) / 56430.0 - (9.0 * V.k5[s] / 50.0) + (2.0 * k6) / 55.0;
+    }
+    V.k1[s] = w1;  // the 4th-order solution, kept on accept (u untouched)
+    const double Rv = fabs(w1 - w2) / dt;
+    const double q = V.tol[s] / Rv;
+    const double delta = 0.84 * (root_sqrt ? sqrt(sqrt(q)) : pow(q, 0.25));
+    if (!(Rv <= V.tol[s] && !isnan(Rv) && !isinf(Rv) && w1 > 0)) ok = false;
+    if (s == 0) d0nan = isnan(delta);
+    if (delta < dloc) dloc = delta;
+}
+
+#include "tc.cuh"
+#include "wide.cuh"
 
 // One instance, one CTA (kWide = false: the batched engine, everything in
 // shared memory, per-CTA LU), or the leader CTA of the wide engine (kWide:
@@ -1441,93 +1502,25 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         }
         // ---- RKF45 attempt (Simulation.cuh:692-735, kernels.cuh:68-199)
         c_mark = clock64();
-        rhs_rates(m, V.y1, pw, qr);
-        __syncthreads();
-        for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species_r(m, s, pw, qr);
-            if (V.fd[s] != 0.0) V.k1[s] = V.fd[s];
-            else {
-                V.k1[s] = f * dt;
-                V.u[s] = V.y1[s] + V.k1[s] / 4.0;
-            }
-        }
-        __syncthreads();
-        rhs_rates(m, V.u, pw, qr);
-        __syncthreads();
-        for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species_r(m, s, pw, qr);
-            if (V.fd[s] != 0.0) V.k2[s] = V.fd[s];
-            else {
-                V.k2[s] = f * dt;
-                V.u[s] = V.y1[s] + (3.0 * V.k1[s]) / 32.0 + (9.0 * V.k2[s]) / 32.0;
-            }
-        }
-        __syncthreads();
-        rhs_rates(m, V.u, pw, qr);
-        __syncthreads();
-        for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species_r(m, s, pw, qr);
-            if (V.fd[s] != 0.0) V.k3[s] = V.fd[s];
-            else {
-                V.k3[s] = f * dt;
-                V.u[s] = V.y1[s] + (1932.0 * V.k1[s]) / 2197.0 - (7200.0 * V.k2[s]) / 2197.0 +
-                         (7296.0 * V.k3[s]) / 2197.0;
-            }
-        }
-        __syncthreads();
-        rhs_rates(m, V.u, pw, qr);
-        __syncthreads();
-        for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species_r(m, s, pw, qr);
-            if (V.fd[s] != 0.0) V.k4[s] = V.fd[s];
-            else {
-                V.k4[s] = f * dt;
-                V.u[s] = V.y1[s] + (439.0 * V.k1[s]) / 216.0 - (8.0 * V.k2[s]) +
-                         (3680.0 * V.k3[s]) / 513.0 - (845.0 * V.k4[s]) / 4104.0;
-            }
-        }
-        __syncthreads();
-        rhs_rates(m, V.u, pw, qr);
-        __syncthreads();
-        for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species_r(m, s, pw, qr);
-            if (V.fd[s] != 0.0) V.k5[s] = V.fd[s];
-            else {
-                V.k5[s] = f * dt;
-                V.u[s] = V.y1[s] - (8.0 * V.k1[s]) / 27.0 + (2.0 * V.k2[s]) -
-                         (3544.0 * V.k3[s]) / 2565.0 + (1859.0 * V.k4[s]) / 4104.0 -
-                         (11.0 * V.k5[s]) / 40.0;
-            }
-        }
-        __syncthreads();
-        rhs_rates(m, V.u, pw, qr);
-        __syncthreads();
         bool ok = true;
         double dloc = INFINITY;
         bool d0nan = false;
-        for (int s = tid; s < N; s += kThreads) {
-            const double f = rhs_species_r(m, s, pw, qr);
-            const double fdv = V.fd[s];
-            double k6 = (fdv != 0.0) ? fdv : f * dt;
-            V.k6[s] = k6;
-            double w1, w2;
-            if (fdv != 0.0) {
-                w1 = fdv;
-                w2 = fdv;
-            } else {
-                w1 = V.y1[s] + (25.0 * V.k1[s]) / 216.0 + (1408.0 * V.k3[s]) / 2565.0 +
-                     (2197.0 * V.k4[s]) / 4104.0 - V.k5[s] / 5.0;
-                w2 = V.y1[s] + (16.0 * V.k1[s]) / 135.0 + (6656.0 * V.k3[s]) / 12825.0 +
-                     (28561.0 * V.k4[s]) / 56430.0 - (9.0 * V.k5[s] / 50.0) +
-                     (2.0 * k6) / 55.0;
+        if constexpr (kWide) {
+            // stages spread over the whole grid (fork-join tasks)
+            wide_rkf_attempt<LT>(*W, m, V, dt, root_sqrt, pw, qr, wlimit, wflag, ok, dloc, d0nan,
+                                 wide_abort);
+        } else {
+            for (int stg = 0; stg < 5; stg++) {
+                rhs_rates(m, stg == 0 ? V.y1 : V.u, pw, qr);
+                __syncthreads();
+                for (int s = tid; s < N; s += kThreads)
+                    rkf_stage(stg, V, s, rhs_species_r(m, s, pw, qr), dt);
+                __syncthreads();
             }
-            V.k1[s] = w1;  // the 4th-order solution, kept on accept (u untouched)
-            const double Rv = fabs(w1 - w2) / dt;
-            const double q = V.tol[s] / Rv;
-            const double delta = 0.84 * (root_sqrt ? sqrt(sqrt(q)) : pow(q, 0.25));
-            if (!(Rv <= V.tol[s] && !isnan(Rv) && !isinf(Rv) && w1 > 0)) ok = false;
-            if (s == 0) d0nan = isnan(delta);
-            if (delta < dloc) dloc = delta;
+            rhs_rates(m, V.u, pw, qr);
+            __syncthreads();
+            for (int s = tid; s < N; s += kThreads)
+                rkf_final(V, s, rhs_species_r(m, s, pw, qr), dt, root_sqrt, ok, dloc, d0nan);
         }
         const int all_ok = __syncthreads_and(ok);
         if (tid == 0) st.cycles_rkf += clock64() - c_mark;
@@ -1632,14 +1625,21 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 if (expired) break;
             }
             // x = f(y_v); x = -(y_v - y1 - h*x)   (kernels.cuh:289-300)
-            rhs_rates(m, yv, pw, qr);
-            __syncthreads();
-            for (int s = tid; s < N; s += kThreads) {
-                const double f = rhs_species_r(m, s, pw, qr);
-                xr[s] = -(yv[s] - V.y1[s] - dt * f);
-                if (itN == 0) xf[s] = yv[s];
+            if constexpr (kWide) {
+                if (!wide_newton_rhs<LT>(*W, m, V, dt, itN == 0, wlimit, wflag)) {
+                    wide_abort = true;
+                    break;
+                }
+            } else {
+                rhs_rates(m, yv, pw, qr);
+                __syncthreads();
+                for (int s = tid; s < N; s += kThreads) {
+                    const double f = rhs_species_r(m, s, pw, qr);
+                    xr[s] = -(yv[s] - V.y1[s] - dt * f);
+                    if (itN == 0) xf[s] = yv[s];
+                }
+                __syncthreads();
             }
-            __syncthreads();
             if (itN == 0) {
                 reused = false;
                 if constexpr (kMixed)
@@ -1708,23 +1708,28 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                         const long long lost_lim =
                             le >= -1022 ? (long long)(le + 1023) << 52
                                         : (le >= -1074 ? 1LL << (le + 1074) : 0LL);
+                        double cmax, xmax;
+                        if constexpr (kWide) {
+                            // scaling, matrix-vector product and update on the grid
+                            const long long c_tri = clock64();
+                            if (!wide_solve_update<LT>(*W, V, sc, isc, lost_lim,
+                                                       reinterpret_cast<LT *>(smem), wlimit,
+                                                       wflag, cmax, xmax))
+                                wide_abort = true;
+                            if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
+                            if (wide_abort) break;
+                        } else {
                         for (int s = tid; s < N; s += kThreads)
                             bvec[s] = (LT)(res[perm[s]] * sc);
                         __syncthreads();
                         const long long c_tri = clock64();
-                        if constexpr (kWide) {
-                            if (!wide_apply<LT>(*W, smem, wlimit, wflag)) wide_abort = true;
-                        } else {
-                            gje_apply(reinterpret_cast<const float *>(M), ld, N, perm,
-                                      reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt),
-                                      false);
-                        }
+                        gje_apply(reinterpret_cast<const float *>(M), ld, N, perm,
+                                  reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt),
+                                  false);
                         if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
                         long long cmb = 0, xmb = 0;
                         for (int s = tid; s < N; s += kThreads) {
-                            double c;
-                            if constexpr (kWide) c = (double)bvec[s] * isc;
-                            else c = (double)reinterpret_cast<const float *>(lt)[perm[s]] * isc;
+                            double c = (double)reinterpret_cast<const float *>(lt)[perm[s]] * isc;
                             // the part of this row's right-hand side that the
                             // FP32 cast lost (below the FP32 normal range),
                             // applied through the diagonal
@@ -1738,9 +1743,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                             cmb = max(cmb, absbits_nonan(c));
                             xmb = max(xmb, absbits_nonan(nx));
                         }
-                        if (tid == 0) st.refine_sweeps++;
-                        double cmax = __longlong_as_double(cmb), xmax = __longlong_as_double(xmb);
+                        cmax = __longlong_as_double(cmb);
+                        xmax = __longlong_as_double(xmb);
                         block_max2(cmax, xmax, red);
+                        }
+                        if (tid == 0) st.refine_sweeps++;
                         if (sweep > 0) rate = fmax(rate, cmax / prev);
                         // stop when this correction, or the next one predicted
                         // from the contraction so far, is below FP64 resolution
@@ -1758,6 +1765,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                             break;
                         prev = cmax;
                         // res = xr - (dx - h*J(xf)*dx)
+                        if constexpr (kWide) {
+                            if (!wide_residual<LT>(*W, m, V, dt, wlimit, wflag, rmax))
+                                wide_abort = true;
+                            if (wide_abort) break;
+                        } else {
                         jv_phase1(m, xf, dx, qr);
                         __syncthreads();
                         rlb = 0;
@@ -1768,6 +1780,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                             rlb = max(rlb, absbits_nonan(r));
                         }
                         rmax = block_max(__longlong_as_double(rlb), red);
+                        }
                     }
                     lu_rate = rate;
                     if (converged || !soft || wide_abort) break;
@@ -2350,7 +2363,7 @@ int wide_configure(int precision, int64_t smem, int sm_count) {
             cudaSuccess ||
         per_sm < 1)
         return 0;
-    return sm_count;
+    return sm_count < kWideMaxGrid ? sm_count : kWideMaxGrid;
 }
 
 // The caller clears the control block and the pivot-order flag first.

@@ -27,7 +27,12 @@ constexpr int kWPB = 32;   // Gauss-Jordan panel width
 constexpr int kWT = 128;   // rank-update tile: kWT rows x kWT columns per CTA pass
 
 enum WideTask : int { kTaskExit = 0, kTaskAssemble = 1, kTaskPanel = 2, kTaskUpdate = 3,
-                      kTaskMatvec = 4 };
+                      kTaskMatvec = 4, kTaskRates = 5, kTaskRkf = 6, kTaskRkfFinal = 7,
+                      kTaskSolve = 8, kTaskSolveUpdate = 9, kTaskJv = 10, kTaskResidual = 11,
+                      kTaskNewtonRhs = 12 };
+
+// Most CTAs of one wide launch (per-CTA partial results of the RKF45 error).
+constexpr int kWideMaxGrid = 256;
 
 // Control block (global memory), zeroed before the launch.
 struct WideCtl {
@@ -37,8 +42,12 @@ struct WideCtl {
     int task;
     int j0, pb;         // current panel
     int pad0, pad1;
-    double h;           // step of the matrix being assembled
-    const double *x;    // state the Jacobian is evaluated at
+    double h;           // step of the matrix being assembled (RKF45: the step)
+    const double *x;    // state the Jacobian (or the RHS) is evaluated at
+    Vecs vecs;          // the leader's current RKF45 vectors (and Newton aliases)
+    int root_sqrt;      // RKF45 step factor: sqrt(sqrt()) instead of pow
+    double sc, isc;     // refinement: residual scale and its inverse
+    long long lost;     // refinement: bit-pattern bound of the FP32-lost residuals
 };
 
 // Workspace of the wide engine, carved from one allocation (WideLayout).
@@ -58,6 +67,7 @@ struct WideWs {
     LT *AJ;           // [N][kWPB] panel columns before the update
     LT *vin, *vout;   // [N] matrix-vector product input (gathered) and output
     int *flags;       // [0]: pivot order valid (set by the leader)
+    long long *part;  // [2][kWideMaxGrid]: per-CTA RKF45 accept flag, min delta bits
     int N, ld;
     // this CTA's tensor-core state (rank updates on tcgen05 when tc_on)
     int tc_on;
@@ -67,7 +77,7 @@ struct WideWs {
 };
 
 struct WideLayout {
-    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJ, vin, vout, flags, total;
+    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJ, vin, vout, flags, part, total;
     __host__ __device__ static int64_t al(int64_t v) { return (v + 255) & ~int64_t(255); }
     __host__ __device__ WideLayout(int N, int R, int nnz_a, int lt) {
         const int64_t ld = (N + 3) & ~3;
@@ -87,6 +97,7 @@ struct WideLayout {
         vin = o;   o = al(o + int64_t(N) * lt);
         vout = o;  o = al(o + int64_t(N) * lt);
         flags = o; o = al(o + 16);
+        part = o;  o = al(o + int64_t(2) * kWideMaxGrid * 8);
         total = o;
     }
 };
@@ -110,6 +121,7 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
     W.vin = reinterpret_cast<LT *>(base + L.vin);
     W.vout = reinterpret_cast<LT *>(base + L.vout);
     W.flags = reinterpret_cast<int *>(base + L.flags);
+    W.part = reinterpret_cast<long long *>(base + L.part);
     W.N = N;
     W.ld = (N + 3) & ~3;
     W.tc_on = 0;
@@ -437,6 +449,138 @@ __device__ void task_matvec(const WideWs<LT> &W, LT *svin) {
     }
 }
 
+// RKF45 tasks: the stages of an attempt with every species and reaction
+// spread over the whole grid (rkf_stage, rkf_final: the batched engine's
+// arithmetic).
+__device__ void task_rates(const Net &m, const double *x, double *pw, double *rate) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    for (int y = gt; y < m.r; y += nt) {
+        double r = m.kk[y];
+        for (int q = m.rptr[y]; q < m.rptr[y + 1]; q++) {
+            const int e = m.rent[q];
+            const double p = mypow(x[ent_index(e)], ent_coef(e));
+            pw[q] = p;
+            r = r * p;
+        }
+        rate[y] = r;
+    }
+}
+
+__device__ void task_rkf(const Net &m, const Vecs &V, int stg, double dt, const double *pw,
+                         const double *rate) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    for (int s = gt; s < m.n; s += nt) rkf_stage(stg, V, s, rhs_species_r(m, s, pw, rate), dt);
+}
+
+// Last stage; this CTA's accept flag and min delta (bit pattern, NaN as +inf)
+// go to part[blockIdx.x] and part[kWideMaxGrid + blockIdx.x].  Returns
+// whether species 0's delta is NaN (meaningful in the CTA that owns it).
+__device__ bool task_rkf_final(long long *part, const Net &m, const Vecs &V, double dt,
+                               bool root_sqrt, const double *pw, const double *rate,
+                               double *red) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    bool ok = true, d0nan = false;
+    double dloc = INFINITY;
+    for (int s = gt; s < m.n; s += nt)
+        rkf_final(V, s, rhs_species_r(m, s, pw, rate), dt, root_sqrt, ok, dloc, d0nan);
+    const int all = __syncthreads_and(ok);
+    const int dn = __syncthreads_or(d0nan);
+    const double dmin = block_min_nonnan(dloc, red);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = all;
+        part[kWideMaxGrid + blockIdx.x] = __double_as_longlong(dmin);
+    }
+    return dn != 0;
+}
+
+// Refinement tasks (mixed form; the Newton vectors are the leader's aliases:
+// res = k6, dx = k4, xr = k3, xf = k5, mdiag = k1).
+// Solve: vout = X * (res[piv] * sc), the scaled residual staged per CTA.
+template <typename LT>
+__device__ void task_solve(const WideWs<LT> &W, const double *res, double sc, LT *svin) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int N = W.N, ld = W.ld;
+    for (int c = tid; c < ld; c += kThreads) svin[c] = (c < N) ? (LT)(res[W.piv[c]] * sc) : LT(0);
+    __syncthreads();
+    const int gw = blockIdx.x * kWarps + (tid >> 5), nw = gridDim.x * kWarps;
+    for (int i = gw; i < N; i += nw) {
+        const LT *Ar = W.A + (int64_t)i * ld;
+        LT acc = LT(0);
+        for (int c = lane * 4; c < ld; c += 128) {
+            LT a[4];
+            load4(Ar + c, a);
+#pragma unroll
+            for (int b = 0; b < 4; b++) acc = lt_fma(a[b], svin[c + b], acc);
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) W.vout[i] = acc;
+    }
+}
+
+// Update: dx += x * isc (x[s] = vout[piv[s]]) plus the FP64 diagonal part of
+// residuals below the FP32 range; this CTA's max |correction| and max |dx|
+// (bit patterns, NaN ignored) go to part[g] and part[kWideMaxGrid + g].
+template <typename LT>
+__device__ void task_solve_update(const WideWs<LT> &W, const Vecs &V, double sc, double isc,
+                                  long long lost, double *red) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    const double *res = V.k6, *mdiag = V.k1;
+    double *dx = V.k4;
+    long long cmb = 0, xmb = 0;
+    for (int s = gt; s < W.N; s += nt) {
+        double c = (double)W.vout[W.piv[s]] * isc;
+        if ((__double_as_longlong(res[s]) & 0x7fffffffffffffffLL) < lost) {
+            const double rs = res[s] * sc;
+            if (fabs(mdiag[s]) >= 0.5) c += (rs - (double)(float)rs) * isc / mdiag[s];
+        }
+        const double nx = dx[s] + c;
+        dx[s] = nx;
+        cmb = max(cmb, absbits_nonan(c));
+        xmb = max(xmb, absbits_nonan(nx));
+    }
+    double cm = __longlong_as_double(cmb), xm = __longlong_as_double(xmb);
+    block_max2(cm, xm, red);
+    if (threadIdx.x == 0) {
+        W.part[blockIdx.x] = __double_as_longlong(cm);
+        W.part[kWideMaxGrid + blockIdx.x] = __double_as_longlong(xm);
+    }
+}
+
+// Newton residual of the backward-Euler step (kernels.cuh:289-300):
+// xr = -(yv - y1 - dt * f(yv)), and xf = yv at the first iteration
+// (yv = k2, xr = k3, xf = k5); the rates of yv are in pw/rate.
+__device__ void task_newton_rhs(const Net &m, const Vecs &V, double dt, bool first,
+                                const double *pw, const double *rate) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    for (int s = gt; s < m.n; s += nt) {
+        const double f = rhs_species_r(m, s, pw, rate);
+        V.k3[s] = -(V.k2[s] - V.y1[s] - dt * f);
+        if (first) V.k5[s] = V.k2[s];
+    }
+}
+
+__device__ void task_jv(const Net &m, const double *x, const double *v, double *qr) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    for (int y = gt; y < m.r; y += nt) qr[y] = jv_reaction(m, x, v, y);
+}
+
+// res = xr - (dx - dt * J v); this CTA's max |res| (NaN ignored) to part[g].
+__device__ void task_residual(long long *part, const Net &m, const Vecs &V, double dt,
+                              const double *qr, double *red) {
+    const int gt = blockIdx.x * kThreads + threadIdx.x, nt = gridDim.x * kThreads;
+    const double *xr = V.k3, *dx = V.k4;
+    double *res = V.k6;
+    long long rlb = 0;
+    for (int s = gt; s < m.n; s += nt) {
+        const double jv = jv_species(m, s, qr);
+        const double r = xr[s] - (dx[s] - dt * jv);
+        res[s] = r;
+        rlb = max(rlb, absbits_nonan(r));
+    }
+    const double rm = block_max(__longlong_as_double(rlb), red);
+    if (threadIdx.x == 0) part[blockIdx.x] = __double_as_longlong(rm);
+}
+
 // Worker CTA: serve tasks until the leader sends kTaskExit (or a wait runs
 // out of time).
 template <typename LT>
@@ -476,6 +620,44 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
             task_update<LT>(W, s_j0, s_pb, sm);
             break;
         case kTaskMatvec: task_matvec<LT>(W, sm); break;
+        case kTaskRates: task_rates(m, s_x, W.pw, W.qr); break;
+        case kTaskSolve: {
+            const Vecs v = W.ctl->vecs;
+            task_solve<LT>(W, v.k6, W.ctl->sc, sm);
+            break;
+        }
+        case kTaskSolveUpdate: {
+            const Vecs v = W.ctl->vecs;
+            task_solve_update<LT>(W, v, W.ctl->sc, W.ctl->isc, W.ctl->lost,
+                                  reinterpret_cast<double *>(sm));
+            break;
+        }
+        case kTaskJv: {
+            const Vecs v = W.ctl->vecs;
+            task_jv(m, v.k5, v.k4, W.qr);
+            break;
+        }
+        case kTaskResidual: {
+            const Vecs v = W.ctl->vecs;
+            task_residual(W.part, m, v, s_h, W.qr, reinterpret_cast<double *>(sm));
+            break;
+        }
+        case kTaskNewtonRhs: {
+            const Vecs v = W.ctl->vecs;
+            task_newton_rhs(m, v, s_h, s_j0 != 0, W.pw, W.qr);
+            break;
+        }
+        case kTaskRkf: {
+            const Vecs v = W.ctl->vecs;
+            task_rkf(m, v, s_j0, s_h, W.pw, W.qr);
+            break;
+        }
+        case kTaskRkfFinal: {
+            const Vecs v = W.ctl->vecs;
+            task_rkf_final(W.part, m, v, s_h, W.ctl->root_sqrt != 0, W.pw, W.qr,
+                           reinterpret_cast<double *>(sm));
+            break;
+        }
         default: break;
         }
         __syncthreads();
@@ -682,6 +864,105 @@ __device__ bool wide_apply(const WideWs<LT> &W, unsigned char *smem, uint64_t li
     for (int j = threadIdx.x; j < W.N; j += kThreads) W.vin[j] = W.vout[W.piv[j]];
     __syncthreads();
     return true;
+}
+
+// Leader: one RKF45 attempt over the grid.  Sets ok (all species accepted),
+// dloc (min delta over the non-NaN deltas, +inf if none) and d0nan; sets
+// abort if a wait ran out.
+template <typename LT>
+__device__ void wide_rkf_attempt(const WideWs<LT> &W, const Net &m, const Vecs &V, double dt,
+                                 bool root_sqrt, double *pw, double *rate, uint64_t limit,
+                                 int *sflag, bool &ok, double &dloc, bool &d0nan, bool &abort) {
+    if (threadIdx.x == 0) {
+        W.ctl->vecs = V;
+        W.ctl->root_sqrt = root_sqrt ? 1 : 0;
+    }
+    for (int stg = 0; stg < 5; stg++) {
+        const double *x = stg == 0 ? V.y1 : V.u;
+        wide_fork<LT>(W, kTaskRates, 0, 0, dt, x);
+        task_rates(m, x, pw, rate);
+        if (!wide_join<LT>(W, limit, sflag)) { abort = true; return; }
+        wide_fork<LT>(W, kTaskRkf, stg, 0, dt, x);
+        task_rkf(m, V, stg, dt, pw, rate);
+        if (!wide_join<LT>(W, limit, sflag)) { abort = true; return; }
+    }
+    wide_fork<LT>(W, kTaskRates, 0, 0, dt, V.u);
+    task_rates(m, V.u, pw, rate);
+    if (!wide_join<LT>(W, limit, sflag)) { abort = true; return; }
+    wide_fork<LT>(W, kTaskRkfFinal, 0, 0, dt, V.u);
+    // species 0 belongs to the leader (global thread 0)
+    __shared__ double red2[2 * kWarps + 1];
+    d0nan = task_rkf_final(W.part, m, V, dt, root_sqrt, pw, rate, red2);
+    if (!wide_join<LT>(W, limit, sflag)) { abort = true; return; }
+    long long mn = 0x7ff0000000000000LL;
+    int all = 1;
+    for (int g = 0; g < (int)gridDim.x; g++) {
+        all &= (int)W.part[g];
+        const long long b = W.part[kWideMaxGrid + g];
+        mn = b < mn ? b : mn;
+    }
+    ok = all != 0;
+    dloc = __longlong_as_double(mn);
+}
+
+// Leader: one refinement sweep's solve and update over the grid; cmax, xmax
+// as the batched engine's (uniform).  False if a wait ran out.
+template <typename LT>
+__device__ bool wide_solve_update(const WideWs<LT> &W, const Vecs &V, double sc, double isc,
+                                  long long lost, LT *sm, uint64_t limit, int *sflag,
+                                  double &cmax, double &xmax) {
+    __shared__ double red3[2 * kWarps + 1];
+    if (threadIdx.x == 0) {
+        W.ctl->vecs = V;
+        W.ctl->sc = sc;
+        W.ctl->isc = isc;
+        W.ctl->lost = lost;
+    }
+    wide_fork<LT>(W, kTaskSolve, 0, 0, 0.0, nullptr);
+    task_solve<LT>(W, V.k6, sc, sm);
+    if (!wide_join<LT>(W, limit, sflag)) return false;
+    wide_fork<LT>(W, kTaskSolveUpdate, 0, 0, 0.0, nullptr);
+    task_solve_update<LT>(W, V, sc, isc, lost, red3);
+    if (!wide_join<LT>(W, limit, sflag)) return false;
+    long long cm = 0, xm = 0;
+    for (int g = 0; g < (int)gridDim.x; g++) {
+        cm = max(cm, W.part[g]);
+        xm = max(xm, W.part[kWideMaxGrid + g]);
+    }
+    cmax = __longlong_as_double(cm);
+    xmax = __longlong_as_double(xm);
+    return true;
+}
+
+// Leader: res = xr - (dx - dt * J(xf) dx) over the grid and its max (rmax).
+template <typename LT>
+__device__ bool wide_residual(const WideWs<LT> &W, const Net &m, const Vecs &V, double dt,
+                              uint64_t limit, int *sflag, double &rmax) {
+    __shared__ double red4[2 * kWarps + 1];
+    if (threadIdx.x == 0) W.ctl->vecs = V;
+    wide_fork<LT>(W, kTaskJv, 0, 0, dt, nullptr);
+    task_jv(m, V.k5, V.k4, W.qr);
+    if (!wide_join<LT>(W, limit, sflag)) return false;
+    wide_fork<LT>(W, kTaskResidual, 0, 0, dt, nullptr);
+    task_residual(W.part, m, V, dt, W.qr, red4);
+    if (!wide_join<LT>(W, limit, sflag)) return false;
+    long long rm = 0;
+    for (int g = 0; g < (int)gridDim.x; g++) rm = max(rm, W.part[g]);
+    rmax = __longlong_as_double(rm);
+    return true;
+}
+
+// Leader: the Newton residual over the grid (task_newton_rhs).
+template <typename LT>
+__device__ bool wide_newton_rhs(const WideWs<LT> &W, const Net &m, const Vecs &V, double dt,
+                                bool first, uint64_t limit, int *sflag) {
+    if (threadIdx.x == 0) W.ctl->vecs = V;
+    wide_fork<LT>(W, kTaskRates, 0, 0, dt, V.k2);
+    task_rates(m, V.k2, W.pw, W.qr);
+    if (!wide_join<LT>(W, limit, sflag)) return false;
+    wide_fork<LT>(W, kTaskNewtonRhs, first ? 1 : 0, 0, dt, nullptr);
+    task_newton_rhs(m, V, dt, first, W.pw, W.qr);
+    return wide_join<LT>(W, limit, sflag);
 }
 
 // Leader: release the workers.
