@@ -97,3 +97,26 @@ def trajectory_misfit(log_k, models: Sequence[Model], targets: Sequence[np.ndarr
                       ckpt_every: int = 8):
     """Differentiable misfit: ``trajectory_misfit(log_k, models, targets).sum().backward()``."""
     return _torch_function().apply(log_k, list(models), list(targets), ckpt_every)
+
+
+def fit_rate_constants(models: Sequence[Model], targets: Sequence[np.ndarray],
+                       log_k0: Optional[np.ndarray] = None, iters: int = 50, lr: float = 0.05,
+                       ckpt_every: int = 8):
+    """Parameter estimation (the misfit of LASSIE's LSODA comparator,
+    ``LSODAsim.py:104-121``, minimised over log k): Adam on
+    sum_b trajectory_misfit(log_k[b]) with the adjoint gradients.  One row
+    of log k per model (initial values log_k0, default the models' own).
+    Returns (log_k [B, R], loss per iteration)."""
+    import torch
+    if log_k0 is None:
+        log_k0 = np.stack([np.log(m.k) for m in models])
+    log_k = torch.tensor(np.asarray(log_k0, np.float64), requires_grad=True)
+    opt = torch.optim.Adam([log_k], lr=lr)
+    history = []
+    for _ in range(iters):
+        opt.zero_grad()
+        loss = trajectory_misfit(log_k, models, targets, ckpt_every).sum()
+        loss.backward()
+        opt.step()
+        history.append(float(loss.detach()))
+    return log_k.detach().numpy(), history

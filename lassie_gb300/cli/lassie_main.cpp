@@ -119,6 +119,63 @@ void write_block_info(const std::string &folder, int sms, const char *type, int 
 
 }  // namespace
 
+// Symbolic right-hand sides (-v2; Simulation.cuh:83-147, printOdes): per
+// species the net-stoichiometry terms in reaction order, "+c*k[j]" times
+// "*x[i]" once per unit of each reactant's stoichiometry; "dx[i] = 0" when
+// there is none.  Fed species print nothing, as in the reference.
+static void print_odes(const std::vector<int32_t> &dl, const std::vector<int32_t> &dr, int N,
+                       int R, const std::vector<double> &feed) {
+    for (int gid = 0; gid < N; gid++) {
+        if (feed[gid] != 0) continue;
+        std::string s;
+        for (int y = 0; y < R; y++) {
+            const int c = dr[(size_t)y * N + gid] - dl[(size_t)y * N + gid];
+            if (c == 0) continue;
+            s += (c > 0 ? "+" : "") + std::to_string(c) + "*k[" + std::to_string(y) + "]";
+            for (int i = 0; i < N; i++)
+                for (int l = 0; l < dl[(size_t)y * N + i]; l++) s += "*x[" + std::to_string(i) + "]";
+        }
+        std::printf("dx[%d] = %s\n", gid, s.empty() ? "0" : s.c_str());
+    }
+}
+
+// Symbolic Jacobian (-v3; Simulation.cuh:149-228, printJac): entry [row][col]
+// sums, over the row species' net-stoichiometry terms, the derivative by the
+// column species with the reference's conventions -- a reactant of
+// stoichiometry 1 gives "+c*k[j]" times the other reactants once each, a
+// reactant of stoichiometry a > 1 gives "(c*a)*k[j]" (no explicit "+"),
+// x[col] a-1 times and the other reactants once each; a fed column prints 0.
+static void print_jacobian(const std::vector<int32_t> &dl, const std::vector<int32_t> &dr, int N,
+                           int R, const std::vector<double> &feed) {
+    for (int row = 0; row < N; row++) {
+        for (int col = 0; col < N; col++) {
+            if (feed[col] != 0) {
+                std::printf("dx[%d][%d] = 0\n", row, col);
+                continue;
+            }
+            std::string s;
+            for (int y = 0; y < R; y++) {
+                const int c = dr[(size_t)y * N + row] - dl[(size_t)y * N + row];
+                if (c == 0) continue;
+                const int a = dl[(size_t)y * N + col];
+                if (a < 1) continue;
+                std::string others;
+                for (int i = 0; i < N; i++)
+                    if (i != col && dl[(size_t)y * N + i] > 0)
+                        others += "*x[" + std::to_string(i) + "]";
+                if (a == 1) {
+                    s += (c > 0 ? "+" : "") + std::to_string(c) + "*k[" + std::to_string(y) + "]";
+                } else {
+                    s += std::to_string(c * a) + "*k[" + std::to_string(y) + "]";
+                    for (int l = 0; l < a - 1; l++) s += "*x[" + std::to_string(col) + "]";
+                }
+                s += others;
+            }
+            std::printf("dx[%d][%d] = %s\n", row, col, s.empty() ? "0" : s.c_str());
+        }
+    }
+}
+
 int main(int argc, char *argv[]) {
     const auto t_start = std::chrono::steady_clock::now();
     if (argc == 1) {
@@ -295,6 +352,18 @@ int main(int argc, char *argv[]) {
             dl[(size_t)j * N + s] = (int16_t)left[j][s];  // the reference stores shorts
             dr[(size_t)j * N + s] = (int16_t)right[j][s];
         }
+
+    // Simulation.cuh:430-447
+    if (verbose > 1) {
+        std::printf("\n%sODEs:\n", kStars);
+        print_odes(dl, dr, N, R, feed);
+        std::printf("%s\n\n", kStars);
+    }
+    if (verbose > 2) {
+        std::printf("\n%sJacobian:\n", kStars);
+        print_jacobian(dl, dr, N, R, feed);
+        std::printf("%s\n\n", kStars);
+    }
 
     // Simulation.cuh:451-465
     {

@@ -1134,7 +1134,6 @@ __device__ __noinline__ void lu_solve_fast(const float *M, int ld, int N, const 
     const int nblk = (N + 31) / 32;
     const bool mine = tid < N;
     const int prow = mine ? perm[tid] : 0;
-    const float *Mr = M + (int64_t)prow * ld;
     float acc = mine ? bvec[tid] : 0.f;
     float inv[32], seg[32];
     // forward: unit lower
@@ -2024,7 +2023,6 @@ __device__ void adjoint_instance(const LaunchParams &P, int id, unsigned char *s
     int *s_asptr = reinterpret_cast<int *>(smem + L.asptr);
     int *s_asent = reinterpret_cast<int *>(smem + L.asent);
     int *perm = reinterpret_cast<int *>(smem + L.perm);
-    int *slot = reinterpret_cast<int *>(smem + L.slot);
     float *bvec = reinterpret_cast<float *>(smem + L.bvec);
     float *lt = reinterpret_cast<float *>(smem + L.lt);
     float *utile = reinterpret_cast<float *>(smem + L.utile);
@@ -2382,7 +2380,7 @@ cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStrea
 // ran out.
 __global__ void __launch_bounds__(kThreads, 1) tc_selftest_kernel(const float *A, const float *B,
                                                                   float *D, int *status) {
-    extern __shared__ __align__(128) unsigned char smem[];
+    extern __shared__ __align__(16) unsigned char smem[];
     float *sAh = reinterpret_cast<float *>(smem);
     float *sAl = sAh + kTcM * kTcK;
     float *sBh = sAl + kTcM * kTcK;
@@ -2585,10 +2583,8 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
     constexpr int PB = LuShape<LT>::PB;
     __shared__ double red[2 * kWarps + 1];
     __shared__ int ired[kWarps + 2 + PB];
-    __shared__ int mv[4 * PB];
     const SmemLayout L(N, 1, 1, 1, (int)sizeof(LT), PB, 128);
     int *perm = reinterpret_cast<int *>(smem + L.perm);
-    int *slot = reinterpret_cast<int *>(smem + L.slot);
     LT *bvec = reinterpret_cast<LT *>(smem + L.bvec);
     LT *lt = reinterpret_cast<LT *>(smem + L.lt);
     LT *utile = reinterpret_cast<LT *>(smem + L.utile);

@@ -366,7 +366,7 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
             const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
             const int c = c0 + n;
             const bool inJ = c >= j0 && c < j0 + kWPB;
-            float v[4], h[4], l[4];
+            float h[4], l[4];
 #pragma unroll
             for (int b = 0; b < 4; b++) {
                 const int k = k4 + b;
@@ -375,7 +375,6 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
                     if (inJ) x = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : 0.f;
                     else x = W.PR[(int64_t)k * ld + c];
                 }
-                v[b] = x;
                 h[b] = tf32_hi(x);
                 l[b] = x - h[b];
             }

@@ -103,3 +103,23 @@ def test_torch_autograd(gpu):
         m.k = np.exp(logk.detach().numpy()[b])
     _, gk, _, _, _ = adjoint_batch(models, targets)
     assert np.allclose(logk.grad.numpy(), np.stack([gk[0], 2.0 * gk[1]]), rtol=1e-12, atol=0)
+
+
+def test_fit_rate_constants_reduces_the_misfit(gpu):
+    """The parameter-fit loop: from rate constants perturbed by exp(N(0, 0.3^2))
+    towards the ones that made the targets, Adam on the adjoint gradient
+    lowers the misfit, at least halving it within 30 iterations."""
+    from lassie_gb300.adjoint import fit_rate_constants
+    base, k_t = synth.make_c5(2)
+    models, targets = [], []
+    for q in range(2):
+        m = synth.shorten(base[q], 0.8, 9)
+        mt = synth.shorten(base[q], 0.8, 9)
+        mt.k = k_t[q]
+        tgt, _, rc = O.solve(mt)
+        assert rc == 0
+        models.append(m)
+        targets.append(tgt)
+    log_k, hist = fit_rate_constants(models, targets, iters=30, lr=0.05)
+    assert np.all(np.isfinite(hist))
+    assert min(hist) < 0.5 * hist[0] and hist[-1] < hist[0], (hist[0], min(hist), hist[-1])

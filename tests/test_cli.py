@@ -70,3 +70,34 @@ def test_output_folder_created(cli, tmp_path):
     (inp / "modelkind").write_text("banana\n")
     run(cli, str(inp), str(tmp_path / "newout"))
     assert os.path.isdir(tmp_path / "newout" / "output")
+
+
+def test_symbolic_odes_and_jacobian(cli, tmp_path):
+    """-v2/-v3 print the ODE system and the Jacobian before integrating,
+    in the reference's notation (Simulation.cuh:83-228): A + B -> 2C,
+    2C -> A, 0 -> B; species 1 fed in a second run (its ODE line is
+    omitted and its Jacobian column is 0)."""
+    import numpy as np
+    from lassie_gb300.model import Model
+    m = Model(left=np.array([[1, 1, 0], [0, 0, 2], [0, 0, 0]]),
+              right=np.array([[0, 0, 2], [1, 0, 0], [0, 1, 0]]),
+              k=np.array([0.5, 0.2, 0.1]), x0=np.array([1.0, 1.0, 0.0]), t=np.linspace(0, 1, 3))
+    write_folder(m, str(tmp_path / "in"))
+    r = subprocess.run([cli, str(tmp_path / "in"), str(tmp_path / "out"), "-v3"],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
+    lines = r.stdout.splitlines()
+    odes = [ln for ln in lines if ln.startswith("dx[") and "][" not in ln]
+    jac = [ln for ln in lines if ln.startswith("dx[") and "][" in ln]
+    assert odes == ["dx[0] = -1*k[0]*x[0]*x[1]+1*k[1]*x[2]*x[2]",
+                    "dx[1] = -1*k[0]*x[0]*x[1]+1*k[2]",
+                    "dx[2] = +2*k[0]*x[0]*x[1]-2*k[1]*x[2]*x[2]"]
+    assert jac == ["dx[0][0] = -1*k[0]*x[1]", "dx[0][1] = -1*k[0]*x[0]", "dx[0][2] = 2*k[1]*x[2]",
+                   "dx[1][0] = -1*k[0]*x[1]", "dx[1][1] = -1*k[0]*x[0]", "dx[1][2] = 0",
+                   "dx[2][0] = +2*k[0]*x[1]", "dx[2][1] = +2*k[0]*x[0]", "dx[2][2] = -4*k[1]*x[2]"]
+    m.feed = np.array([0.0, 1.0, 0.0])
+    write_folder(m, str(tmp_path / "fed"))
+    r = subprocess.run([cli, str(tmp_path / "fed"), str(tmp_path / "out2"), "-v3"],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=120)
+    lines = r.stdout.splitlines()
+    assert not any(ln.startswith("dx[1] =") for ln in lines)
+    assert "dx[0][1] = 0" in lines and "dx[2][1] = 0" in lines
