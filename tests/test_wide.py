@@ -98,3 +98,23 @@ def test_wide_networks_do_not_batch(gpu):
     with pytest.raises(nat.LassieError) as e:
         solver.simulate_batch([big, small], engine="mixed")
     assert e.value.status == nat.ERR_TOO_LARGE
+
+
+@pytest.mark.parametrize("tensor_cores", [False, True], ids=["fp32-pipes", "tensor-cores"])
+def test_wide_c3_full_horizon_conserves_total_amount(gpu, tensor_cores):
+    """The whole 4096-species workload (t in [0, 50], 100 samples) through
+    lassie_solve: every reaction turns 2 molecules into 2, so sum(x) is a
+    linear invariant of both step types (w^T M = w^T makes every Newton
+    correction conserve it, converged or not); it holds at every sample to
+    FP64 rounding over the ~6000 steps, and every species stays finite and
+    non-negative.  (A revert of negative species would break the invariant;
+    this trajectory has none.)"""
+    m = synth.make_c3()
+    out, st = solver.simulate(m, engine="mixed", deadline_s=600, root="sqrt",
+                              tensor_cores=tensor_cores)
+    assert st["status"] == 0 and st["nan_reverts"] == 0 and st["lu_failures"] == 0
+    assert st["be_steps"] > 1000
+    assert np.all(np.isfinite(out)) and np.all(out >= 0)
+    total = out.sum(axis=1)
+    assert np.all(np.abs(total - m.x0.sum()) <= 1e-10 * m.x0.sum()), \
+        float(np.max(np.abs(total - m.x0.sum())))
