@@ -2289,8 +2289,9 @@ __global__ void __launch_bounds__(kThreads, 1) wide_kernel(LaunchParams P) {
     if (threadIdx.x == 0) start = global_ns();
     __syncthreads();
     const uint64_t deadline = P.deadline_ns ? start + P.deadline_ns : 0;
-    // every wait on another CTA ends at the launch deadline, or after an hour
-    const uint64_t wlimit = deadline ? deadline : start + 3600ull * 1000000000ull;
+    // every wait on another CTA ends at the launch deadline (if any) or after
+    // kWideStallNs without progress
+    const uint64_t wlimit = deadline;
     const InstDesc &D0 = P.inst[0];
     const int N = D0.n;
     WideWs<LT> W = wide_ws<LT>(P.workspace, N, D0.r, D0.nnz_a);

@@ -153,15 +153,25 @@ __device__ __forceinline__ int ld_acquire_i(const int *p) {
     return v;
 }
 
+// A wait on another CTA that sees no progress for this long gives up (tasks
+// take milliseconds; the leader's longest serial phase, a fresh pivot
+// search, tens of milliseconds).
+constexpr uint64_t kWideStallNs = 60ull * 1000000000ull;
+
 // Thread 0 waits until *p >= target; false if the control block's abort flag
-// is set or the wall clock passes `limit` (then it sets the abort flag).
+// is set, the wait sees no progress for kWideStallNs, or the wall clock
+// passes `limit` (the launch deadline, 0 = none); it then sets the abort flag.
 __device__ bool wide_wait(const unsigned *p, unsigned target, WideCtl *ctl, uint64_t limit) {
     unsigned spins = 0;
+    const uint64_t t0 = global_ns();
     while (ld_acquire(p) < target) {
         if (ld_acquire_i(&ctl->abort)) return false;
-        if ((++spins & 255) == 0 && global_ns() > limit) {
-            atomicExch(&ctl->abort, 1);
-            return false;
+        if ((++spins & 255) == 0) {
+            const uint64_t now = global_ns();
+            if ((limit && now > limit) || now - t0 > kWideStallNs) {
+                atomicExch(&ctl->abort, 1);
+                return false;
+            }
         }
         __nanosleep(256);
     }
