@@ -205,7 +205,7 @@ def run_reference(args):
     return 0
 
 
-def rhs_bandwidth(torch, stream, n_inst=65536, reps=20):
+def rhs_bandwidth(torch, stream, n_inst=65536, reps=20, warm=3):
     """Batched RHS kernel on one 256-species network with n_inst
     parameterisations (x, k, dx each n_inst*256 doubles, larger than L2)."""
     import ctypes as C
@@ -226,7 +226,7 @@ def rhs_bandwidth(torch, stream, n_inst=65536, reps=20):
                                                    dx.data_ptr(), C.c_void_p(stream.cuda_stream)),
                                "lassie_rhs_device")
     with torch.cuda.stream(stream):
-        for _ in range(3):
+        for _ in range(warm):
             launch()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
@@ -240,6 +240,67 @@ def rhs_bandwidth(torch, stream, n_inst=65536, reps=20):
     alg = n_inst * (8 * R + 8 * N + 8 * N) + 4 * (R + 1 + n_a + N + 1 + n_h)
     return {"gbs": alg / (ms * 1e-3) / 1e9, "ms_per_launch": ms, "bytes_per_launch": alg,
             "network": "256 species x 256 reactions", "instances": n_inst}
+
+
+def newton_bandwidth(torch, stream, precision, n_inst=2048, reps=10, warm=3):
+    """Batched Newton-matrix kernel (I - h*J(x_b), dense row-major) on one
+    256-species network with n_inst parameterisations: 2048 x 256 x 256
+    outputs, 1.07 GB in FP64 or 0.54 GB in FP32 per launch (larger than L2).
+    Algorithmic bytes: the matrices written plus x and k read."""
+    import ctypes as C
+    from lassie_gb300 import synth, _native as nat
+    from lassie_gb300.solver import NativeModel
+    base, _ = synth.make_c5(1)
+    m = base[0]
+    nm = NativeModel.of(m)
+    N, R = m.n_species, m.n_reactions
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(1)
+    x = torch.rand((n_inst, N), dtype=torch.float64, device=dev, generator=g)
+    k = torch.rand((n_inst, R), dtype=torch.float64, device=dev, generator=g)
+    es = 8 if precision == 0 else 4
+    M = torch.empty((n_inst, N, N), dtype=torch.float64 if es == 8 else torch.float32, device=dev)
+    L = nat.load()
+    launch = lambda: nat.check(L.lassie_newton_matrix_device(  # noqa: E731
+        nm.handle, n_inst, 0.01, k.data_ptr(), x.data_ptr(), M.data_ptr(), precision,
+        C.c_void_p(stream.cuda_stream)), "lassie_newton_matrix_device")
+    with torch.cuda.stream(stream):
+        for _ in range(warm):
+            launch()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            launch()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nnz = C.c_int64(0)
+    nat.check(L.lassie_jacobian_nnz(nm.handle, C.byref(nnz)), "lassie_jacobian_nnz")
+    alg = n_inst * (es * N * N + 8 * (N + R))
+    return {"gbs": alg / (ms * 1e-3) / 1e9, "ms_per_launch": ms, "bytes_per_launch": alg,
+            "out": "fp64" if es == 8 else "fp32", "network": "256 species x 256 reactions",
+            "jacobian_nnz": int(nnz.value), "instances": n_inst}
+
+
+def run_kernels(args):
+    """Single-evaluation kernels alone (RHS and Newton matrix on device
+    buffers), with their HBM fractions; one JSON line.  Each kernel runs
+    --warmup untimed launches, then --steps timed ones."""
+    import torch
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    peaks, peak_kind = load_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    out = {"workload": "kernels", "peak_hbm_gbs": hbm, "peak_source": peak_kind}
+    reps, warm = max(1, args.steps), max(1, args.warmup)
+    out["rhs_hbm"] = rhs_bandwidth(torch, stream, reps=reps, warm=warm)
+    for prec, key in ((0, "newton_hbm_fp64"), (1, "newton_hbm_fp32")):
+        out[key] = newton_bandwidth(torch, stream, prec, reps=reps, warm=warm)
+    for key in ("rhs_hbm", "newton_hbm_fp64", "newton_hbm_fp32"):
+        out[key]["frac"] = out[key]["gbs"] / hbm
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def parity_table():
@@ -387,9 +448,10 @@ def main():
                          "make small profiling cases)")
     ap.add_argument("--max-steps", type=int, default=25000,
                     help="loop-iteration cap per instance (the same for every arm)")
-    ap.add_argument("--workload", default="c4", choices=["c4", "c3"],
+    ap.add_argument("--workload", default="c4", choices=["c4", "c3", "kernels"],
                     help="c4: the 2048-instance batch (default); c3: the 4096-species "
-                         "network on the wide engine (t in [0, 50], or --horizon)")
+                         "network on the wide engine (t in [0, 50], or --horizon); "
+                         "kernels: the RHS and Newton-matrix kernels alone")
     ap.add_argument("--tensor-cores", action="store_true",
                     help="c3: rank-32 updates of the factorisation on the tensor cores")
     ap.add_argument("--no-extras", action="store_true",
@@ -399,6 +461,8 @@ def main():
         return run_reference(args)
     if args.workload == "c3":
         return run_c3(args)
+    if args.workload == "kernels":
+        return run_kernels(args)
 
     import numpy as np
     import torch
@@ -534,6 +598,9 @@ def main():
         line["adjoint"] = adjoint_measure()
         line["rhs_hbm"] = rhs_bandwidth(torch, stream)
         line["rhs_hbm"]["frac"] = line["rhs_hbm"]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
+        for prec, key in ((0, "newton_hbm_fp64"), (1, "newton_hbm_fp32")):
+            line[key] = newton_bandwidth(torch, stream, prec)
+            line[key]["frac"] = line[key]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
         line["cpu_baseline"] = cpu_baseline(args.instances, max_steps=args.max_steps)
         line["cpu_baseline"].pop("seconds", None)
     if rank == 0:

@@ -249,6 +249,20 @@ int lassie_rhs(const lassie_model *model, const double *k, const double *x,
    createJac semantics (kernels.cuh:205-271, 393-402). */
 int lassie_newton_matrix(const lassie_model *model, const double *k,
                          const double *x, double h, double *M);
+/* M_b = I - h*J(x_b) for n_inst parameterisations of one network, device
+   buffers, instance-major: k [n_inst][R], x [n_inst][N], M [n_inst][N][N]
+   row-major, FP64 (precision LASSIE_PREC_FP64) or FP32 (LASSIE_PREC_MIXED,
+   the entries rounded once from their FP64 value).  Same entries as
+   lassie_newton_matrix.  Replaces the Newton-matrix launches of the
+   backward-Euler step, createJac + aggiorna_Jacobiano1 + transposteJacobian
+   (Simulation.cuh:828-862; kernels.cuh:206-287, 394-402), for many
+   instances at once.  Requires N + R <= 20480. */
+int lassie_newton_matrix_device(const lassie_model *model, int32_t n_inst, double h,
+                                const double *k, const double *x, void *M,
+                                int32_t precision, void *stream);
+/* Structural nonzeros of J (entries createJac fills); builds and uploads the
+   pattern the batched Newton-matrix call uses. */
+int lassie_jacobian_nnz(const lassie_model *model, int64_t *nnz);
 /* Factor a row-major n x n matrix with the engine's LU (precision as in
    lassie_opts) and solve A x = b; returns 1 + column of the first exactly
    zero pivot when singular.  Replaces linearSolverLU (Simulation.cuh:1280). */

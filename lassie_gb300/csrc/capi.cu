@@ -26,12 +26,15 @@ int64_t wide_dynamic_smem(int N, int precision);
 int wide_configure(int precision, int64_t smem, int sm_count);
 cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
 cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, int nnz_h, const int *rptr,
-                             const int *rent, const int *sptr, const int *sent,
+                             const int *rent, const int *sptr, const int *sent, const int *order,
                              const double *k, const double *x, double *dx, int sm_count,
                              cudaStream_t stream);
 cudaError_t newton_matrix_launch(int N, int R, int nnz_a, const int *rptr, const int *rent,
                                  const int *sptr, const int *sent, const double *k,
                                  const double *x, double h, double *M, cudaStream_t stream);
+cudaError_t newton_batch_launch(int n_inst, int N, int R, const int *rptr, const int *rent,
+                                const int *jac, int64_t nnz, const double *k, const double *x,
+                                double h, void *M, bool fp32, int sm_count, cudaStream_t stream);
 cudaError_t lu_solve_launch(int N, void *A, int ld, const double *b, double *x, int *info,
                             int precision, cudaStream_t stream);
 int64_t lu_solve_smem(int N, int precision);
@@ -70,6 +73,13 @@ struct lassie_model {
     std::mutex mu;
     int dev = -1;
     int32_t *d_struct = nullptr;  // [rxn_ptr | rxn_ent | sp_ptr | sp_ent]
+    // structural nonzeros of J and their terms (model_jac_device), built on
+    // the first batched Newton-matrix call
+    int32_t *d_jac = nullptr;
+    int64_t jac_nnz = 0;
+    // reactions, then species, in descending order of their loop trip counts
+    // in the batched RHS (model_order_device)
+    int32_t *d_order = nullptr;
 
     int64_t off_rent() const { return R + 1; }
     int64_t off_sptr() const { return off_rent() + (int64_t)rxn_ent.size(); }
@@ -197,6 +207,8 @@ extern "C" void lassie_model_destroy(lassie_model *m) {
         cudaGetDevice(&cur);
         cudaSetDevice(m->dev);
         cudaFree(m->d_struct);
+        if (m->d_jac) cudaFree(m->d_jac);
+        if (m->d_order) cudaFree(m->d_order);
         cudaSetDevice(cur);
     }
     delete m;
@@ -795,22 +807,56 @@ extern "C" int lassie_adjoint_batch(const lassie_instance *inst, int32_t n,
 
 // ---------------------------------------------------- single evaluations
 
+// Work order of the batched RHS: reactions by their number of reactants,
+// species by the work of their sums (an entry of coefficient +-1 is one
+// addition, any other a product over the reaction's reactants), both
+// descending and stable, so that the lanes of a warp run loops of equal
+// length.  [reactions R | species N], uploaded once per model.
+static int model_order_device(lassie_model *m, const int32_t **d) {
+    std::lock_guard<std::mutex> g(m->mu);
+    if (m->d_order) {
+        *d = m->d_order;
+        return LASSIE_OK;
+    }
+    std::vector<int32_t> rord(m->R), sord(m->N);
+    std::vector<int64_t> rw(m->R), sw(m->N, 0);
+    for (int y = 0; y < m->R; y++) rw[y] = m->rxn_ptr[y + 1] - m->rxn_ptr[y];
+    for (int s = 0; s < m->N; s++)
+        for (int e = m->sp_ptr[s]; e < m->sp_ptr[s + 1]; e++) {
+            const int c = ent_coef(m->sp_ent[e]);
+            sw[s] += (c == 1 || c == -1) ? 1 : 2 + rw[ent_index(m->sp_ent[e])];
+        }
+    std::iota(rord.begin(), rord.end(), 0);
+    std::iota(sord.begin(), sord.end(), 0);
+    std::stable_sort(rord.begin(), rord.end(), [&](int a, int b) { return rw[a] > rw[b]; });
+    std::stable_sort(sord.begin(), sord.end(), [&](int a, int b) { return sw[a] > sw[b]; });
+    rord.insert(rord.end(), sord.begin(), sord.end());
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (m->d_struct && m->dev != dev)
+        return set_error(LASSIE_ERR_ARGS, "model already bound to another device");
+    CU(cudaMalloc(&m->d_order, rord.size() * sizeof(int32_t)));
+    CU(cudaMemcpy(m->d_order, rord.data(), rord.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    *d = m->d_order;
+    return LASSIE_OK;
+}
+
 extern "C" int lassie_rhs_device(const lassie_model *cm, int32_t n_inst, const double *k,
                                  const double *x, double *dx, void *stream) {
     lassie_model *m = const_cast<lassie_model *>(cm);
     if (!m || n_inst < 0 || (n_inst > 0 && (!k || !x || !dx)))
         return set_error(LASSIE_ERR_ARGS, "rhs_device");
     if (n_inst == 0) return LASSIE_OK;
-    const int32_t *d = nullptr;
+    const int32_t *d = nullptr, *dord = nullptr;
     int rc = model_device(m, &d);
+    if (!rc) rc = model_order_device(m, &dord);
     if (rc) return rc;
     int dev = 0, sms = 0;
     CU(cudaGetDevice(&dev));
     CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CU(rhs_batch_launch(n_inst, m->N, m->R, (int)m->rxn_ent.size(), (int)m->sp_ent.size(), d,
-                        d + m->off_rent(),
-                        d + m->off_sptr(), d + m->off_sent(), k, x, dx, sms,
-                        (cudaStream_t)stream));
+                        d + m->off_rent(), d + m->off_sptr(), d + m->off_sent(), dord, k, x, dx,
+                        sms, (cudaStream_t)stream));
     return LASSIE_OK;
 }
 
@@ -859,6 +905,104 @@ extern "C" int lassie_newton_matrix(const lassie_model *cm, const double *k, con
     cudaFree(dxv);
     cudaFree(dM);
     return rc;
+}
+
+// Structural nonzeros of J: column g is in row i when some reaction with net
+// stoichiometry in species i has g among its reactants (the entries
+// createJac fills, kernels.cuh:219-271).  Per row the columns ascend; per
+// nonzero (i,g) the terms are the reactions of row i, in ascending order,
+// that have g among their reactants: (make_ent(reaction, net coefficient),
+// coefficient of g).  Layout [jptr N+1 | jcol | jrow | tptr nnz+1 | pad to
+// 8 bytes | terms as int pairs], uploaded once per model.
+static int model_jac_device(lassie_model *m, const int32_t **d) {
+    std::lock_guard<std::mutex> g(m->mu);
+    if (m->d_jac) {
+        *d = m->d_jac;
+        return LASSIE_OK;
+    }
+    const int N = m->N;
+    std::vector<int32_t> ptr(N + 1), col, row, tptr, tent;
+    std::vector<int32_t> mark(N, -1);
+    for (int i = 0; i < N; i++) {
+        ptr[i] = (int32_t)col.size();
+        const size_t first = col.size();
+        for (int e = m->sp_ptr[i]; e < m->sp_ptr[i + 1]; e++) {
+            const int y = ent_index(m->sp_ent[e]);
+            for (int q = m->rxn_ptr[y]; q < m->rxn_ptr[y + 1]; q++) {
+                const int gcol = ent_index(m->rxn_ent[q]);
+                if (mark[gcol] != i) {
+                    mark[gcol] = i;
+                    col.push_back(gcol);
+                }
+            }
+        }
+        std::sort(col.begin() + first, col.end());
+        for (size_t p = first; p < col.size(); p++) {
+            row.push_back(i);
+            tptr.push_back((int32_t)(tent.size() / 2));
+            for (int e = m->sp_ptr[i]; e < m->sp_ptr[i + 1]; e++) {
+                const int y = ent_index(m->sp_ent[e]);
+                for (int q = m->rxn_ptr[y]; q < m->rxn_ptr[y + 1]; q++) {
+                    if (ent_index(m->rxn_ent[q]) != col[p]) continue;
+                    const int a = ent_coef(m->rxn_ent[q]);
+                    if (a > 0) {
+                        tent.push_back(m->sp_ent[e]);
+                        tent.push_back(a);
+                    }
+                    break;
+                }
+            }
+        }
+    }
+    ptr[N] = (int32_t)col.size();
+    tptr.push_back((int32_t)(tent.size() / 2));
+    std::vector<int32_t> h(ptr);
+    h.insert(h.end(), col.begin(), col.end());
+    h.insert(h.end(), row.begin(), row.end());
+    h.insert(h.end(), tptr.begin(), tptr.end());
+    if (h.size() & 1) h.push_back(0);
+    h.insert(h.end(), tent.begin(), tent.end());
+    int dev = 0;
+    CU(cudaGetDevice(&dev));
+    if (m->d_struct && m->dev != dev)
+        return set_error(LASSIE_ERR_ARGS, "model already bound to another device");
+    CU(cudaMalloc(&m->d_jac, h.size() * sizeof(int32_t)));
+    CU(cudaMemcpy(m->d_jac, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    m->jac_nnz = (int64_t)col.size();
+    *d = m->d_jac;
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_newton_matrix_device(const lassie_model *cm, int32_t n_inst, double h,
+                                           const double *k, const double *x, void *M,
+                                           int32_t precision, void *stream) {
+    lassie_model *m = const_cast<lassie_model *>(cm);
+    if (!m || n_inst < 0 || (n_inst > 0 && (!k || !x || !M)) ||
+        (precision != LASSIE_PREC_FP64 && precision != LASSIE_PREC_MIXED))
+        return set_error(LASSIE_ERR_ARGS, "newton_matrix_device");
+    if (int64_t(m->N + m->R) * 8 > 160 * 1024)
+        return set_error(LASSIE_ERR_TOO_LARGE, "newton_matrix_device: N + R above 20480");
+    if (n_inst == 0) return LASSIE_OK;
+    const int32_t *d = nullptr, *dj = nullptr;
+    int rc = model_device(m, &d);
+    if (!rc) rc = model_jac_device(m, &dj);
+    if (rc) return rc;
+    int dev = 0, sms = 0;
+    CU(cudaGetDevice(&dev));
+    CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CU(newton_batch_launch(n_inst, m->N, m->R, d, d + m->off_rent(), dj, m->jac_nnz, k, x, h, M,
+                           precision == LASSIE_PREC_MIXED, sms, (cudaStream_t)stream));
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_jacobian_nnz(const lassie_model *cm, int64_t *nnz) {
+    lassie_model *m = const_cast<lassie_model *>(cm);
+    if (!m || !nnz) return set_error(LASSIE_ERR_ARGS, "jacobian_nnz");
+    const int32_t *dj = nullptr;
+    int rc = model_jac_device(m, &dj);
+    if (rc) return rc;
+    *nnz = m->jac_nnz;
+    return LASSIE_OK;
 }
 
 extern "C" int lassie_lu_solve(int32_t n, const double *a, const double *b, double *x,

@@ -211,22 +211,37 @@ __device__ __forceinline__ void rhs_rates(const Net &m, const double *x, double 
     }
 }
 
+// The sum starts from its first term instead of 0.0 + term, and a -1 entry
+// subtracts (acc - r is acc + (-r) in IEEE arithmetic), so each entry costs
+// one FP64 addition.  Only an all-zero sum can differ, in its sign (0.0 +
+// -0.0 is +0.0, and no other partial sum is -0.0 in round-to-nearest): the
+// last line restores it.
 __device__ __forceinline__ double rhs_species_r(const Net &m, int i, const double *pw,
                                                 const double *rate) {
-    double acc = 0.0;
     const int e0 = m.sptr[i], e1 = m.sptr[i + 1];
-    for (int e = e0; e < e1; e++) {
+    if (e0 == e1) return 0.0;
+    auto scaled = [&](int y, int c) {
+        double v = (double)c * m.kk[y];
+        for (int q = m.rptr[y]; q < m.rptr[y + 1]; q++) v = v * pw[q];
+        return v;
+    };
+    double acc;
+    {
+        const int ent = m.sent[e0];
+        const int y = ent_index(ent), c = ent_coef(ent);
+        acc = c == 1 ? rate[y]
+                     : (c == -1 ? __longlong_as_double(__double_as_longlong(rate[y]) ^
+                                                       (long long)0x8000000000000000ull)
+                                : scaled(y, c));
+    }
+    for (int e = e0 + 1; e < e1; e++) {
         const int ent = m.sent[e];
         const int y = ent_index(ent), c = ent_coef(ent);
-        double v;
-        if (c == 1) v = rate[y];
-        else if (c == -1) v = -rate[y];
-        else {
-            v = (double)c * m.kk[y];
-            for (int q = m.rptr[y]; q < m.rptr[y + 1]; q++) v = v * pw[q];
-        }
-        acc = acc + v;
+        if (c == 1) acc = acc + rate[y];
+        else if (c == -1) acc = acc - rate[y];
+        else acc = acc + scaled(y, c);
     }
+    if (__double_as_longlong(acc) == (long long)0x8000000000000000ull) acc = 0.0;
     return acc;
 }
 
@@ -2437,9 +2452,19 @@ extern "C" int lassie_tc_selftest(const float *dA, const float *dB, float *dD, i
 
 // dx = f(x) for a batch of parameterisations of one network: one warp per
 // instance (no CTA barrier on the data path).  The network structure is
-// staged once per CTA; each warp copies its instance's x and k into its own
-// shared-memory slice with 16-byte loads, forms the reactant powers, then the
-// species sums in the oracle's order (rhs_species), and stores dx coalesced.
+// staged once per CTA; each warp copies its instance's x into its own
+// shared-memory slice with 16-byte loads, forms the reaction rates (k read
+// coalesced), then the species sums in the oracle's order (rhs_species), and
+// stores dx.  On GB300 the FP64 pipe (about two operations per clock per SM),
+// not HBM, bounds this kernel: one product per reactant and one sum per
+// net-stoichiometry entry against 24 bytes per species.  So the kernel keeps
+// that pipe's instruction count at the useful work:
+// - lanes take reactions and species in the host's order of their trip
+//   counts (rord, sord), so the 32 lanes of a warp run loops of equal length;
+// - a species sum starts from its first term rather than 0.0 + term.  The
+//   two differ only in the sign of an all-zero sum (0.0 + -0.0 is +0.0, and
+//   no other partial sum can be -0.0 in round-to-nearest), which the final
+//   line restores.
 constexpr int kRhsThreads = 256;
 constexpr int kRhsWarps = kRhsThreads / 32;
 
@@ -2454,72 +2479,100 @@ __device__ __forceinline__ void warp_copy_f64(double *dst, const double *src, in
     }
 }
 
+// Net-stoichiometry term c * k * prod(x^a) of entry `ent` when |c| != 1 (the
+// oracle's per-entry product order).
+__device__ __forceinline__ double rhs_term_scaled(int y, int c, const int *rptr, const int *rent,
+                                                  const double *kb, const double *xs) {
+    double v = (double)c * __ldg(kb + y);
+    for (int q = rptr[y]; q < rptr[y + 1]; q++) {
+        const int eq = rent[q];
+        v = v * mypow(xs[ent_index(eq)], ent_coef(eq));
+    }
+    return v;
+}
+
+__device__ __forceinline__ double neg_bits(double v) {
+    return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+}
+
 __global__ void __launch_bounds__(kRhsThreads) rhs_batch_kernel(
     int n_inst, int N, int R, int nnz_a, int nnz_h, const int *__restrict__ rptr_g,
     const int *__restrict__ rent_g, const int *__restrict__ sptr_g, const int *__restrict__ sent_g,
-    const double *__restrict__ k, const double *__restrict__ x, double *__restrict__ dx) {
+    const int *__restrict__ order_g, const double *__restrict__ k, const double *__restrict__ x,
+    double *__restrict__ dx) {
     extern __shared__ __align__(16) unsigned char smem[];
     int *rptr = reinterpret_cast<int *>(smem);
     int *sptr = rptr + (R + 1);
     int *rent = sptr + (N + 1);
     int *sent = rent + (nnz_a > 0 ? nnz_a : 1);
-    const int64_t ints = (int64_t)(R + 1) + (N + 1) + (nnz_a > 0 ? nnz_a : 1) + (nnz_h > 0 ? nnz_h : 1);
+    int *rord = sent + (nnz_h > 0 ? nnz_h : 1);
+    int *sord = rord + R;
+    const int64_t ints = (int64_t)(R + 1) + (N + 1) + (nnz_a > 0 ? nnz_a : 1) +
+                         (nnz_h > 0 ? nnz_h : 1) + R + N;
     double *wbase = reinterpret_cast<double *>(smem + ((ints * 4 + 15) & ~int64_t(15)));
-    const int per_warp = ((N + 1) & ~1) + 2 * ((R + 1) & ~1) + ((nnz_a + 1) & ~1);
+    const int per_warp = ((N + 1) & ~1) + ((R + 1) & ~1);
     for (int j = threadIdx.x; j <= R; j += kRhsThreads) rptr[j] = rptr_g[j];
     for (int j = threadIdx.x; j <= N; j += kRhsThreads) sptr[j] = sptr_g[j];
     for (int j = threadIdx.x; j < nnz_a; j += kRhsThreads) rent[j] = rent_g[j];
     for (int j = threadIdx.x; j < nnz_h; j += kRhsThreads) sent[j] = sent_g[j];
+    for (int j = threadIdx.x; j < R + N; j += kRhsThreads) rord[j] = order_g[j];
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double *xs = wbase + (int64_t)warp * per_warp;
-    double *kk = xs + ((N + 1) & ~1);
-    double *rate = kk + ((R + 1) & ~1);
-    double *pw = rate + ((R + 1) & ~1);
+    double *rate = xs + ((N + 1) & ~1);
     for (int b = blockIdx.x * kRhsWarps + warp; b < n_inst; b += gridDim.x * kRhsWarps) {
         warp_copy_f64(xs, x + (int64_t)b * N, N);
-        warp_copy_f64(kk, k + (int64_t)b * R, R);
         __syncwarp();
+        const double *kb = k + (int64_t)b * R;
         // reaction products once per reaction (rhs_rates), then the species
         // sums (rhs_species_r): bit-identical to the per-entry products
-        for (int y = lane; y < R; y += 32) {
-            double r = kk[y];
+        for (int t = lane; t < R; t += 32) {
+            const int y = rord[t];
+            double r = __ldg(kb + y);
             for (int q = rptr[y]; q < rptr[y + 1]; q++) {
                 const int e = rent[q];
-                const double p = mypow(xs[ent_index(e)], ent_coef(e));
-                pw[q] = p;
-                r = r * p;
+                r = r * mypow(xs[ent_index(e)], ent_coef(e));
             }
             rate[y] = r;
         }
         __syncwarp();
         double *db = dx + (int64_t)b * N;
-        for (int s = lane; s < N; s += 32) {
+        for (int t = lane; t < N; t += 32) {
+            const int s = sord[t];
+            const int e0 = sptr[s], e1 = sptr[s + 1];
             double acc = 0.0;
-            for (int e = sptr[s]; e < sptr[s + 1]; e++) {
-                const int ent = sent[e];
-                const int y = ent_index(ent), c = ent_coef(ent);
-                double v;
-                if (c == 1) v = rate[y];
-                else if (c == -1) v = -rate[y];
-                else {
-                    v = (double)c * kk[y];
-                    for (int q = rptr[y]; q < rptr[y + 1]; q++) v = v * pw[q];
+            if (e0 < e1) {
+                // acc - r is acc + (-r) in IEEE arithmetic: one addition per
+                // entry, and a sign flip (integer) for a leading -r
+                {
+                    const int ent = sent[e0];
+                    const int y = ent_index(ent), c = ent_coef(ent);
+                    acc = c == 1 ? rate[y]
+                                 : (c == -1 ? neg_bits(rate[y])
+                                            : rhs_term_scaled(y, c, rptr, rent, kb, xs));
                 }
-                acc = acc + v;
+                for (int e = e0 + 1; e < e1; e++) {
+                    const int ent = sent[e];
+                    const int y = ent_index(ent), c = ent_coef(ent);
+                    if (c == 1) acc = acc + rate[y];
+                    else if (c == -1) acc = acc - rate[y];
+                    else acc = acc + rhs_term_scaled(y, c, rptr, rent, kb, xs);
+                }
+                if (__double_as_longlong(acc) == (long long)0x8000000000000000ull) acc = 0.0;
             }
-            __stcs(db + s, acc);
+            db[s] = acc;
         }
         __syncwarp();
     }
 }
 
 cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, int nnz_h, const int *rptr,
-                             const int *rent, const int *sptr, const int *sent,
+                             const int *rent, const int *sptr, const int *sent, const int *order,
                              const double *k, const double *x, double *dx, int sm_count,
                              cudaStream_t stream) {
-    const int64_t ints = (int64_t)(R + 1) + (N + 1) + (nnz_a > 0 ? nnz_a : 1) + (nnz_h > 0 ? nnz_h : 1);
-    const int64_t per_warp = ((N + 1) & ~1) + 2 * ((R + 1) & ~1) + ((nnz_a + 1) & ~1);
+    const int64_t ints = (int64_t)(R + 1) + (N + 1) + (nnz_a > 0 ? nnz_a : 1) +
+                         (nnz_h > 0 ? nnz_h : 1) + R + N;
+    const int64_t per_warp = ((N + 1) & ~1) + ((R + 1) & ~1);
     const int64_t smem = ((ints * 4 + 15) & ~int64_t(15)) + per_warp * 8 * kRhsWarps;
     if (smem > 200 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(rhs_batch_kernel,
@@ -2533,7 +2586,7 @@ cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, int nnz_h, con
     const int64_t want = ((int64_t)n_inst + kRhsWarps - 1) / kRhsWarps;
     const int grid = (int)std::min<int64_t>(want, (int64_t)sm_count * per_sm);
     rhs_batch_kernel<<<grid, kRhsThreads, smem, stream>>>(n_inst, N, R, nnz_a, nnz_h, rptr, rent,
-                                                          sptr, sent, k, x, dx);
+                                                          sptr, sent, order, k, x, dx);
     return cudaGetLastError();
 }
 
@@ -2573,6 +2626,142 @@ cudaError_t newton_matrix_launch(int N, int R, int nnz_a, const int *rptr, const
     newton_matrix_kernel<<<1, kThreads, smem, stream>>>(N, R, nnz_a, rptr, rent, sptr, sent, k,
                                                        x, h, M);
     return cudaGetLastError();
+}
+
+// M_b = I - h*J(x_b) for a batch of parameterisations of one network, dense
+// row-major, FP64 or FP32 (the matrix the mixed form factors).  The output is
+// n_inst*N*N elements against (N+R) doubles read per instance, so the kernel
+// is bound by HBM writes.  Each CTA stages its instance's x and k
+// in shared memory.  Work units are (instance, chunk of kJacChunk rows): the
+// warps write the chunk's identity/zero rows with 16-byte streaming stores,
+// then all threads of the CTA compute the chunk's structural nonzeros (one
+// per thread) and patch them while those lines are still in L2.  The nonzero pattern comes
+// from the host: jptr/jcol/jrow (columns ascending in each row) and, per
+// nonzero (i,g), the reactions of H row i in ascending order that have g
+// among their reactants (tptr/tent: reaction and net coefficient, then the
+// reactant coefficient of g).  Each contributes createJac's term
+// (kernels.cuh:219-271): s*k [*a*x_g^(a-1)] * (each other reactant once), so
+// the entries are the ones assemble_newton_matrix writes, bit for bit.
+constexpr int kJacThreads = 256;
+constexpr int kJacWarps = kJacThreads / 32;
+constexpr int kJacChunk = 64;
+
+template <typename OT>
+__device__ __forceinline__ void warp_identity_row(OT *row, int N, int diag) {
+    constexpr int V = 16 / (int)sizeof(OT);
+    const int lane = threadIdx.x & 31;
+    int head = (int)((((uintptr_t)0 - (uintptr_t)row) & 15) / sizeof(OT));
+    if (head > N) head = N;
+    for (int c = lane; c < head; c += 32) __stcs(row + c, c == diag ? OT(1) : OT(0));
+    const int nv = (N - head) / V;
+    OT *body = row + head;
+    const int dv = diag - head;  // diagonal position inside the body
+    for (int v = lane; v < nv; v += 32) {
+        const int c0 = v * V;
+        if constexpr (V == 2) {
+            double2 w = make_double2(c0 == dv ? 1.0 : 0.0, c0 + 1 == dv ? 1.0 : 0.0);
+            __stcs(reinterpret_cast<double2 *>(body) + v, w);
+        } else {
+            float4 w = make_float4(c0 == dv ? 1.f : 0.f, c0 + 1 == dv ? 1.f : 0.f,
+                                   c0 + 2 == dv ? 1.f : 0.f, c0 + 3 == dv ? 1.f : 0.f);
+            __stcs(reinterpret_cast<float4 *>(body) + v, w);
+        }
+    }
+    for (int c = head + nv * V + lane; c < N; c += 32) __stcs(row + c, c == diag ? OT(1) : OT(0));
+}
+
+struct JacPattern {
+    const int *jptr, *jcol, *jrow, *tptr;
+    const int2 *tent;  // (make_ent(reaction, net coefficient), coefficient of g)
+};
+
+// createJac's entry (i,g) without the identity, same operations in the same
+// order as assemble_newton_matrix (non-exact form).
+__device__ __forceinline__ double jac_entry(const int *__restrict__ rptr,
+                                            const int *__restrict__ rent, const JacPattern &P,
+                                            const double *kk, const double *x, int p, int g) {
+    double J = 0.0;
+    for (int t = __ldg(P.tptr + p), te = __ldg(P.tptr + p + 1); t < te; t++) {
+        const int2 tt = __ldg(P.tent + t);
+        const int y2 = ent_index(tt.x), s2 = ent_coef(tt.x), a = tt.y;
+        double temp = 0.0;
+        if (a == 1) temp = temp + (double)s2 * kk[y2];
+        else temp = temp + (double)s2 * kk[y2] * (double)a * mypow(x[g], a - 1);
+        for (int q2 = __ldg(rptr + y2), en2 = __ldg(rptr + y2 + 1); q2 < en2; q2++) {
+            const int o = ent_index(__ldg(rent + q2));
+            if (o != g) temp = temp * x[o];
+        }
+        J = J + temp;
+    }
+    return J;
+}
+
+template <typename OT>
+__global__ void __launch_bounds__(kJacThreads) newton_batch_kernel(
+    int n_inst, int N, int R, const int *__restrict__ rptr, const int *__restrict__ rent,
+    JacPattern P, const double *__restrict__ k, const double *__restrict__ x, double h,
+    OT *__restrict__ M) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *xs = reinterpret_cast<double *>(smem);
+    double *kk = xs + N;
+    const int warp = threadIdx.x >> 5;
+    // work units (instance, chunk of rows); each CTA takes a contiguous range
+    // of them, so it restages x and k only when the instance changes
+    const int nchunk = (N + kJacChunk - 1) / kJacChunk;
+    const int64_t units = (int64_t)n_inst * nchunk;
+    const int64_t u0 = units * blockIdx.x / gridDim.x, u1 = units * (blockIdx.x + 1) / gridDim.x;
+    int staged = -1;
+    for (int64_t u = u0; u < u1; u++) {
+        const int b = (int)(u / nchunk), r0 = (int)(u % nchunk) * kJacChunk;
+        const int r1 = min(N, r0 + kJacChunk);
+        if (b != staged) {  // uniform across the CTA
+            __syncthreads();  // the previous instance's patches are done with xs/kk
+            for (int s = threadIdx.x; s < N; s += kJacThreads) xs[s] = __ldcs(x + (int64_t)b * N + s);
+            for (int j = threadIdx.x; j < R; j += kJacThreads) kk[j] = __ldcs(k + (int64_t)b * R + j);
+            staged = b;
+        }
+        OT *Mb = M + (int64_t)b * N * N;
+        for (int i = r0 + warp; i < r1; i += kJacWarps)
+            warp_identity_row<OT>(Mb + (int64_t)i * N, N, i);
+        __syncthreads();  // rows written, xs/kk staged
+        for (int p = __ldg(P.jptr + r0) + threadIdx.x, pe = __ldg(P.jptr + r1); p < pe;
+             p += kJacThreads) {
+            const int i = __ldg(P.jrow + p), g = __ldg(P.jcol + p);
+            const double J = jac_entry(rptr, rent, P, kk, xs, p, g);
+            const double I = (i == g) ? 1.0 : 0.0;
+            Mb[(int64_t)i * N + g] = (OT)(I - h * J);
+        }
+    }
+}
+
+cudaError_t newton_batch_launch(int n_inst, int N, int R, const int *rptr, const int *rent,
+                                const int *jac, int64_t nnz, const double *k, const double *x,
+                                double h, void *M, bool fp32, int sm_count, cudaStream_t stream) {
+    const int64_t smem = int64_t(N + R) * 8;
+    if (smem > 160 * 1024) return cudaErrorInvalidValue;
+    // jac = [jptr N+1 | jcol nnz | jrow nnz | tptr nnz+1 | pad to 8 bytes | tent]
+    JacPattern P;
+    P.jptr = jac;
+    P.jcol = P.jptr + N + 1;
+    P.jrow = P.jcol + nnz;
+    P.tptr = P.jrow + nnz;
+    const int64_t ints = (int64_t)N + 1 + 2 * nnz + nnz + 1;
+    P.tent = reinterpret_cast<const int2 *>(jac + ((ints + 1) & ~int64_t(1)));
+    auto launch = [&](auto kern, auto *out) -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kJacThreads, (size_t)smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+        const int64_t units = (int64_t)n_inst * ((N + kJacChunk - 1) / kJacChunk);
+        const int grid = (int)std::min<int64_t>(units, (int64_t)sm_count * per_sm);
+        kern<<<grid, kJacThreads, smem, stream>>>(n_inst, N, R, rptr, rent, P, k, x, h, out);
+        return cudaGetLastError();
+    };
+    if (fp32) return launch(newton_batch_kernel<float>, static_cast<float *>(M));
+    return launch(newton_batch_kernel<double>, static_cast<double *>(M));
 }
 
 // Factor + solve one dense system with the engine's LU (tests).

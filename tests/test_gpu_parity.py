@@ -61,6 +61,63 @@ def test_newton_matrix_bit_exact(gpu, name, m):
     assert np.array_equal(solver.newton_matrix(m, x, h), M_ref)
 
 
+def _newton_batch_cases():
+    base, _ = synth.make_c5(1)
+    yield "c5-256", base[0], 300
+    yield "sized-37", synth.make_sized(37, 0), 64
+    yield "sized-601", synth.make_sized(601, 1), 3
+    for kind in ("decay", "dimer", "bimolecular", "reversible"):
+        yield kind, synth.tiny_network(kind), 5
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "fp32"])
+@pytest.mark.parametrize("name,m,n_inst", list(_newton_batch_cases()),
+                         ids=[c[0] for c in _newton_batch_cases()])
+def test_newton_matrix_device_batch_bit_exact(gpu, name, m, n_inst, precision):
+    """lassie_newton_matrix_device: I - h*J(x_b) for every parameterisation
+    equals the oracle's Jacobian formed in FP64 (FP32 output: that matrix
+    rounded once).  Odd N covers the unaligned row heads and tails."""
+    torch = pytest.importorskip("torch")
+    from lassie_gb300 import _native as nat
+    nm = solver.NativeModel.of(m)
+    om = O.OracleModel(m.left, m.right)
+    N, R = m.n_species, m.n_reactions
+    rng = np.random.default_rng(N + n_inst)
+    x = rng.uniform(0, 2, (n_inst, N))
+    k = 10.0 ** rng.uniform(-3, 3, (n_inst, R))
+    h = 0.0123
+    dt = torch.float64 if precision == 0 else torch.float32
+    M_t = torch.full((n_inst, N, N), float("nan"), dtype=dt, device="cuda")
+    x_t, k_t = torch.tensor(x, device="cuda"), torch.tensor(k, device="cuda")
+    nat.check(nat.load().lassie_newton_matrix_device(nm.handle, n_inst, h, k_t.data_ptr(),
+                                                     x_t.data_ptr(), M_t.data_ptr(),
+                                                     precision, None),
+              "lassie_newton_matrix_device")
+    torch.cuda.synchronize()
+    M = M_t.cpu().numpy()
+    for b in sorted({0, n_inst // 2, n_inst - 1}):
+        ref = np.eye(N) - h * om.jacobian(k[b], x[b])
+        if precision == 1:
+            ref = ref.astype(np.float32)
+        assert np.array_equal(M[b], ref), (name, b)
+
+
+def test_newton_matrix_device_empty_and_args(gpu):
+    from lassie_gb300 import _native as nat
+    m = synth.tiny_network("dimer")
+    nm = solver.NativeModel.of(m)
+    L = nat.load()
+    assert L.lassie_newton_matrix_device(nm.handle, 0, 0.1, None, None, None, 0, None) == 0
+    assert L.lassie_newton_matrix_device(nm.handle, 1, 0.1, None, None, None, 0, None) == -20
+    assert L.lassie_newton_matrix_device(nm.handle, 0, 0.1, None, None, None, 7, None) == -20
+    import ctypes as C
+    nnz = C.c_int64(0)
+    assert L.lassie_jacobian_nnz(nm.handle, C.byref(nnz)) == 0
+    om = O.OracleModel(m.left, m.right)
+    J = om.jacobian(m.k, np.full(m.n_species, 0.7))
+    assert nnz.value >= int(np.count_nonzero(J))
+
+
 @pytest.mark.parametrize("n", [1, 5, 31, 32, 33, 64, 100, 257, 512])
 def test_lu_fp64_bit_exact(gpu, n):
     rng = np.random.default_rng(n)
@@ -152,6 +209,41 @@ def test_batch_equals_single(gpu):
         ref, _, _ = O.solve(m)
         assert s["status"] == 0
         assert np.array_equal(o, ref)
+
+
+def _rhs_batch_models():
+    base, _ = synth.make_c5(1)
+    yield "c5-256", base[0]
+    yield "sized-37", synth.make_sized(37, 0)
+    yield "sized-601", synth.make_sized(601, 1)
+    yield "c2-512", synth.make_c2()
+    for kind in ("dimer", "source", "reversible"):
+        yield kind, synth.tiny_network(kind)
+
+
+@pytest.mark.parametrize("name,m", list(_rhs_batch_models()), ids=[c[0] for c in _rhs_batch_models()])
+def test_rhs_device_batch_bits(gpu, name, m):
+    """lassie_rhs_device against the oracle bit for bit, the sign of zero
+    included: every third state has a quarter of its species at 0, so some
+    sums consist of -0.0 terms only (the oracle's 0.0 + -0.0 is +0.0)."""
+    torch = pytest.importorskip("torch")
+    from lassie_gb300 import _native as nat
+    nm = solver.NativeModel.of(m)
+    om = O.OracleModel(m.left, m.right)
+    n_inst = 97
+    rng = np.random.default_rng(m.n_species)
+    x = rng.uniform(0, 2, (n_inst, m.n_species))
+    x[::3, rng.random(m.n_species) < 0.25] = 0.0
+    k = 10.0 ** rng.uniform(-3, 3, (n_inst, m.n_reactions))
+    dx_t = torch.full((n_inst, m.n_species), float("nan"), dtype=torch.float64, device="cuda")
+    x_t, k_t = torch.tensor(x, device="cuda"), torch.tensor(k, device="cuda")
+    nat.check(nat.load().lassie_rhs_device(nm.handle, n_inst, k_t.data_ptr(), x_t.data_ptr(),
+                                           dx_t.data_ptr(), None), "lassie_rhs_device")
+    torch.cuda.synchronize()
+    dx = dx_t.cpu().numpy()
+    for b in range(n_inst):
+        ref = om.rhs(k[b], x[b])
+        assert np.array_equal(dx[b].view(np.int64), ref.view(np.int64)), (name, b)
 
 
 @pytest.mark.parametrize("n_inst", [1, 7, 1000])
