@@ -275,12 +275,26 @@ def newton_bandwidth(torch, stream, precision, n_inst=2048, reps=10, warm=3):
         e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
+    # the write-only ceiling on the same buffer: torch's fill kernel
+    with torch.cuda.stream(stream):
+        for _ in range(warm):
+            M.fill_(0.5)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record(stream)
+        for _ in range(reps):
+            M.fill_(0.5)
+        f1.record(stream)
+    torch.cuda.synchronize()
+    fill_gbs = M.numel() * es / (f0.elapsed_time(f1) / reps * 1e-3) / 1e9
     nnz = C.c_int64(0)
     nat.check(L.lassie_jacobian_nnz(nm.handle, C.byref(nnz)), "lassie_jacobian_nnz")
     alg = n_inst * (es * N * N + 8 * (N + R))
     return {"gbs": alg / (ms * 1e-3) / 1e9, "ms_per_launch": ms, "bytes_per_launch": alg,
             "out": "fp64" if es == 8 else "fp32", "network": "256 species x 256 reactions",
-            "jacobian_nnz": int(nnz.value), "instances": n_inst}
+            "jacobian_nnz": int(nnz.value), "instances": n_inst,
+            "write_only_ceiling_gbs": fill_gbs,
+            "frac_of_write_ceiling": alg / (ms * 1e-3) / 1e9 / fill_gbs}
 
 
 def run_kernels(args):

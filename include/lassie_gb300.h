@@ -44,6 +44,15 @@ extern "C" {
 #define LASSIE_ERR_DEADLINE (-24)    /* opts.deadline_s elapsed on the device */
 #define LASSIE_ERR_NO_DEVICE (-25)   /* no CUDA device / not sm_103 */
 #define LASSIE_ERR_RECORD_FULL (-26) /* adjoint step record capacity reached */
+#define LASSIE_ERR_STEP_TOO_SMALL (-27) /* BDF controller: step below 10 ulp of t */
+
+/* step control (lassie_opts.controller) */
+#define LASSIE_CTRL_COMPAT 0 /* LASSIE's loop: RKF45 + fixed-step backward Euler
+                                (Simulation.cuh:632-925) */
+#define LASSIE_CTRL_BDF 1    /* variable-order BDF 1-5 with rtol/atol error control
+                                (the reference's unused BDF2-6 correctors,
+                                kernels.cuh:302-457, with step and order
+                                selection); FP64 factorisation, N <= 512 */
 
 /* precision of the Newton matrix factorisation */
 #define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */
@@ -79,6 +88,15 @@ typedef struct {
                              factorisation on the tensor cores (tcgen05, TF32
                              products of split operands), 0 (default) on the
                              FP32 pipes */
+    int32_t controller;   /* LASSIE_CTRL_* (default LASSIE_CTRL_COMPAT) */
+    /* LASSIE_CTRL_BDF only: */
+    double rtol;          /* relative tolerance (1e-6) */
+    double atol;          /* absolute tolerance when an instance has no atol
+                             vector (1e-9); an instance's atol vector is used
+                             as absolute tolerances per species */
+    double first_step;    /* 0 = chosen from f(x0) */
+    double max_step;      /* 0 = unbounded */
+    int32_t max_order;    /* 1..5 (5) */
     int32_t pad;
 } lassie_opts;
 
@@ -110,9 +128,16 @@ typedef struct {
     /* part of cycles_solve: the FP32 triangular solves (mixed form) */
     int64_t cycles_solve_tri;
     double t_final;
-    double dt_be_final;
+    double dt_be_final;   /* BDF controller: the last step size */
     int32_t status;
     int32_t pad;
+    /* BDF controller (be_steps counts its accepted steps, rkf_retries its
+       error-test rejections, lu_failures its Newton failures, outer_iters
+       its attempts) */
+    int64_t jac_evals;
+    int64_t rhs_evals;
+    int32_t order_final;
+    int32_t pad2;
 } lassie_stats;
 
 /* One instance of a batch: a network, its parameterisation and its outputs.

@@ -18,9 +18,12 @@ ERR_TOO_LARGE = -23
 ERR_DEADLINE = -24
 ERR_NO_DEVICE = -25
 ERR_RECORD_FULL = -26
+ERR_STEP_TOO_SMALL = -27
 ERR_CUDA = -13
 PREC_FP64 = 0
 PREC_MIXED = 1
+CTRL_COMPAT = 0
+CTRL_BDF = 1
 ROOT_POW = 0
 ROOT_SQRT = 1
 
@@ -42,7 +45,9 @@ class Opts(C.Structure):
                 ("newton_iter", C.c_int64), ("max_steps", C.c_int64),
                 ("deadline_s", C.c_double), ("precision", C.c_int32),
                 ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("lu_reuse", C.c_int32),
-                ("tensor_cores", C.c_int32), ("pad", C.c_int32)]
+                ("tensor_cores", C.c_int32), ("controller", C.c_int32),
+                ("rtol", C.c_double), ("atol", C.c_double), ("first_step", C.c_double),
+                ("max_step", C.c_double), ("max_order", C.c_int32), ("pad", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -56,10 +61,12 @@ class Stats(C.Structure):
                 ("cycles_lu_rows", C.c_int64), ("cycles_lu_trailing", C.c_int64),
                 ("cycles_solve_tri", C.c_int64),
                 ("t_final", C.c_double),
-                ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32)]
+                ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32),
+                ("jac_evals", C.c_int64), ("rhs_evals", C.c_int64),
+                ("order_final", C.c_int32), ("pad2", C.c_int32)]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+        return {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("pad")}
 
 
 class Instance(C.Structure):

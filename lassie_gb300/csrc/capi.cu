@@ -1,6 +1,7 @@
 // C ABI of the LASSIE GB300 engine: model compiler, batch packing, device
 // memory, launches.  Host code only; the kernels are in compat_engine.cu.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -17,7 +18,8 @@
 #include "lassie_gb300.h"
 
 namespace lassie {
-int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision);
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision,
+                          int controller);
 cudaError_t compat_configure(int precision, int64_t smem);
 cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
 int64_t wide_workspace_bytes(int N, int R, int nnz_a, int precision);
@@ -285,6 +287,12 @@ extern "C" void lassie_opts_default(lassie_opts *o) {
     o->quarter_root = LASSIE_ROOT_POW;
     o->lu_reuse = 1;
     o->tensor_cores = 0;
+    o->controller = LASSIE_CTRL_COMPAT;
+    o->rtol = 1e-6;
+    o->atol = 1e-9;
+    o->first_step = 0.0;
+    o->max_step = 0.0;
+    o->max_order = 5;
     o->pad = 0;
 }
 
@@ -304,6 +312,7 @@ extern "C" const char *lassie_status_string(int s) {
     case LASSIE_ERR_DEADLINE: return "device deadline elapsed";
     case LASSIE_ERR_NO_DEVICE: return "no sm_103 CUDA device";
     case LASSIE_ERR_RECORD_FULL: return "adjoint step record is full";
+    case LASSIE_ERR_STEP_TOO_SMALL: return "BDF step size below 10 ulp of t";
     default: return "unknown status";
     }
 }
@@ -398,9 +407,26 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     else lassie_opts_default(&o);
     if (o.precision != LASSIE_PREC_FP64 && o.precision != LASSIE_PREC_MIXED)
         return set_error(LASSIE_ERR_ARGS, "precision");
+    if (o.controller != LASSIE_CTRL_COMPAT && o.controller != LASSIE_CTRL_BDF)
+        return set_error(LASSIE_ERR_ARGS, "controller");
+    const bool bdf = o.controller == LASSIE_CTRL_BDF;
+    if (bdf) {
+        if (!(o.rtol > 0.0) || !(o.atol >= 0.0) || o.max_order < 1 || o.max_order > 5 ||
+            o.first_step < 0.0 || o.max_step < 0.0)
+            return set_error(LASSIE_ERR_ARGS, "BDF controller options");
+        o.precision = LASSIE_PREC_FP64;  // the BDF controller factors in FP64
+    }
     for (int q = 0; q < n; q++) {
         int rc = validate_instance(inst[q]);
         if (rc) return rc;
+        if (bdf && inst[q].model->N > kThreads)
+            return set_error(LASSIE_ERR_TOO_LARGE, "the BDF controller runs networks of at most " +
+                                                       std::to_string(kThreads) + " species");
+        if (bdf)  // the BDF loop advances to t[nt-1] through finite, ordered samples
+            for (int i = 0; i < inst[q].nt; i++)
+                if (!std::isfinite(inst[q].t[i]) || (i > 0 && !(inst[q].t[i] >= inst[q].t[i - 1])))
+                    return set_error(LASSIE_ERR_ARGS,
+                                     "BDF controller: sample times must be finite and ascending");
     }
     lassie_batch *b = new (std::nothrow) lassie_batch;
     if (!b) return set_error(LASSIE_ERR_ALLOC, "batch allocation");
@@ -521,7 +547,8 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         ws_stride = ws_total;
         b->wide_flags = wide_flags_offset(b->nmax, b->rmax, b->amax, o.precision);
     } else {
-        b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax, o.precision);
+        b->smem = compat_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax, o.precision,
+                                    o.controller);
         if (n > 0 && b->smem > max_optin - 1024) {
             delete b;
             return set_error(LASSIE_ERR_TOO_LARGE, "network needs " + std::to_string(b->smem) +
@@ -581,6 +608,12 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     P.lu_reuse = o.lu_reuse;
     P.tensor_cores = o.tensor_cores;
     P.deadline_ns = o.deadline_s > 0 ? (uint64_t)(o.deadline_s * 1e9) : 0;
+    P.controller = o.controller;
+    P.max_order = o.max_order;
+    P.rtol = o.rtol;
+    P.atol = o.atol;
+    P.first_step = o.first_step;
+    P.max_step = o.max_step;
     *out = b;
     return LASSIE_OK;
 }

@@ -44,6 +44,8 @@ struct InstResult {
     int64_t cycles_lu_panel, cycles_lu_rows, cycles_lu_trailing, cycles_solve_tri;
     double t_final, dt_be_final;
     int32_t status, pad;
+    int64_t jac_evals, rhs_evals;  // BDF controller
+    int32_t order_final, pad2;
 };
 static_assert(sizeof(InstResult) == sizeof(lassie_stats), "stats layout");
 
@@ -91,10 +93,14 @@ struct LaunchParams {
     int32_t precision, refine_max, lu_reuse, tensor_cores;
     uint64_t deadline_ns;      // per-launch wall-clock limit (ns), 0 = none
     AdjArrays adj;             // adj.desc == nullptr: no recording
+    // controller: 0 LASSIE's loop (integrate), 1 BDF with rtol/atol (bdf_integrate)
+    int32_t controller, max_order;
+    double rtol, atol, first_step, max_step;
 };
 
 // Dynamic shared-memory layout of the integrator (bytes), identical on host
-// and device.  Vectors are FP64 N-vectors; the sparse structure of the
+// and device.  Vectors are nvec FP64 N-vectors (10 for LASSIE's loop, more
+// for the BDF controller's differences); the sparse structure of the
 // network is staged here too; lt holds the factor panel column-major
 // (PB x (round_up32(N) + 4), plus slack for the 8-row tile reads past its end),
 // utile one PB x 128 tile of U12, rowbuf the pivot and swap rows.
@@ -102,9 +108,9 @@ struct SmemLayout {
     int64_t vec, kk, pw, qr, rptr, sptr, sent, rent, perm, slot, bvec, lt, utile, rowbuf, dblk, total;
     __host__ __device__ static int64_t align(int64_t v) { return (v + 15) & ~int64_t(15); }
     __host__ __device__ SmemLayout(int nmax, int rmax, int amax, int hmax, int lt_bytes, int pb,
-                                   int tn) {
+                                   int tn, int nvec = 10) {
         int64_t o = 0;
-        vec = o;    o = align(o + int64_t(10) * nmax * 8);
+        vec = o;    o = align(o + int64_t(nvec) * nmax * 8);
         kk = o;     o = align(o + int64_t(rmax) * 8);
         pw = o;     o = align(o + int64_t(amax > 0 ? amax : 1) * 8);
         qr = o;     o = align(o + int64_t(rmax) * 8);

@@ -1885,6 +1885,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     __syncthreads();
 }
 
+#include "bdf.cuh"
+
 template <typename LT>
 __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1904,6 +1906,12 @@ __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
         const int q = next;
         __syncthreads();
         if (q >= P.n_inst) break;
+        if constexpr (std::is_same<LT, double>::value) {
+            if (P.controller == LASSIE_CTRL_BDF) {
+                bdf_integrate(P, P.order[q], smem, red, ired, D, st, deadline);
+                continue;
+            }
+        }
         integrate<LT>(P, P.order[q], smem, red, ired, mv, D, st, deadline);
     }
 }
@@ -2265,7 +2273,12 @@ cudaError_t adjoint_launch(const LaunchParams &P, int grid, int64_t smem, cudaSt
 
 // ------------------------------------------------------------- launch
 
-int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision) {
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision,
+                          int controller) {
+    if (controller == LASSIE_CTRL_BDF)
+        return SmemLayout(nmax, rmax, amax, hmax, 8, LuShape<double>::PB, LuShape<double>::TN,
+                          kBdfVecs)
+            .total;
     if (precision == LASSIE_PREC_FP64)
         return SmemLayout(nmax, rmax, amax, hmax, 8, LuShape<double>::PB, LuShape<double>::TN)
             .total;

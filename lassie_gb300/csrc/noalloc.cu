@@ -31,7 +31,8 @@
 #include "lassie_gb300.h"
 
 namespace lassie {
-int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision);
+int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision,
+                          int controller);
 cudaError_t compat_configure(int precision, int64_t smem);
 cudaError_t compat_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
 int model_pack_for_noalloc(const lassie_model *m, std::vector<int32_t> &out, int32_t *n,
@@ -85,6 +86,8 @@ extern "C" int lassie_solve_noalloc(const lassie_model *model, const double *d_k
     else lassie_opts_default(&o);
     if (o.precision != LASSIE_PREC_FP64 && o.precision != LASSIE_PREC_MIXED)
         return set_error_noalloc(LASSIE_ERR_ARGS, "noalloc: precision");
+    if (o.controller != LASSIE_CTRL_COMPAT)
+        return set_error_noalloc(LASSIE_ERR_ARGS, "noalloc: LASSIE's controller only");
     std::vector<int32_t> ints;
     int32_t N = 0, R = 0, na = 0, nh = 0;
     int64_t offs[8];
@@ -112,7 +115,7 @@ extern "C" int lassie_solve_noalloc(const lassie_model *model, const double *d_k
     const int64_t total = off_ws + ws;
     if (total > LASSIE_NOALLOC_ARENA_BYTES)
         return set_error_noalloc(LASSIE_ERR_TOO_LARGE, "noalloc: arena too small for this network");
-    const int64_t smem = compat_smem_bytes(N, R, na, nh, o.precision);
+    const int64_t smem = compat_smem_bytes(N, R, na, nh, o.precision, LASSIE_CTRL_COMPAT);
     int dev = 0, max_optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=

@@ -59,9 +59,16 @@ class NativeModel:
 ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
 
 
+BDF_KEYS = ("rtol", "atol", "first_step", "max_step", "max_order")
+
+
 def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int = 0,
               deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow",
-              lu_reuse: bool = True, tensor_cores: bool = False) -> nat.Opts:
+              lu_reuse: bool = True, tensor_cores: bool = False,
+              bdf: Optional[Dict] = None) -> nat.Opts:
+    """Options of a solve.  ``bdf`` (a dict, possibly empty, of rtol, atol,
+    first_step, max_step, max_order) selects the BDF controller with rtol/atol
+    error control instead of LASSIE's loop; it factors in FP64."""
     o = nat.Opts()
     nat.load().lassie_opts_default(C.byref(o))
     if m is not None:
@@ -77,6 +84,13 @@ def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int =
     o.quarter_root = ROOTS[root]
     o.lu_reuse = 1 if lu_reuse else 0
     o.tensor_cores = 1 if tensor_cores else 0
+    if bdf is not None:
+        unknown = set(bdf) - set(BDF_KEYS)
+        if unknown:
+            raise ValueError(f"unknown BDF options {sorted(unknown)}")
+        o.controller = nat.CTRL_BDF
+        for key, val in bdf.items():
+            setattr(o, key, int(val) if key == "max_order" else float(val))
     return o
 
 
@@ -109,19 +123,20 @@ class _Packed:
 
 def simulate(m: Model, engine: str = "mixed", max_steps: int = 0, deadline_s: float = 0.0,
              nm: Optional[NativeModel] = None, root: str = "pow",
-             lu_reuse: bool = True, tensor_cores: bool = False) -> Tuple[np.ndarray, Dict]:
+             lu_reuse: bool = True, tensor_cores: bool = False,
+             bdf: Optional[Dict] = None) -> Tuple[np.ndarray, Dict]:
     """Integrate one model on the GPU.  Returns (trajectory [nt, ncs], stats)."""
     nm = nm or NativeModel.of(m)
     pk = _Packed(m, nm)
     st = nat.Stats()
     o = make_opts(m, engine, max_steps, deadline_s, root=root, lu_reuse=lu_reuse,
-                  tensor_cores=tensor_cores)
+                  tensor_cores=tensor_cores, bdf=bdf)
     rc = nat.load().lassie_solve(nm.handle, _p(pk.k), _p(pk.x0), _p(pk.feed), _p(pk.atol),
                                  _p(pk.t), pk.t.shape[0], _p(pk.cs),
                                  0 if pk.cs is None else pk.cs.shape[0], C.byref(o),
                                  _p(pk.out), C.byref(st))
     stats = st.as_dict()
-    if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE):
+    if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE, nat.ERR_STEP_TOO_SMALL):
         nat.check(rc, "lassie_solve")
     stats["status"] = rc
     return pk.out, stats
@@ -134,7 +149,7 @@ class Batch:
     def __init__(self, models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                  deadline_s: float = 0.0, native: Optional[Sequence[NativeModel]] = None,
                  refine_max: int = 0, root: str = "pow", lu_reuse: bool = True,
-                 tensor_cores: bool = False):
+                 tensor_cores: bool = False, bdf: Optional[Dict] = None):
         L = nat.load()
         cache: Dict[int, NativeModel] = {}
         self.packs = []
@@ -150,7 +165,7 @@ class Batch:
         self.n = len(models)
         self._inst = (nat.Instance * max(self.n, 1))(*[p.instance() for p in self.packs])
         self.opts = make_opts(models[0] if self.n else None, engine, max_steps, deadline_s,
-                              refine_max, root, lu_reuse, tensor_cores)
+                              refine_max, root, lu_reuse, tensor_cores, bdf)
         h = C.c_void_p()
         nat.check(L.lassie_batch_create(C.cast(self._inst, C.c_void_p), self.n,
                                         C.byref(self.opts), C.byref(h)), "lassie_batch_create")
@@ -189,7 +204,8 @@ class Batch:
 
 def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                    deadline_s: float = 0.0, root: str = "pow",
-                   lu_reuse: bool = True) -> Tuple[List[np.ndarray], List[Dict]]:
+                   lu_reuse: bool = True,
+                   bdf: Optional[Dict] = None) -> Tuple[List[np.ndarray], List[Dict]]:
     """Integrate independent instances in one persistent launch (host buffers
     in and out, ``lassie_solve_batch``)."""
     L = nat.load()
@@ -204,9 +220,9 @@ def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: in
     inst = (nat.Instance * max(n, 1))(*[p.instance() for p in packs])
     stats = (nat.Stats * max(n, 1))()
     o = make_opts(models[0] if n else None, engine, max_steps, deadline_s, root=root,
-                  lu_reuse=lu_reuse)
+                  lu_reuse=lu_reuse, bdf=bdf)
     rc = L.lassie_solve_batch(C.cast(inst, C.c_void_p), n, C.byref(o), C.cast(stats, C.c_void_p))
-    if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE):
+    if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE, nat.ERR_STEP_TOO_SMALL):
         nat.check(rc, "lassie_solve_batch")
     return [p.out for p in packs], [stats[q].as_dict() for q in range(n)]
 

@@ -115,6 +115,57 @@ int lo_solve_batch(int n_inst, const lo_model *const *models,
                    const lo_opts *opts, double *const *out, lo_stats *stats,
                    int *status, int threads);
 
+/* ------------------------------------------------ standard controller
+   Variable-order (1..max_order <= 5), quasi-constant-step BDF in backward-
+   difference form with rtol/atol error control (Shampine & Reichelt, "The
+   MATLAB ODE Suite", 1997, with kappa = 0: plain BDF).  At a constant step h
+   and order k its corrector is the classical BDFk formula of the
+   reference's unused kernels (kernels.cuh:289-370; BDF5 with the
+   denominator 137) and its Newton matrix is I - beta_k h J
+   (aggiorna_Jacobiano1..5, kernels.cuh:393-447), beta_k = 1/sum_{j<=k} 1/j.
+   J is the exact analytic Jacobian.  Samples come from the interpolating
+   polynomial of the differences.  Arithmetic shared with the FP64 CUDA
+   form: RMS norms sum like the 512-thread block reduction of the kernel
+   (lo_block_sum512), step-size factors are rounded down to multiples of
+   2^-10 so that a last-bit difference in pow() cannot change h. */
+typedef struct {
+    double rtol;          /* relative tolerance (default 1e-6) */
+    double atol;          /* absolute tolerance when atol[] is NULL (1e-9) */
+    double first_step;    /* 0 = automatic */
+    double max_step;      /* 0 = unbounded */
+    int32_t max_order;    /* 1..5 (default 5) */
+    int32_t pad;
+    int64_t max_steps;    /* step attempts; <= 0 unlimited */
+} lo_bdf_opts;
+
+typedef struct {
+    int64_t steps;             /* accepted */
+    int64_t rejected;          /* error-test failures */
+    int64_t newton_failures;   /* steps retried after Newton failed */
+    int64_t newton_iters;
+    int64_t jac_evals;
+    int64_t lu_factorisations;
+    int64_t rhs_evals;
+    int32_t order_final;
+    int32_t pad;
+    double h_final;
+    double t_final;
+} lo_bdf_stats;
+
+#define LO_ERR_STEP_TOO_SMALL (-27)
+
+/* Exact dense Jacobian (each other reactant with its stoichiometry), in the
+   FP64 CUDA form's operation order. */
+void lo_jacobian_exact(const lo_model *m, const double *k, const double *x, double *J);
+/* sum of v[0..n) in the order of the CUDA kernels' 512-thread block sum */
+double lo_block_sum512(const double *v, int n);
+void lo_bdf_opts_default(lo_bdf_opts *o);
+/* k[R], x0[N], feed[N] (NULL: none), atol[N] (NULL: opts->atol), t[nt]
+   ascending with t[0] the start, cs[ncs] (NULL: all), out[nt*ncs]. */
+int lo_solve_bdf(const lo_model *m, const double *k, const double *x0, const double *feed,
+                 const double *atol, const double *t, int nt, const int *cs, int ncs,
+                 const lo_bdf_opts *opts, double *out, lo_bdf_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

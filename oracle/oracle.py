@@ -48,6 +48,23 @@ class Stats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class BdfOpts(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("first_step", C.c_double),
+                ("max_step", C.c_double), ("max_order", C.c_int32), ("pad", C.c_int32),
+                ("max_steps", C.c_int64)]
+
+
+class BdfStats(C.Structure):
+    _fields_ = [("steps", C.c_int64), ("rejected", C.c_int64), ("newton_failures", C.c_int64),
+                ("newton_iters", C.c_int64), ("jac_evals", C.c_int64),
+                ("lu_factorisations", C.c_int64), ("rhs_evals", C.c_int64),
+                ("order_final", C.c_int32), ("pad", C.c_int32), ("h_final", C.c_double),
+                ("t_final", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "pad"}
+
+
 def build() -> str:
     """Compile the oracle with its Makefile (gcc, -ffp-contract=off)."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
@@ -83,6 +100,14 @@ def lib():
                                          C.c_void_p, _i32p, C.POINTER(Opts), C.c_void_p,
                                          C.c_void_p, _i32p, C.c_int]
             L.lo_solve_batch.restype = C.c_int
+            L.lo_jacobian_exact.argtypes = [C.POINTER(_Model), _f64p, _f64p, _f64p]
+            L.lo_block_sum512.argtypes = [_f64p, C.c_int]
+            L.lo_block_sum512.restype = C.c_double
+            L.lo_bdf_opts_default.argtypes = [C.POINTER(BdfOpts)]
+            L.lo_solve_bdf.argtypes = [C.POINTER(_Model), _f64p, _f64p, C.c_void_p, C.c_void_p,
+                                       _f64p, C.c_int, C.c_void_p, C.c_int,
+                                       C.POINTER(BdfOpts), _f64p, C.POINTER(BdfStats)]
+            L.lo_solve_bdf.restype = C.c_int
             _lib = L
     return _lib
 
@@ -110,6 +135,12 @@ class OracleModel:
         lib().lo_rhs(C.byref(self._m), np.ascontiguousarray(k, np.float64),
                      np.ascontiguousarray(x, np.float64), dx)
         return dx
+
+    def jacobian_exact(self, k, x) -> np.ndarray:
+        J = np.zeros((self.n_species, self.n_species))
+        lib().lo_jacobian_exact(C.byref(self._m), np.ascontiguousarray(k, np.float64),
+                                np.ascontiguousarray(x, np.float64), J)
+        return J
 
     def jacobian(self, k, x) -> np.ndarray:
         J = np.zeros((self.n_species, self.n_species))
@@ -150,6 +181,35 @@ def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None):
     rc = lib().lo_solve_compat(C.byref(om._m), k, x0, _ptr(feed), _ptr(atol), t,
                                t.shape[0], _ptr(cs), cs.shape[0], C.byref(o), out,
                                C.byref(st))
+    return out, st.as_dict(), rc
+
+
+def bdf_opts(rtol: float = 1e-6, atol: float = 1e-9, first_step: float = 0.0,
+             max_step: float = 0.0, max_order: int = 5, max_steps: int = 0) -> BdfOpts:
+    o = BdfOpts()
+    lib().lo_bdf_opts_default(C.byref(o))
+    o.rtol, o.atol, o.first_step, o.max_step = rtol, atol, first_step, max_step
+    o.max_order, o.max_steps = max_order, max_steps
+    return o
+
+
+def solve_bdf(model, om: Optional[OracleModel] = None, **kw):
+    """The standard controller (variable-order BDF, rtol/atol) on a
+    ``Model``; ``kw`` as ``bdf_opts``.  The model's atol vector, when set,
+    replaces the scalar atol.  Returns (trajectory [nt, ncs], stats, status)."""
+    om = om or OracleModel(model.left, model.right)
+    N = model.n_species
+    k = np.ascontiguousarray(model.k, np.float64)
+    x0 = np.ascontiguousarray(model.x0[:N], np.float64)
+    t = np.ascontiguousarray(model.t, np.float64)
+    cs = model.sampled().astype(np.int32)
+    feed = None if model.feed is None else np.ascontiguousarray(model.feed[:N], np.float64)
+    atol = None if model.atol is None else np.ascontiguousarray(model.atol[:N], np.float64)
+    out = np.zeros((t.shape[0], cs.shape[0]))
+    st = BdfStats()
+    o = bdf_opts(**kw)
+    rc = lib().lo_solve_bdf(C.byref(om._m), k, x0, _ptr(feed), _ptr(atol), t, t.shape[0],
+                            _ptr(cs), cs.shape[0], C.byref(o), out, C.byref(st))
     return out, st.as_dict(), rc
 
 
