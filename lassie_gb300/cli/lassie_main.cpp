@@ -1,5 +1,10 @@
 // `lassie input_folder output_folder [-v1|-v2|-v3] [-p double|float]
-//        [-engine mixed|fp64] [-root pow|sqrt] [-dump-f64] [-stats]`
+//        [-engine mixed|fp64] [-root pow|sqrt] [-dump-f64] [-stats]
+//        [-controller lassie|bdf] [-rtol R] [-atol A] [-max-order K]`
+//
+// -controller bdf replaces LASSIE's RKF45/backward-Euler loop with the
+// variable-order BDF controller (rtol/atol error control, orders 1..K); the
+// atol_vector file, when present, then gives absolute tolerances per species.
 //
 // Drop-in host for the reference CLI (src/c++/simulator.cu:29-319): the same
 // input-folder files and parsing (src/c++/header/Reader.h:23-134), defaults
@@ -232,6 +237,9 @@ int main(int argc, char *argv[]) {
     std::string prec = "double";
     std::string engine = "mixed";
     bool dump_f64 = false, want_stats = false, root_sqrt = false;
+    std::string controller = "lassie";
+    double bdf_rtol = 1e-6, bdf_atol = 1e-9;
+    int bdf_max_order = 5;
     for (int i = 3; i < argc; i++) {
         const std::string a = argv[i];
         if (a == "-v1") verbose = 1;
@@ -253,6 +261,14 @@ int main(int argc, char *argv[]) {
             if (r != "pow" && r != "sqrt") fail(-6, "Error: the root must be pow or sqrt");
             root_sqrt = r == "sqrt";
         }
+        if (a == "-controller" && i + 1 < argc) {
+            controller = argv[i + 1];
+            if (controller != "lassie" && controller != "bdf")
+                fail(-6, "Error: the controller must be lassie or bdf");
+        }
+        if (a == "-rtol" && i + 1 < argc) bdf_rtol = std::strtod(argv[i + 1], nullptr);
+        if (a == "-atol" && i + 1 < argc) bdf_atol = std::strtod(argv[i + 1], nullptr);
+        if (a == "-max-order" && i + 1 < argc) bdf_max_order = std::atoi(argv[i + 1]);
         if (a == "-dump-f64") dump_f64 = true;
         if (a == "-stats") want_stats = true;
     }
@@ -270,6 +286,12 @@ int main(int argc, char *argv[]) {
     lassie_opts_default(&opts);
     opts.precision = engine == "fp64" ? LASSIE_PREC_FP64 : LASSIE_PREC_MIXED;
     opts.quarter_root = root_sqrt ? LASSIE_ROOT_SQRT : LASSIE_ROOT_POW;
+    if (controller == "bdf") {
+        opts.controller = LASSIE_CTRL_BDF;
+        opts.rtol = bdf_rtol;
+        opts.atol = bdf_atol;
+        opts.max_order = bdf_max_order;
+    }
     if (files.count("be_step")) opts.be_step = read_single(files["be_step"]);
     if (files.count("rkf_step")) opts.rkf_step = read_single(files["rkf_step"]);
     if (files.count("newton_iter")) opts.newton_iter = (int64_t)(int)read_single(files["newton_iter"]);
@@ -299,6 +321,9 @@ int main(int argc, char *argv[]) {
         std::printf("Runge-Kutta-Fehlberg's tollerances = %g\n", atol.empty() ? 0.0 : atol[0]);
         std::printf("Float pointing precision = %s\n", prec.c_str());
         std::printf("Engine = %s\n", engine.c_str());
+        if (controller == "bdf")
+            std::printf("Controller = BDF (rtol %g, atol %g, orders 1-%d)\n", bdf_rtol, bdf_atol,
+                        bdf_max_order);
     }
     if (modelkind == 2) {
         std::printf("\nError: the modelkind can be: deterministic/concentration or stochastic/number\n");
@@ -390,7 +415,10 @@ int main(int argc, char *argv[]) {
     write_block_info(folder, 0, "DINAM-SUBSPEC", ncs, true, 512, 1);
     if (verbose > 1) std::printf("****Start simulation***\n");
     const auto t_int0 = std::chrono::steady_clock::now();
-    rc = lassie_solve(model, c_vector.data(), M_0.data(), feed.data(), atol.data(),
+    // the BDF controller takes per-species tolerances only from atol_vector
+    const double *atol_arg =
+        (controller == "bdf" && !files.count("atol_vector")) ? nullptr : atol.data();
+    rc = lassie_solve(model, c_vector.data(), M_0.data(), feed.data(), atol_arg,
                       t_vector.data(), nt, cs32.data(), ncs, &opts, out.data(), &st);
     const auto t_int1 = std::chrono::steady_clock::now();
     if (rc) {
@@ -447,13 +475,15 @@ int main(int argc, char *argv[]) {
                          "\"rkf_accepts\": %lld, \"rkf_retries\": %lld, \"be_steps\": %lld, "
                          "\"newton_iters\": %lld, \"lu_factorisations\": %lld, "
                          "\"lu_failures\": %lld, \"nan_reverts\": %lld, \"refine_sweeps\": %lld, "
-                         "\"t_final\": %.17g, \"dt_be_final\": %.17g}\n",
+                         "\"t_final\": %.17g, \"dt_be_final\": %.17g, \"controller\": \"%s\", "
+                         "\"jac_evals\": %lld, \"rhs_evals\": %lld, \"order_final\": %d}\n",
                          engine.c_str(), sim_s, (long long)st.outer_iters,
                          (long long)st.rkf_accepts, (long long)st.rkf_retries,
                          (long long)st.be_steps, (long long)st.newton_iters,
                          (long long)st.lu_factorisations, (long long)st.lu_failures,
                          (long long)st.nan_reverts, (long long)st.refine_sweeps, st.t_final,
-                         st.dt_be_final);
+                         st.dt_be_final, controller.c_str(), (long long)st.jac_evals,
+                         (long long)st.rhs_evals, (int)st.order_final);
             std::fclose(fd);
         }
     }

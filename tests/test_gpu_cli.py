@@ -54,6 +54,28 @@ def test_cli_outputs(gpu, tmp_path, engine):
     assert os.path.exists(out / "output" / "infoBlockThread")
 
 
+def test_cli_bdf_controller(gpu, tmp_path):
+    """-controller bdf: the BDF controller's trajectory, bit for bit its CPU
+    restatement at the same tolerances, in the reference's output files."""
+    build.build()
+    m = synth.shorten(synth.make_c4_instance(7), 2.0, 21)
+    m.atol = None
+    inp, out = tmp_path / "in", tmp_path / "out"
+    write_folder(m, str(inp))
+    r = subprocess.run([build.CLI, str(inp), str(out), "-controller", "bdf", "-rtol", "1e-7",
+                        "-atol", "1e-10", "-max-order", "4", "-dump-f64", "-stats"],
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    ref, rst, rc = O.solve_bdf(m, rtol=1e-7, atol=1e-10, max_order=4)
+    assert rc == 0
+    full = read_table(out / "output" / "Solution.f64")
+    assert np.array_equal(full[:, 1:], ref)
+    import json
+    st = json.loads((out / "output" / "stats.json").read_text())
+    assert st["controller"] == "bdf" and st["be_steps"] == rst["steps"]
+    assert st["order_final"] <= 4
+
+
 def test_cli_stochastic_rescales_output(gpu, tmp_path):
     build.build()
     m = synth.tiny_network("reversible")
