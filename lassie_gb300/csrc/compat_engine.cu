@@ -2508,6 +2508,45 @@ __device__ __forceinline__ double neg_bits(double v) {
     return __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
 }
 
+// k_y * x_a^ea * x_b^eb ... in reactant order (rhs_rates' product)
+__device__ __forceinline__ double rhs_rate(int y, const int *rptr, const int *rent,
+                                           const double *kb, const double *xs) {
+    double r = __ldg(kb + y);
+    for (int q = rptr[y]; q < rptr[y + 1]; q++) {
+        const int e = rent[q];
+        r = r * mypow(xs[ent_index(e)], ent_coef(e));
+    }
+    return r;
+}
+
+// dx_s from the rates: the entries of H row s in ascending order.  acc - r
+// is acc + (-r) in IEEE arithmetic: one addition per entry, and a sign flip
+// (integer) for a leading -r; the sum starts from its first term, and the
+// sign of an all-zero sum is restored at the end.
+__device__ __forceinline__ double rhs_species_sum(int s, const int *sptr, const int *sent,
+                                                  const int *rptr, const int *rent,
+                                                  const double *rate, const double *kb,
+                                                  const double *xs) {
+    const int e0 = sptr[s], e1 = sptr[s + 1];
+    if (e0 == e1) return 0.0;
+    double acc;
+    {
+        const int ent = sent[e0];
+        const int y = ent_index(ent), c = ent_coef(ent);
+        acc = c == 1 ? rate[y]
+                     : (c == -1 ? neg_bits(rate[y]) : rhs_term_scaled(y, c, rptr, rent, kb, xs));
+    }
+    for (int e = e0 + 1; e < e1; e++) {
+        const int ent = sent[e];
+        const int y = ent_index(ent), c = ent_coef(ent);
+        if (c == 1) acc = acc + rate[y];
+        else if (c == -1) acc = acc - rate[y];
+        else acc = acc + rhs_term_scaled(y, c, rptr, rent, kb, xs);
+    }
+    if (__double_as_longlong(acc) == (long long)0x8000000000000000ull) acc = 0.0;
+    return acc;
+}
+
 __global__ void __launch_bounds__(kRhsThreads) rhs_batch_kernel(
     int n_inst, int N, int R, int nnz_a, int nnz_h, const int *__restrict__ rptr_g,
     const int *__restrict__ rent_g, const int *__restrict__ sptr_g, const int *__restrict__ sent_g,
@@ -2541,41 +2580,45 @@ __global__ void __launch_bounds__(kRhsThreads) rhs_batch_kernel(
         // sums (rhs_species_r): bit-identical to the per-entry products
         for (int t = lane; t < R; t += 32) {
             const int y = rord[t];
-            double r = __ldg(kb + y);
-            for (int q = rptr[y]; q < rptr[y + 1]; q++) {
-                const int e = rent[q];
-                r = r * mypow(xs[ent_index(e)], ent_coef(e));
-            }
-            rate[y] = r;
+            rate[y] = rhs_rate(y, rptr, rent, kb, xs);
         }
         __syncwarp();
         double *db = dx + (int64_t)b * N;
         for (int t = lane; t < N; t += 32) {
             const int s = sord[t];
-            const int e0 = sptr[s], e1 = sptr[s + 1];
-            double acc = 0.0;
-            if (e0 < e1) {
-                // acc - r is acc + (-r) in IEEE arithmetic: one addition per
-                // entry, and a sign flip (integer) for a leading -r
-                {
-                    const int ent = sent[e0];
-                    const int y = ent_index(ent), c = ent_coef(ent);
-                    acc = c == 1 ? rate[y]
-                                 : (c == -1 ? neg_bits(rate[y])
-                                            : rhs_term_scaled(y, c, rptr, rent, kb, xs));
-                }
-                for (int e = e0 + 1; e < e1; e++) {
-                    const int ent = sent[e];
-                    const int y = ent_index(ent), c = ent_coef(ent);
-                    if (c == 1) acc = acc + rate[y];
-                    else if (c == -1) acc = acc - rate[y];
-                    else acc = acc + rhs_term_scaled(y, c, rptr, rent, kb, xs);
-                }
-                if (__double_as_longlong(acc) == (long long)0x8000000000000000ull) acc = 0.0;
-            }
-            db[s] = acc;
+            db[s] = rhs_species_sum(s, sptr, sent, rptr, rent, rate, kb, xs);
         }
         __syncwarp();
+    }
+}
+
+
+// The same RHS for networks whose x and rates do not fit once per warp: one
+// CTA per parameterisation, x and the rates in shared memory, the structure
+// read through L1/L2.  Same operations in the same order as rhs_batch_kernel.
+__global__ void __launch_bounds__(kRhsThreads) rhs_batch_cta_kernel(
+    int n_inst, int N, int R, const int *__restrict__ rptr, const int *__restrict__ rent,
+    const int *__restrict__ sptr, const int *__restrict__ sent, const int *__restrict__ order,
+    const double *__restrict__ k, const double *__restrict__ x, double *__restrict__ dx) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    double *xs = reinterpret_cast<double *>(smem);
+    double *rate = xs + N;
+    const int *rord = order, *sord = order + R;
+    for (int b = blockIdx.x; b < n_inst; b += gridDim.x) {
+        __syncthreads();  // the previous instance is done with xs/rate
+        for (int s = threadIdx.x; s < N; s += kRhsThreads) xs[s] = __ldcs(x + (int64_t)b * N + s);
+        __syncthreads();
+        const double *kb = k + (int64_t)b * R;
+        for (int t = threadIdx.x; t < R; t += kRhsThreads) {
+            const int y = __ldg(rord + t);
+            rate[y] = rhs_rate(y, rptr, rent, kb, xs);
+        }
+        __syncthreads();
+        double *db = dx + (int64_t)b * N;
+        for (int t = threadIdx.x; t < N; t += kRhsThreads) {
+            const int s = __ldg(sord + t);
+            db[s] = rhs_species_sum(s, sptr, sent, rptr, rent, rate, kb, xs);
+        }
     }
 }
 
@@ -2587,7 +2630,23 @@ cudaError_t rhs_batch_launch(int n_inst, int N, int R, int nnz_a, int nnz_h, con
                          (nnz_h > 0 ? nnz_h : 1) + R + N;
     const int64_t per_warp = ((N + 1) & ~1) + ((R + 1) & ~1);
     const int64_t smem = ((ints * 4 + 15) & ~int64_t(15)) + per_warp * 8 * kRhsWarps;
-    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    if (smem > 200 * 1024) {
+        // large network: one CTA per parameterisation
+        const int64_t smem1 = int64_t(N + R) * 8;
+        if (smem1 > 200 * 1024) return cudaErrorInvalidValue;
+        cudaError_t e = cudaFuncSetAttribute(rhs_batch_cta_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rhs_batch_cta_kernel, kRhsThreads,
+                                                          (size_t)smem1);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+        const int grid = (int)std::min<int64_t>(n_inst, (int64_t)sm_count * per_sm);
+        rhs_batch_cta_kernel<<<grid, kRhsThreads, smem1, stream>>>(n_inst, N, R, rptr, rent, sptr,
+                                                                   sent, order, k, x, dx);
+        return cudaGetLastError();
+    }
     cudaError_t e = cudaFuncSetAttribute(rhs_batch_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

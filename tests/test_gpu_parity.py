@@ -102,6 +102,42 @@ def test_newton_matrix_device_batch_bit_exact(gpu, name, m, n_inst, precision):
         assert np.array_equal(M[b], ref), (name, b)
 
 
+def test_device_kernels_at_4096_species(gpu):
+    """The largest network of the workloads (4096 species, 4096 reactions):
+    batched RHS and Newton matrix (FP64 and FP32) bit for bit against the
+    oracle for two parameterisations (2 x 128 MB of FP64 matrices)."""
+    torch = pytest.importorskip("torch")
+    from lassie_gb300 import _native as nat
+    m = synth.make_c3()
+    nm = solver.NativeModel.of(m)
+    om = O.OracleModel(m.left, m.right)
+    N, R, n_inst = m.n_species, m.n_reactions, 2
+    rng = np.random.default_rng(4096)
+    x = rng.uniform(0, 2, (n_inst, N))
+    k = 10.0 ** rng.uniform(-4, 2, (n_inst, R))
+    x_t, k_t = torch.tensor(x, device="cuda"), torch.tensor(k, device="cuda")
+    L = nat.load()
+    dx_t = torch.empty((n_inst, N), dtype=torch.float64, device="cuda")
+    nat.check(L.lassie_rhs_device(nm.handle, n_inst, k_t.data_ptr(), x_t.data_ptr(),
+                                  dx_t.data_ptr(), None), "lassie_rhs_device")
+    h = 0.01
+    for precision, dt in ((0, torch.float64), (1, torch.float32)):
+        M_t = torch.full((n_inst, N, N), float("nan"), dtype=dt, device="cuda")
+        nat.check(L.lassie_newton_matrix_device(nm.handle, n_inst, h, k_t.data_ptr(),
+                                                x_t.data_ptr(), M_t.data_ptr(), precision, None),
+                  "lassie_newton_matrix_device")
+        torch.cuda.synchronize()
+        for b in range(n_inst):
+            ref = np.eye(N) - h * om.jacobian(k[b], x[b])
+            if precision == 1:
+                ref = ref.astype(np.float32)
+            assert np.array_equal(M_t[b].cpu().numpy(), ref), (precision, b)
+        del M_t
+    dx = dx_t.cpu().numpy()
+    for b in range(n_inst):
+        assert np.array_equal(dx[b].view(np.int64), om.rhs(k[b], x[b]).view(np.int64))
+
+
 def test_newton_matrix_device_empty_and_args(gpu):
     from lassie_gb300 import _native as nat
     m = synth.tiny_network("dimer")
