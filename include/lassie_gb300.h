@@ -52,7 +52,10 @@ extern "C" {
 #define LASSIE_CTRL_BDF 1    /* variable-order BDF 1-5 with rtol/atol error control
                                 (the reference's unused BDF2-6 correctors,
                                 kernels.cuh:302-457, with step and order
-                                selection); FP64 factorisation, N <= 512 */
+                                selection); N <= 512.  precision FP64: FP64
+                                LU; MIXED: an FP32 Gauss-Jordan inverse as the
+                                modified-Newton iteration matrix, FP64
+                                residuals */
 
 /* precision of the Newton matrix factorisation */
 #define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */

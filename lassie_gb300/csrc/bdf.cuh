@@ -26,15 +26,19 @@
 // largest step.  Step changes rescale D (D <- (R(f) U)^T D).  Step factors
 // are rounded down to multiples of 2^-10, so that a last-bit difference of
 // pow() between platforms does not change h.  The CPU oracle follows the
-// same operation order, and the norms sum in block_sum's order, so this
-// kernel (FP64 LU) reproduces the oracle bit for bit.
+// same operation order, and the norms sum in block_sum's order, so the FP64
+// form (FP64 LU) reproduces the oracle bit for bit.  The mixed form
+// (LT = float) uses an FP32 Gauss-Jordan inverse of I - cJ as the modified
+// Newton iteration matrix: the corrections are applied to FP64 residuals,
+// so the converged step solves the same FP64 equations to the Newton
+// tolerance, with possibly more iterations.
 //
 // Included by compat_engine.cu after the RHS, Jacobian, LU and reduction
 // helpers (namespace lassie).
 
 constexpr int kBdfMaxOrder = 5;
 constexpr int kBdfNewtonMaxIter = 4;
-constexpr int kBdfVecs = kBdfMaxOrder + 3 + 11;  // differences + work vectors
+constexpr int kBdfVecs = kBdfMaxOrder + 3 + 12;  // differences + work vectors
 constexpr double kBdfMinFactor = 0.2, kBdfMaxFactor = 10.0;
 constexpr double kBdfEps = 2.220446049250313e-16;  // 2^-52
 
@@ -92,9 +96,10 @@ __device__ __noinline__ void bdf_change_d(double *Dd, int vstride, int N, int q,
     __syncthreads();
 }
 
+template <typename LT>
 __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsigned char *smem, double *red,
                               int *ired, InstDesc &D, InstResult &st, uint64_t deadline) {
-    using LT = double;
+    constexpr bool kMixed = std::is_same<LT, float>::value;
     constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN;
     const int tid = threadIdx.x;
     if (tid == 0) {
@@ -105,7 +110,7 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     const int N = D.n, R = D.r;
     const int *ia = P.iarena;
     const double *da = P.darena;
-    const SmemLayout L(P.nmax, P.rmax, P.amax, P.hmax, 8, PB, TN, kBdfVecs);
+    const SmemLayout L(P.nmax, P.rmax, P.amax, P.hmax, (int)sizeof(LT), PB, TN, kBdfVecs);
     double *vbase = reinterpret_cast<double *>(smem + L.vec);
     const int vstride = P.nmax;
     double *kk = reinterpret_cast<double *>(smem + L.kk);
@@ -120,6 +125,8 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     LT *lt = reinterpret_cast<LT *>(smem + L.lt);
     LT *utile = reinterpret_cast<LT *>(smem + L.utile);
     LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
+    LT *dblk = reinterpret_cast<LT *>(smem + L.dblk);
+    int *pos = reinterpret_cast<int *>(smem + L.slot);
     for (int q = tid; q < D.nnz_a; q += kThreads) w_rent[q] = ia[D.rxn_ent + q];
     for (int q = tid; q < D.nnz_h; q += kThreads) w_sent[q] = ia[D.sp_ent + q];
     for (int q = tid; q <= N; q += kThreads) w_sptr[q] = ia[D.sp_ptr + q];
@@ -141,7 +148,7 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     double *psi = ypred + vstride, *dv = psi + vstride, *ynew = dv + vstride;
     double *f = ynew + vstride, *dy = f + vstride, *scale = dy + vstride;
     double *atolv = scale + vstride, *aux = atolv + vstride, *xj = aux + vstride;
-    double *fedv = xj + vstride;
+    double *fedv = xj + vstride, *res = fedv + vstride;
 
     const double rtol = P.rtol;
     for (int s = tid; s < N; s += kThreads) {
@@ -284,8 +291,12 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                         assemble_newton_matrix<LT>(m, xj, c, M, ld, true, fedv);
                         if (tid == 0) st.cycles_matrix += clock64() - c_mark;
                         c_mark = clock64();
-                        const int fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red,
-                                                       ired, cyc);
+                        int fail;
+                        if constexpr (kMixed)
+                            fail = gje_factor(M, ld, N, perm, pos, lt, utile, dblk, rowbuf, red,
+                                              ired, cyc);
+                        else
+                            fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired, cyc);
                         if (tid == 0) {
                             st.cycles_lu += clock64() - c_mark;
                             st.lu_factorisations++;
@@ -309,14 +320,63 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                             for (int s = tid; s < N; s += kThreads) bad |= !isfinite(f[s]);
                             if (__syncthreads_or(bad)) break;
                             c_mark = clock64();
-                            for (int s = tid; s < N; s += kThreads) {
-                                const int ps = perm[s];
-                                bvec[s] = c * f[ps] - psi[ps] - dv[ps];
+                            if constexpr (kMixed) {
+                                // dy solves (I - cJ) dy = r in FP64 by
+                                // refinement with the FP32 inverse X:
+                                // dy += X res, res = r - (dy - c J dy) with
+                                // the exact J at xj, matrix-free; each res
+                                // is scaled by a power of two to unit max
+                                // norm for the FP32 cast
+                                long long rb = 0;
+                                for (int s = tid; s < N; s += kThreads) {
+                                    const double r = c * f[s] - psi[s] - dv[s];
+                                    aux[s] = r;
+                                    res[s] = r;
+                                    dy[s] = 0.0;
+                                    rb = max(rb, absbits_nonan(r));
+                                }
+                                double rmax = block_max(__longlong_as_double(rb), red);
+                                const double r0max = rmax;
+                                const int sweeps = P.refine_max > 0 ? P.refine_max : 8;
+                                for (int sw = 0; sw < sweeps; sw++) {
+                                    if (!(rmax > 0.0) || !isfinite(rmax)) break;
+                                    const int e = ilogb(rmax);
+                                    const double sc = ldexp(1.0, -e), isc = ldexp(1.0, e);
+                                    for (int s = tid; s < N; s += kThreads)
+                                        bvec[s] = (LT)(res[perm[s]] * sc);
+                                    __syncthreads();
+                                    gje_apply(reinterpret_cast<const float *>(M), ld, N, perm,
+                                              reinterpret_cast<float *>(bvec),
+                                              reinterpret_cast<float *>(lt), false);
+                                    for (int s = tid; s < N; s += kThreads)
+                                        dy[s] = dy[s] + (double)reinterpret_cast<const float *>(lt)[perm[s]] * isc;
+                                    __syncthreads();
+                                    if (tid == 0) st.refine_sweeps++;
+                                    // res = r - (dy - c J dy)
+                                    jv_phase1(m, xj, dy, qr, true);
+                                    __syncthreads();
+                                    long long nb = 0;
+                                    for (int s = tid; s < N; s += kThreads) {
+                                        const double jv = fedv[s] != 0.0 ? 0.0 : jv_species(m, s, qr);
+                                        const double rr = aux[s] - (dy[s] - c * jv);
+                                        res[s] = rr;
+                                        nb = max(nb, absbits_nonan(rr));
+                                    }
+                                    const double nmax = block_max(__longlong_as_double(nb), red);
+                                    const bool done = nmax <= r0max * 0x1p-50 || nmax > 0.5 * rmax;
+                                    rmax = nmax;
+                                    if (done) break;
+                                }
+                            } else {
+                                for (int s = tid; s < N; s += kThreads) {
+                                    const int ps = perm[s];
+                                    bvec[s] = c * f[ps] - psi[ps] - dv[ps];
+                                }
+                                __syncthreads();
+                                lu_solve<LT>(M, ld, N, perm, bvec);
+                                for (int s = tid; s < N; s += kThreads) dy[s] = bvec[s];
+                                __syncthreads();
                             }
-                            __syncthreads();
-                            lu_solve<LT>(M, ld, N, perm, bvec);
-                            for (int s = tid; s < N; s += kThreads) dy[s] = bvec[s];
-                            __syncthreads();
                             if (tid == 0) {
                                 st.cycles_solve += clock64() - c_mark;
                                 st.newton_iters++;

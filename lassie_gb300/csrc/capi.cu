@@ -414,7 +414,6 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         if (!(o.rtol > 0.0) || !(o.atol >= 0.0) || o.max_order < 1 || o.max_order > 5 ||
             o.first_step < 0.0 || o.max_step < 0.0)
             return set_error(LASSIE_ERR_ARGS, "BDF controller options");
-        o.precision = LASSIE_PREC_FP64;  // the BDF controller factors in FP64
     }
     for (int q = 0; q < n; q++) {
         int rc = validate_instance(inst[q]);

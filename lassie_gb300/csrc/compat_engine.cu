@@ -249,8 +249,10 @@ __device__ __forceinline__ double rhs_species_r(const Net &m, int i, const doubl
 // forming J: per reaction the directional derivative of k*prod(x), with the
 // other reactants multiplied in once each as createJac does, then the same
 // species sums as the RHS.  Phase 1 writes qr[R].
+// exact = true: the exact derivative (the other reactants with their
+// stoichiometry), as assemble_newton_matrix(exact) for the BDF controller.
 __device__ __forceinline__ double jv_reaction(const Net &m, const double *x, const double *v,
-                                               int y) {
+                                               int y, bool exact = false) {
     const int b = m.rptr[y], en = m.rptr[y + 1];
     double q = 0.0;
     for (int j = b; j < en; j++) {
@@ -261,16 +263,18 @@ __device__ __forceinline__ double jv_reaction(const Net &m, const double *x, con
         else if (a > 1) d = m.kk[y] * (double)a * mypow(x[g], a - 1);
         else continue;
         for (int jj = b; jj < en; jj++) {
-            const int o = ent_index(m.rent[jj]);
-            if (o != g) d = d * x[o];
+            const int eo = m.rent[jj];
+            const int o = ent_index(eo);
+            if (o != g) d = exact ? d * mypow(x[o], ent_coef(eo)) : d * x[o];
         }
         q = fma(d, v[g], q);
     }
     return q;
 }
 
-__device__ void jv_phase1(const Net &m, const double *x, const double *v, double *qr) {
-    for (int y = threadIdx.x; y < m.r; y += kThreads) qr[y] = jv_reaction(m, x, v, y);
+__device__ void jv_phase1(const Net &m, const double *x, const double *v, double *qr,
+                          bool exact = false) {
+    for (int y = threadIdx.x; y < m.r; y += kThreads) qr[y] = jv_reaction(m, x, v, y, exact);
 }
 
 __device__ __forceinline__ double jv_species(const Net &m, int i, const double *qr) {
@@ -1906,11 +1910,9 @@ __global__ void __launch_bounds__(kThreads, 1) compat_kernel(LaunchParams P) {
         const int q = next;
         __syncthreads();
         if (q >= P.n_inst) break;
-        if constexpr (std::is_same<LT, double>::value) {
-            if (P.controller == LASSIE_CTRL_BDF) {
-                bdf_integrate(P, P.order[q], smem, red, ired, D, st, deadline);
-                continue;
-            }
+        if (P.controller == LASSIE_CTRL_BDF) {
+            bdf_integrate<LT>(P, P.order[q], smem, red, ired, D, st, deadline);
+            continue;
         }
         integrate<LT>(P, P.order[q], smem, red, ired, mv, D, st, deadline);
     }
@@ -2276,9 +2278,13 @@ cudaError_t adjoint_launch(const LaunchParams &P, int grid, int64_t smem, cudaSt
 int64_t compat_smem_bytes(int nmax, int rmax, int amax, int hmax, int precision,
                           int controller) {
     if (controller == LASSIE_CTRL_BDF)
-        return SmemLayout(nmax, rmax, amax, hmax, 8, LuShape<double>::PB, LuShape<double>::TN,
-                          kBdfVecs)
-            .total;
+        return precision == LASSIE_PREC_FP64
+                   ? SmemLayout(nmax, rmax, amax, hmax, 8, LuShape<double>::PB,
+                                LuShape<double>::TN, kBdfVecs)
+                         .total
+                   : SmemLayout(nmax, rmax, amax, hmax, 4, LuShape<float>::PB,
+                                LuShape<float>::TN, kBdfVecs)
+                         .total;
     if (precision == LASSIE_PREC_FP64)
         return SmemLayout(nmax, rmax, amax, hmax, 8, LuShape<double>::PB, LuShape<double>::TN)
             .total;

@@ -68,7 +68,8 @@ def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int =
               bdf: Optional[Dict] = None) -> nat.Opts:
     """Options of a solve.  ``bdf`` (a dict, possibly empty, of rtol, atol,
     first_step, max_step, max_order) selects the BDF controller with rtol/atol
-    error control instead of LASSIE's loop; it factors in FP64."""
+    error control instead of LASSIE's loop; ``engine`` then picks its Newton
+    iteration matrix (fp64: FP64 LU; mixed: FP32 Gauss-Jordan inverse)."""
     o = nat.Opts()
     nat.load().lassie_opts_default(C.byref(o))
     if m is not None:
@@ -191,7 +192,7 @@ class Batch:
         stats = (nat.Stats * max(self.n, 1))()
         rc = nat.load().lassie_batch_read(self.handle, C.cast(self._inst, C.c_void_p),
                                           C.cast(stats, C.c_void_p))
-        if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE):
+        if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE, nat.ERR_STEP_TOO_SMALL):
             nat.check(rc, "lassie_batch_read")
         return [p.out for p in self.packs], [stats[q].as_dict() for q in range(self.n)]
 

@@ -62,7 +62,8 @@ def test_cli_bdf_controller(gpu, tmp_path):
     m.atol = None
     inp, out = tmp_path / "in", tmp_path / "out"
     write_folder(m, str(inp))
-    r = subprocess.run([build.CLI, str(inp), str(out), "-controller", "bdf", "-rtol", "1e-7",
+    r = subprocess.run([build.CLI, str(inp), str(out), "-engine", "fp64", "-controller", "bdf",
+                        "-rtol", "1e-7",
                         "-atol", "1e-10", "-max-order", "4", "-dump-f64", "-stats"],
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
