@@ -285,6 +285,12 @@ int main(int argc, char *argv[]) {
     lassie_opts opts;
     lassie_opts_default(&opts);
     opts.precision = engine == "fp64" ? LASSIE_PREC_FP64 : LASSIE_PREC_MIXED;
+    // the reference's -p float integrates with float state (Simulation<float>);
+    // this engine keeps the state, the RHS and the step control in FP64
+    // (-engine mixed factors in FP32), so -p float is accepted and reported
+    if (prec == "float")
+        std::fprintf(stderr, "Note: -p float is accepted for compatibility; the state is "
+                             "integrated in FP64 (-engine %s)\n", engine.c_str());
     opts.quarter_root = root_sqrt ? LASSIE_ROOT_SQRT : LASSIE_ROOT_POW;
     if (controller == "bdf") {
         opts.controller = LASSIE_CTRL_BDF;
