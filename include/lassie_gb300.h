@@ -53,9 +53,9 @@ extern "C" {
                                 (the reference's unused BDF2-6 correctors,
                                 kernels.cuh:302-457, with step and order
                                 selection); N <= 512.  precision FP64: FP64
-                                LU; MIXED: an FP32 Gauss-Jordan inverse as the
-                                modified-Newton iteration matrix, FP64
-                                residuals */
+                                LU; MIXED: an FP32 Gauss-Jordan inverse refined
+                                in FP64 as the Newton solve, FP64 factors for
+                                an instance after 4 Newton failures in a row */
 
 /* precision of the Newton matrix factorisation */
 #define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */

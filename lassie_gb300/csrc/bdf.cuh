@@ -38,6 +38,7 @@
 
 constexpr int kBdfMaxOrder = 5;
 constexpr int kBdfNewtonMaxIter = 4;
+constexpr int kBdfFallback = 4;  // Newton failures in a row before FP64 factors (mixed)
 constexpr int kBdfVecs = kBdfMaxOrder + 3 + 12;  // differences + work vectors
 constexpr double kBdfMinFactor = 0.2, kBdfMaxFactor = 10.0;
 constexpr double kBdfEps = 2.220446049250313e-16;  // 2^-52
@@ -197,6 +198,11 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     }
     int status = LASSIE_OK;
     int q = 1;
+    // mixed form: after kBdfFallback Newton failures in a row the instance
+    // factors in FP64 from then on (the workspace has FP64 room; the FP32
+    // panel buffers are as large as the FP64 ones, the solve vector is res)
+    bool fp64_lu = !kMixed;
+    int fail_run = 0;
     double h = 0.0;
     int64_t attempts = 0, rhs_evals = 0, jac_evals = 0;
     if (isample < nt) {
@@ -292,11 +298,22 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                         if (tid == 0) st.cycles_matrix += clock64() - c_mark;
                         c_mark = clock64();
                         int fail;
-                        if constexpr (kMixed)
-                            fail = gje_factor(M, ld, N, perm, pos, lt, utile, dblk, rowbuf, red,
-                                              ired, cyc);
-                        else
+                        if constexpr (kMixed) {
+                            if (fp64_lu) {
+                                double *Md = reinterpret_cast<double *>(M);
+                                assemble_newton_matrix<double>(m, xj, c, Md, ld, true, fedv);
+                                fail = lu_factor<double>(Md, ld, N, perm,
+                                                         reinterpret_cast<double *>(lt),
+                                                         reinterpret_cast<double *>(utile),
+                                                         reinterpret_cast<double *>(rowbuf), red,
+                                                         ired, cyc);
+                            } else {
+                                fail = gje_factor(M, ld, N, perm, pos, lt, utile, dblk, rowbuf,
+                                                  red, ired, cyc);
+                            }
+                        } else {
                             fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired, cyc);
+                        }
                         if (tid == 0) {
                             st.cycles_lu += clock64() - c_mark;
                             st.lu_factorisations++;
@@ -320,7 +337,7 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                             for (int s = tid; s < N; s += kThreads) bad |= !isfinite(f[s]);
                             if (__syncthreads_or(bad)) break;
                             c_mark = clock64();
-                            if constexpr (kMixed) {
+                            if (kMixed && !fp64_lu) {
                                 // dy solves (I - cJ) dy = r in FP64 by
                                 // refinement with the FP32 inverse X:
                                 // dy += X res, res = r - (dy - c J dy) with
@@ -368,13 +385,17 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                                     if (done) break;
                                 }
                             } else {
+                                // FP64 LU (the FP64 form, or the mixed form's
+                                // fallback with res as the solve vector)
+                                double *Md = reinterpret_cast<double *>(M);
+                                double *bv = kMixed ? res : reinterpret_cast<double *>(bvec);
                                 for (int s = tid; s < N; s += kThreads) {
                                     const int ps = perm[s];
-                                    bvec[s] = c * f[ps] - psi[ps] - dv[ps];
+                                    bv[s] = c * f[ps] - psi[ps] - dv[ps];
                                 }
                                 __syncthreads();
-                                lu_solve<LT>(M, ld, N, perm, bvec);
-                                for (int s = tid; s < N; s += kThreads) dy[s] = bvec[s];
+                                lu_solve<double>(Md, ld, N, perm, bv);
+                                for (int s = tid; s < N; s += kThreads) dy[s] = bv[s];
                                 __syncthreads();
                             }
                             if (tid == 0) {
@@ -413,6 +434,10 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                 }
                 if (!converged) {
                     if (tid == 0) st.lu_failures++;
+                    if (kMixed && !fp64_lu && ++fail_run >= kBdfFallback) {
+                        fp64_lu = true;
+                        if (tid == 0) st.nan_reverts++;  // counts the switch
+                    }
                     bdf_change_d(Dd, vstride, N, q, 0.5);
                     h = h * 0.5;
                     n_equal = 0;
@@ -439,6 +464,7 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                     continue;
                 }
                 accepted = true;
+                fail_run = 0;
                 if (tid == 0) st.be_steps++;
                 n_equal++;
                 tc = t_new;

@@ -554,7 +554,8 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
                                                        " bytes of shared memory per CTA");
         }
         b->grid = std::max(1, std::min(n, b->sm_count));
-        const int lt = o.precision == LASSIE_PREC_FP64 ? 8 : 4;
+        // the mixed BDF form may fall back to an FP64 factorisation: FP64 room
+        const int lt = (o.precision == LASSIE_PREC_FP64 || bdf) ? 8 : 4;
         // FP32 inverses of the 32x32 diagonal blocks after the matrix: the mixed
         // forward's solves and the adjoint's transposed solves (either form) use them
         const int64_t dinv_bytes = (int64_t)((b->nmax + 31) / 32) * 2048 * 4;

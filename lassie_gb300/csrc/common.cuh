@@ -121,7 +121,9 @@ struct SmemLayout {
         perm = o;   o = align(o + int64_t(nmax) * 4);
         slot = o;   o = align(o + int64_t(nmax) * 4);
         bvec = o;   o = align(o + int64_t(nmax) * lt_bytes);
-        lt = o;     o = align(o + (int64_t(pb) * (((nmax + 31) & ~31) + 4) + 160) * lt_bytes);
+        // 160 elements of slack (1280 bytes whatever the element type, so that
+        // an FP64 panel of half the width also fits)
+        lt = o;     o = align(o + int64_t(pb) * (((nmax + 31) & ~31) + 4) * lt_bytes + 160 * 8);
         utile = o;  o = align(o + int64_t(pb) * tn * lt_bytes);
         rowbuf = o; o = align(o + int64_t(2 * pb) * lt_bytes);
         dblk = o;   o = align(o + int64_t(pb) * pb * lt_bytes);
