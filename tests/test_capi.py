@@ -75,3 +75,38 @@ def test_bad_arguments_are_rejected(native):
     left = np.array([[300]], np.int32); right = np.zeros((1, 1), np.int32)
     assert native.lassie_model_create_dense(1, 1, left.ctypes.data, right.ctypes.data,
                                             C.byref(h)) == nat.ERR_TOO_LARGE
+
+
+def test_bdf_controller_options_checked_on_host(native):
+    """BDF controller: defaults, and option / instance checks that run before
+    any device query (so they hold without a GPU)."""
+    from lassie_gb300 import solver
+    o = nat.Opts()
+    native.lassie_opts_default(C.byref(o))
+    assert (o.controller, o.rtol, o.atol, o.max_order) == (nat.CTRL_COMPAT, 1e-6, 1e-9, 5)
+    assert native.lassie_status_string(nat.ERR_STEP_TOO_SMALL).startswith(b"BDF step size")
+
+    def create(m, **bdf):
+        nm = solver.NativeModel.of(m)
+        pk = solver._Packed(m, nm)
+        inst = nat.Instance()
+        inst.model, inst.k, inst.x0 = nm.handle, pk.k.ctypes.data, pk.x0.ctypes.data
+        inst.t, inst.nt = pk.t.ctypes.data, pk.t.shape[0]
+        inst.out, inst.cs, inst.ncs = pk.out.ctypes.data, None, 0
+        opts = solver.make_opts(m, bdf=bdf)
+        h = C.c_void_p()
+        rc = native.lassie_batch_create(C.byref(inst), 1, C.byref(opts), C.byref(h))
+        if rc == 0:
+            native.lassie_batch_destroy(h)
+        return rc
+
+    m = synth.make_c1()
+    assert create(m, rtol=0.0) == nat.ERR_ARGS
+    assert create(m, max_order=6) == nat.ERR_ARGS
+    assert create(m, max_step=-1.0) == nat.ERR_ARGS
+    bad_t = synth.make_c1()
+    bad_t.t = bad_t.t[::-1].copy()
+    assert create(bad_t) == nat.ERR_ARGS          # sample times must ascend
+    assert create(synth.make_sized(600, 0)) == nat.ERR_TOO_LARGE
+    # valid options: the next check is the device (none here, or one on a GPU box)
+    assert create(m) in (nat.OK, nat.ERR_NO_DEVICE)
