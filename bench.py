@@ -176,6 +176,47 @@ def cpu_baseline(n_total, threads=None, stride=64, t_frac=0.1, max_steps=25000):
             "seconds": dt}
 
 
+def _lsoda_one(q):
+    """One workload instance with scipy's LSODA (odeint): the oracle's RHS and
+    exact dense Jacobian through ctypes, rtol 1e-6, atol 1e-12, mxstep 10000.
+    Returns (seconds, success)."""
+    import warnings
+    from scipy.integrate import odeint
+    from lassie_gb300 import synth
+    from oracle import oracle as O
+    m = synth.make_c4_instance(q)
+    om = O.OracleModel(m.left, m.right)
+    k = m.k
+    t0 = time.perf_counter()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        _, info = odeint(lambda x, t: om.rhs(k, x), m.x0, m.t,
+                         Dfun=lambda x, t: om.jacobian_exact(k, x), rtol=1e-6, atol=1e-12,
+                         mxstep=10000, full_output=True)
+    return time.perf_counter() - t0, info.get("message", "") == "Integration successful."
+
+
+def lsoda_baseline(n_total, stride=128, threads=None):
+    """The CPU baseline the hot-path table defines: scipy's LSODA with the
+    analytic Jacobian on the host cores (one process per core, spawn-started),
+    on every `stride`-th instance of the workload over its whole horizon.  A
+    different algorithm from the reference's loop (error control), so it is
+    the CPU counterpart of the BDF controller."""
+    import multiprocessing as mp
+    idx = list(range(0, n_total, stride))
+    threads = threads or os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(threads, len(idx))) as pool:
+        res = pool.map(_lsoda_one, idx)
+    dt = time.perf_counter() - t0
+    done = sum(1 for _, ok in res if ok)
+    return {"value": done / dt, "unit": "sims/s", "cores": min(threads, len(idx)),
+            "kind": "scipy LSODA (odeint, analytic Jacobian, rtol 1e-6, atol 1e-12)",
+            "sample": f"{len(idx)} of the {n_total} instances (every {stride}th), full "
+                      f"horizon t in [0,20]; {done} integrated successfully; {dt:.2f} s wall",
+            "cpu_seconds_per_instance": sum(t for t, _ in res) / len(res)}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -498,6 +539,9 @@ def main():
                          "kernels: the RHS and Newton-matrix kernels alone")
     ap.add_argument("--tensor-cores", action="store_true",
                     help="c3: rank-32 updates of the factorisation on the tensor cores")
+    ap.add_argument("--lsoda", action="store_true",
+                    help="add scipy LSODA on the host cores (16 instances, full horizon; "
+                         "several minutes) as cpu_lsoda")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64-form, RHS and CPU-baseline measurements")
     args = ap.parse_args()
@@ -647,6 +691,8 @@ def main():
             line[key]["frac"] = line[key]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
         line["bdf_controller"] = {eng: bdf_measure(torch, stream, models, args.max_steps, eng)
                                   for eng in ("mixed", "fp64")}
+        if args.lsoda:
+            line["cpu_lsoda"] = lsoda_baseline(args.instances)
         line["cpu_baseline"] = cpu_baseline(args.instances, max_steps=args.max_steps)
         line["cpu_baseline"].pop("seconds", None)
     if rank == 0:
