@@ -288,9 +288,13 @@ int lassie_newton_matrix(const lassie_model *model, const double *k,
 int lassie_newton_matrix_device(const lassie_model *model, int32_t n_inst, double h,
                                 const double *k, const double *x, void *M,
                                 int32_t precision, void *stream);
-/* Structural nonzeros of J (entries createJac fills); builds and uploads the
-   pattern the batched Newton-matrix call uses. */
+/* Structural nonzeros of J, the entries createJac fills (kernels.cuh:219-271):
+   column g is in row i when a reaction with net stoichiometry in species i
+   has g among its reactants.  Host only (no device needed).  The pattern is
+   row_ptr[N+1] and cols[nnz] (columns ascending per row), the nonzeros the
+   batched Newton-matrix call writes besides the identity. */
 int lassie_jacobian_nnz(const lassie_model *model, int64_t *nnz);
+int lassie_jacobian_pattern(const lassie_model *model, int32_t *row_ptr, int32_t *cols);
 /* Factor a row-major n x n matrix with the engine's LU (precision as in
    lassie_opts) and solve A x = b; returns 1 + column of the first exactly
    zero pivot when singular.  Replaces linearSolverLU (Simulation.cuh:1280). */

@@ -34,7 +34,7 @@ EXPORTS = (
     "lassie_model_info", "lassie_solve", "lassie_solve_batch", "lassie_batch_create",
     "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
     "lassie_batch_bytes", "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
-    "lassie_newton_matrix_device", "lassie_jacobian_nnz",
+    "lassie_newton_matrix_device", "lassie_jacobian_nnz", "lassie_jacobian_pattern",
     "lassie_lu_solve", "lassie_adjoint_batch", "lassie_solve_noalloc", "lassie_tc_selftest",
 )
 
@@ -133,6 +133,7 @@ def load():
         L.lassie_newton_matrix.argtypes = [vp, vp, vp, dbl, vp]
         L.lassie_newton_matrix_device.argtypes = [vp, i32, dbl, vp, vp, vp, i32, vp]
         L.lassie_jacobian_nnz.argtypes = [vp, C.POINTER(C.c_int64)]
+        L.lassie_jacobian_pattern.argtypes = [vp, vp, vp]
         L.lassie_lu_solve.argtypes = [i32, vp, vp, vp, i32]
         L.lassie_adjoint_batch.argtypes = [vp, i32, vp, C.POINTER(Opts), i32, i32, vp, vp, vp, vp]
         L.lassie_solve_noalloc.argtypes = [vp, vp, vp, vp, i32, C.POINTER(Opts), vp,

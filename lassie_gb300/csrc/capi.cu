@@ -1028,13 +1028,45 @@ extern "C" int lassie_newton_matrix_device(const lassie_model *cm, int32_t n_ins
     return LASSIE_OK;
 }
 
-extern "C" int lassie_jacobian_nnz(const lassie_model *cm, int64_t *nnz) {
-    lassie_model *m = const_cast<lassie_model *>(cm);
+// Host-only: column g is in row i when a reaction with net stoichiometry in
+// species i has g among its reactants; columns ascending per row.
+static void jac_pattern_host(const lassie_model *m, std::vector<int32_t> &ptr,
+                             std::vector<int32_t> &col) {
+    ptr.assign(m->N + 1, 0);
+    col.clear();
+    std::vector<int32_t> mark(m->N, -1);
+    for (int i = 0; i < m->N; i++) {
+        ptr[i] = (int32_t)col.size();
+        const size_t first = col.size();
+        for (int e = m->sp_ptr[i]; e < m->sp_ptr[i + 1]; e++) {
+            const int y = ent_index(m->sp_ent[e]);
+            for (int q = m->rxn_ptr[y]; q < m->rxn_ptr[y + 1]; q++) {
+                const int g = ent_index(m->rxn_ent[q]);
+                if (mark[g] != i) {
+                    mark[g] = i;
+                    col.push_back(g);
+                }
+            }
+        }
+        std::sort(col.begin() + first, col.end());
+    }
+    ptr[m->N] = (int32_t)col.size();
+}
+
+extern "C" int lassie_jacobian_nnz(const lassie_model *m, int64_t *nnz) {
     if (!m || !nnz) return set_error(LASSIE_ERR_ARGS, "jacobian_nnz");
-    const int32_t *dj = nullptr;
-    int rc = model_jac_device(m, &dj);
-    if (rc) return rc;
-    *nnz = m->jac_nnz;
+    std::vector<int32_t> ptr, col;
+    jac_pattern_host(m, ptr, col);
+    *nnz = (int64_t)col.size();
+    return LASSIE_OK;
+}
+
+extern "C" int lassie_jacobian_pattern(const lassie_model *m, int32_t *row_ptr, int32_t *cols) {
+    if (!m || !row_ptr || !cols) return set_error(LASSIE_ERR_ARGS, "jacobian_pattern");
+    std::vector<int32_t> ptr, col;
+    jac_pattern_host(m, ptr, col);
+    std::memcpy(row_ptr, ptr.data(), ptr.size() * sizeof(int32_t));
+    if (!col.empty()) std::memcpy(cols, col.data(), col.size() * sizeof(int32_t));
     return LASSIE_OK;
 }
 

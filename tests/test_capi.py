@@ -110,3 +110,32 @@ def test_bdf_controller_options_checked_on_host(native):
     assert create(synth.make_sized(600, 0)) == nat.ERR_TOO_LARGE
     # valid options: the next check is the device (none here, or one on a GPU machine)
     assert create(m) in (nat.OK, nat.ERR_NO_DEVICE)
+
+
+def test_jacobian_pattern_on_host(native):
+    """lassie_jacobian_pattern / _nnz (host only): the structural nonzeros of
+    J, columns ascending per row, equal to the nonzeros of the oracle's
+    Jacobian at positive states (no cancellation at random x)."""
+    from lassie_gb300 import solver
+    from oracle import oracle as O
+    for m in (synth.make_c1(), synth.make_c5(1)[0][0], synth.make_sized(77, 2),
+              synth.tiny_network("reversible")):
+        nm = solver.NativeModel.of(m)
+        N = m.n_species
+        nnz = C.c_int64()
+        assert native.lassie_jacobian_nnz(nm.handle, C.byref(nnz)) == 0
+        ptr = np.zeros(N + 1, np.int32)
+        cols = np.zeros(max(1, nnz.value), np.int32)
+        assert native.lassie_jacobian_pattern(nm.handle, ptr.ctypes.data, cols.ctypes.data) == 0
+        assert ptr[-1] == nnz.value
+        pat = np.zeros((N, N), bool)
+        for i in range(N):
+            row = cols[ptr[i]:ptr[i + 1]]
+            assert np.all(np.diff(row) > 0)
+            pat[i, row] = True
+        om = O.OracleModel(m.left, m.right)
+        rng = np.random.default_rng(N)
+        seen = np.zeros((N, N), bool)
+        for _ in range(3):
+            seen |= om.jacobian(m.k, rng.uniform(0.1, 2.0, N)) != 0
+        assert np.array_equal(seen, pat)
