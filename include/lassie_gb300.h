@@ -226,7 +226,8 @@ void lassie_batch_destroy(lassie_batch *batch);
    steps are differentiated as exactly solved; steps that reverted species
    or failed to factor are treated as the identity.  Accepted RKF45 steps
    store their output every ckpt_every steps (0 = 8) and are recomputed in
-   between; max_record caps the recorded steps per instance (0 = 100000). */
+   between; max_record caps the recorded steps per instance (0 = 100000).
+   opts->controller must be LASSIE_CTRL_COMPAT (LASSIE_ERR_ARGS otherwise). */
 int lassie_adjoint_batch(const lassie_instance *inst, int32_t n, const double *const *targets,
                          const lassie_opts *opts, int32_t ckpt_every, int32_t max_record,
                          double *loss, double *const *grad_logk, double *const *grad_x0,

@@ -718,6 +718,9 @@ extern "C" int lassie_adjoint_batch(const lassie_instance *inst, int32_t n,
     lassie_opts o;
     if (opts) o = *opts;
     else lassie_opts_default(&o);
+    // the recorded forward and its reverse are LASSIE's loop
+    if (o.controller != LASSIE_CTRL_COMPAT)
+        return set_error(LASSIE_ERR_ARGS, "adjoint_batch: LASSIE's controller only");
     const int K = ckpt_every > 0 ? ckpt_every : 8;
     const int cap = max_record > 0 ? max_record : 100000;
     lassie_batch *b = nullptr;

@@ -139,3 +139,25 @@ def test_jacobian_pattern_on_host(native):
         for _ in range(3):
             seen |= om.jacobian(m.k, rng.uniform(0.1, 2.0, N)) != 0
         assert np.array_equal(seen, pat)
+
+
+def test_adjoint_refuses_the_bdf_controller(native):
+    """The adjoint differentiates LASSIE's loop; BDF options are refused on
+    the host before any device work."""
+    from lassie_gb300 import solver
+    m = synth.make_c1()
+    nm = solver.NativeModel.of(m)
+    pk = solver._Packed(m, nm)
+    inst = nat.Instance()
+    inst.model, inst.k, inst.x0 = nm.handle, pk.k.ctypes.data, pk.x0.ctypes.data
+    inst.t, inst.nt = pk.t.ctypes.data, pk.t.shape[0]
+    inst.out, inst.cs, inst.ncs = pk.out.ctypes.data, None, 0
+    target = np.zeros_like(pk.out)
+    tp = (C.c_void_p * 1)(target.ctypes.data)
+    g = np.zeros(m.n_reactions)
+    gp = (C.c_void_p * 1)(g.ctypes.data)
+    loss = np.zeros(1)
+    opts = solver.make_opts(m, bdf={})
+    rc = native.lassie_adjoint_batch(C.byref(inst), 1, C.cast(tp, C.c_void_p), C.byref(opts), 0, 0,
+                                     loss.ctypes.data, C.cast(gp, C.c_void_p), None, None)
+    assert rc == nat.ERR_ARGS
