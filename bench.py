@@ -19,9 +19,11 @@ default 25000: the instances whose step ends at 1e-3 need about 20000);
 capped ones are reported.
 
 Extra keys: the plain FP64 GPU form and the max relative error against it on
-a sample, the batched RHS kernel's HBM bandwidth, the roofline of the
-integrator kernel, the CPU baseline (the oracle port on the host cores), the
-SM clocks sampled during the timed region.
+a sample, the mixed-vs-FP64 parity per configuration, the adjoint, the
+batched RHS and Newton-matrix kernels' HBM bandwidth, the BDF controller on
+the same batch (both forms), the roofline of the integrator kernel, the CPU
+baselines (the oracle port, and scipy LSODA, on the host cores), the SM clocks
+sampled during the timed region.
 
 ``--impl reference`` times the reference algorithm's CPU implementation (the
 oracle port, all host threads) on a bounded sample of the same workload.
@@ -205,10 +207,24 @@ def lsoda_baseline(n_total, stride=128, threads=None):
     import multiprocessing as mp
     idx = list(range(0, n_total, stride))
     threads = threads or os.cpu_count() or 1
-    t0 = time.perf_counter()
-    with mp.get_context("spawn").Pool(min(threads, len(idx))) as pool:
-        res = pool.map(_lsoda_one, idx)
-    dt = time.perf_counter() - t0
+    # one BLAS/OpenMP thread per worker process (the workers inherit the
+    # environment at spawn); otherwise every worker's BLAS pool spans all cores
+    # and LSODA's many small BLAS calls slow down by orders of magnitude
+    pinned = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {v: os.environ.get(v) for v in pinned}
+    for v in pinned:
+        os.environ[v] = "1"
+    try:
+        t0 = time.perf_counter()
+        with mp.get_context("spawn").Pool(min(threads, len(idx))) as pool:
+            res = pool.map(_lsoda_one, idx)
+        dt = time.perf_counter() - t0
+    finally:
+        for v, val in saved.items():
+            if val is None:
+                os.environ.pop(v, None)
+            else:
+                os.environ[v] = val
     done = sum(1 for _, ok in res if ok)
     return {"value": done / dt, "unit": "sims/s", "cores": min(threads, len(idx)),
             "kind": "scipy LSODA (odeint, analytic Jacobian, rtol 1e-6, atol 1e-12)",
@@ -539,9 +555,6 @@ def main():
                          "kernels: the RHS and Newton-matrix kernels alone")
     ap.add_argument("--tensor-cores", action="store_true",
                     help="c3: rank-32 updates of the factorisation on the tensor cores")
-    ap.add_argument("--lsoda", action="store_true",
-                    help="add scipy LSODA on the host cores (16 instances, full horizon; "
-                         "several minutes) as cpu_lsoda")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64-form, RHS and CPU-baseline measurements")
     args = ap.parse_args()
@@ -691,8 +704,7 @@ def main():
             line[key]["frac"] = line[key]["gbs"] / float(peaks.get("hbm_gbs", 6800.0))
         line["bdf_controller"] = {eng: bdf_measure(torch, stream, models, args.max_steps, eng)
                                   for eng in ("mixed", "fp64")}
-        if args.lsoda:
-            line["cpu_lsoda"] = lsoda_baseline(args.instances)
+        line["cpu_lsoda"] = lsoda_baseline(args.instances, stride=64)
         line["cpu_baseline"] = cpu_baseline(args.instances, max_steps=args.max_steps)
         line["cpu_baseline"].pop("seconds", None)
     if rank == 0:
