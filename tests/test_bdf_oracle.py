@@ -55,12 +55,15 @@ def test_closed_forms():
     assert np.allclose(out[:, 0], m.x0[0] + m.k[0] * m.t, rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.parametrize("name", ["c1", "c5", "sized-100"])
+@pytest.mark.parametrize("name", ["c1", "c5", "sized-100", "c2-short"])
 def test_accuracy_like_scipy_bdf(name):
     """Global error against LSODA at rtol 1e-12 is of the size scipy's BDF
-    reaches at the same tolerances (both control the local error only)."""
+    reaches at the same tolerances (both control the local error only).  On
+    the stiff 512-species network (t in [0, 0.01]) this restatement's error is
+    about 11x the tolerance, scipy's about 62x."""
     m = {"c1": synth.make_c1, "c5": lambda: synth.make_c5(1)[0][0],
-         "sized-100": lambda: synth.make_sized(100, 3)}[name]()
+         "sized-100": lambda: synth.make_sized(100, 3),
+         "c2-short": lambda: synth.shorten(synth.make_c2(), 0.01, 6)}[name]()
     om = O.OracleModel(m.left, m.right)
     out, st, rc = O.solve_bdf(m, om=om, rtol=RTOL, atol=ATOL)
     assert rc == 0
