@@ -136,3 +136,41 @@ def test_block_sum_mirror():
     # rounding; the result is one of the two neighbours of the exact sum
     s = O.lib().lo_block_sum512(v, 512)
     assert s in (1.0, 1.0 + 2.0 ** -52)
+
+
+def test_fed_species_and_atol_vector_like_scipy():
+    """Fed species held constant and per-species absolute tolerances: the
+    restatement's error against LSODA at rtol 1e-12 (the same constraint
+    applied there) is of the size of scipy's BDF with the same tolerances."""
+    from scipy.integrate import solve_ivp
+    m = synth.make_sized(60, 7)
+    m.feed = np.zeros(m.n_species)
+    m.feed[[5, 33]] = [0.8, 1.7]
+    m.atol = np.full(m.n_species, 1e-10)
+    m.atol[::4] = 1e-7
+    om = O.OracleModel(m.left, m.right)
+    fed = m.feed != 0
+    x0 = np.where(fed, m.feed, m.x0)
+
+    def f(t, x):
+        d = om.rhs(m.k, x)
+        d[fed] = 0.0
+        return d
+
+    def jac(t, x):
+        J = om.jacobian_exact(m.k, x)
+        J[fed, :] = 0.0
+        return J
+
+    ref = solve_ivp(f, (m.t[0], m.t[-1]), x0, method="LSODA", t_eval=m.t, rtol=1e-12,
+                    atol=1e-14, jac=jac).y.T
+    theirs = solve_ivp(f, (m.t[0], m.t[-1]), x0, method="BDF", t_eval=m.t, rtol=RTOL,
+                       atol=m.atol, jac=jac).y.T
+    out, st, rc = O.solve_bdf(m, rtol=RTOL)
+    assert rc == 0
+    cs = list(m.sampled())
+    assert np.all(out[:, cs.index(5)] == 0.8) and np.all(out[:, cs.index(33)] == 1.7)
+    tol = m.atol + RTOL * np.abs(ref)
+    mine = float(np.max(np.abs(out - ref) / tol))
+    other = float(np.max(np.abs(theirs - ref) / tol))
+    assert mine < max(3 * other, 10.0), (mine, other)
