@@ -7,14 +7,15 @@
 #   build  (anywhere nvcc is): compile the staged sources with the
 #          force-included oracle/ref_prelude.h into oracle/_ref/lassie_ref
 #          (stock output) and oracle/_ref/lassie_ref_f64 (17-digit Solution).
-# Usage: oracle/build_ref.sh [stage|build|all]   (default: all)
+# Usage: LASSIE_REFERENCE_DIR=<LASSIE checkout> oracle/build_ref.sh [stage|build|all]
+#        (default: all; stage needs LASSIE_REFERENCE_DIR)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${LASSIE_REFERENCE_DIR:-/root/reference}"
+REF="${LASSIE_REFERENCE_DIR:-}"
 OUT="$HERE/_ref"
 what="${1:-all}"
 if [[ "$what" == stage || "$what" == all ]]; then
-  if [[ -d "$REF/src/c++" ]]; then
+  if [[ -n "$REF" && -d "$REF/src/c++" ]]; then
     mkdir -p "$OUT/src/header"
     install -m 644 "$REF/src/c++/simulator.cu" "$OUT/src/"
     install -m 644 "$REF/src/c++/header/Simulation.cuh" "$REF/src/c++/header/kernels.cuh" \

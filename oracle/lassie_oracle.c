@@ -157,7 +157,18 @@ void lo_jacobian(const lo_model *m, const double *k, const double *x,
    Simulation.cuh:1280-1326).  Pivot = first index of max |a|; failure when the
    pivot is exactly zero (getrf's info > 0).  Right-looking: every trailing
    element is updated as a = fma(-l, u, a) once per pivot, in pivot order. */
+/* LU-order variant (tests only, process-global, like the perturbation
+   below): 0 the default order above the GPU form shares; 1 the triangular
+   solves round the products and sums separately (no fma); 2 the Schur
+   update rounds them separately; 3 both.  Each is a valid partial-pivot FP64
+   LU solve that differs from the default in the last bits only -- as another
+   library's getrf/getrs (the reference calls cuSOLVER) does. */
+static int g_lu_variant = 0;
+
+void lo_set_lu_variant(int v) { g_lu_variant = v; }
+
 int lo_lu_factor(int n, double *a, int *piv) {
+    const int split = (g_lu_variant & 2) != 0;
     for (int j = 0; j < n; j++) {
         int p = j;
         double best = fabs(a[(size_t)j * n + j]);
@@ -184,7 +195,14 @@ int lo_lu_factor(int n, double *a, int *piv) {
             double *ri = a + (size_t)i * n;
             const double l = ri[j] / d;
             ri[j] = l;
-            for (int c = j + 1; c < n; c++) ri[c] = fma(-l, uj[c], ri[c]);
+            if (split) {
+                for (int c = j + 1; c < n; c++) {
+                    const double prod = l * uj[c];
+                    ri[c] = ri[c] - prod;
+                }
+            } else {
+                for (int c = j + 1; c < n; c++) ri[c] = fma(-l, uj[c], ri[c]);
+            }
         }
     }
     return 0;
@@ -202,16 +220,31 @@ void lo_lu_solve(int n, const double *lu, const int *piv, double *b) {
             b[p] = tmp;
         }
     }
+    const int split = (g_lu_variant & 1) != 0;
     for (int i = 0; i < n; i++) {
         double acc = b[i];
         const double *ri = lu + (size_t)i * n;
-        for (int j = 0; j < i; j++) acc = fma(-ri[j], b[j], acc);
+        if (split) {
+            for (int j = 0; j < i; j++) {
+                const double prod = ri[j] * b[j];
+                acc = acc - prod;
+            }
+        } else {
+            for (int j = 0; j < i; j++) acc = fma(-ri[j], b[j], acc);
+        }
         b[i] = acc;
     }
     for (int i = n - 1; i >= 0; i--) {
         double acc = b[i];
         const double *ri = lu + (size_t)i * n;
-        for (int j = n - 1; j > i; j--) acc = fma(-ri[j], b[j], acc);
+        if (split) {
+            for (int j = n - 1; j > i; j--) {
+                const double prod = ri[j] * b[j];
+                acc = acc - prod;
+            }
+        } else {
+            for (int j = n - 1; j > i; j--) acc = fma(-ri[j], b[j], acc);
+        }
         b[i] = acc / ri[i];
     }
 }

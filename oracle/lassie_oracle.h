@@ -74,6 +74,10 @@ typedef struct {
 /* Tests only: multiply each Newton correction componentwise by (1 +- rel)
    with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
 void lo_set_solve_perturbation(double rel, uint64_t seed);
+/* Tests only: pick the LU's rounding order (0 default; 1 the triangular
+   solves, 2 the Schur update, 3 both, round products and sums separately
+   instead of using fma); process-global, not thread safe. */
+void lo_set_lu_variant(int v);
 
 int lo_model_build(int n_reactions, int n_species, const int32_t *left,
                    const int32_t *right, lo_model *out);

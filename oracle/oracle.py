@@ -87,6 +87,7 @@ def lib():
             L.lo_lu_factor.restype = C.c_int
             L.lo_lu_solve.argtypes = [C.c_int, _f64p, _i32p, _f64p]
             L.lo_set_solve_perturbation.argtypes = [C.c_double, C.c_uint64]
+            L.lo_set_lu_variant.argtypes = [C.c_int]
             L.lo_solve_compat.argtypes = [C.POINTER(_Model), _f64p, _f64p, C.c_void_p,
                                           C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Opts), _f64p, C.POINTER(Stats)]
@@ -290,4 +291,22 @@ class solve_perturbation:
 
     def __exit__(self, *exc):
         lib().lo_set_solve_perturbation(0.0, 0)
+        return False
+
+
+class lu_variant:
+    """Context manager: inside it the oracle's LU rounds in another valid
+    order (1: triangular solves without fma, 2: Schur update without fma,
+    3: both) -- another FP64 getrf/getrs that differs in the last bits only.
+    Single-threaded use only."""
+
+    def __init__(self, variant: int):
+        self.variant = int(variant)
+
+    def __enter__(self):
+        lib().lo_set_lu_variant(self.variant)
+        return self
+
+    def __exit__(self, *exc):
+        lib().lo_set_lu_variant(0)
         return False
