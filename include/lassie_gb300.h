@@ -244,8 +244,8 @@ int lassie_tc_selftest(const float *d_a, const float *d_b, float *d_d, int *d_st
 
 /* One integration that allocates no device memory (no counterpart in the
    reference, which allocates in every solve).  For callers that cannot call
-   cudaMalloc -- code running under another framework's memory pool or
-   inside a stream capture, plugins that may not allocate after start-up,
+   cudaMalloc: code running under another framework's memory pool that owns
+   all device memory, plugins that may not allocate after start-up,
    real-time loops that must not wait on the allocator.  All working memory
    (network structure, descriptor, Newton matrix, result) lives in one
    static device arena of LASSIE_NOALLOC_ARENA_BYTES that every device which
@@ -253,10 +253,13 @@ int lassie_tc_selftest(const float *d_a, const float *d_b, float *d_d, int *d_st
    and d_out[nt*N] (all species sampled) are device buffers owned by the
    caller; stats is host memory (may be NULL).  Networks above the limits
    below are rejected with LASSIE_ERR_TOO_LARGE.  The first call on a device
-   looks up the arena's device address: make it before any stream capture.
+   looks up the arena's device address and keeps it (it does not survive a
+   cudaDeviceReset): make that first call before any stream capture.
    Calls share the arena and keep its last contents (the queue counter and
    the result are cleared per call); calls that overlap on the GPU race, so
-   serialise them.  Returns the instance status; synchronises `stream`. */
+   serialise them.  Returns the instance status; synchronises `stream`, and
+   therefore returns LASSIE_ERR_ARGS without doing anything while `stream`
+   is being captured. */
 #define LASSIE_NOALLOC_MAX_SPECIES 128
 #define LASSIE_NOALLOC_MAX_REACTIONS 256
 #define LASSIE_NOALLOC_MAX_SAMPLES 4096

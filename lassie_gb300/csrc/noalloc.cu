@@ -1,24 +1,27 @@
 // lassie_solve_noalloc: one integration without any device allocation.
 //
 // Some callers cannot call cudaMalloc: a host that runs inside another
-// framework's memory pool or a CUDA-graph capture, a plugin whose process
-// forbids driver allocations after start-up, a real-time loop that must not
-// block on the allocator.  This entry point gives them the integrator with
-// all of its working memory in one fixed arena compiled into the library: a
-// file-scope static __device__ array of LASSIE_NOALLOC_ARENA_BYTES bytes that
-// every device which loads the library holds until the process exits.  The
-// caller passes device buffers for the inputs (k, x0, t) and for the
-// trajectory; the network structure, the instance descriptor, the Newton
-// matrix, the diagonal-block inverses, the work-queue counter and the
-// per-instance result all live in the arena.
+// framework's memory pool (which owns all device memory and forbids outside
+// allocations), a plugin whose process forbids driver allocations after
+// start-up, a real-time loop that must not block on the allocator.  This
+// entry point gives them the integrator with all of its working memory in
+// one fixed arena compiled into the library: a file-scope static __device__
+// array of LASSIE_NOALLOC_ARENA_BYTES bytes that every device which loads the
+// library holds until the process exits.  The caller passes device buffers
+// for the inputs (k, x0, t) and for the trajectory; the network structure,
+// the instance descriptor, the Newton matrix, the diagonal-block inverses,
+// the work-queue counter and the per-instance result all live in the arena.
 //
 // Set-up: the first call on a device takes the arena's device address with
 // cudaGetSymbolAddress (host code must not use the array's name as an
-// address) and keeps it for that device; make that first call before any
-// stream capture.  Every call shares the arena, which keeps the previous
-// call's contents: the work-queue counter and the result are cleared on each
-// call, everything else is overwritten.  Calls that overlap on the GPU (two
-// host threads, or two streams) race on the arena: serialise them.
+// address: it is a host-side stand-in) and keeps it for that device; make
+// that first call before any stream capture.  The kept address does not
+// survive a cudaDeviceReset of that device.  Every call shares the arena,
+// which keeps the previous call's contents: the work-queue counter and the
+// result are cleared on each call, everything else is overwritten.  Calls
+// that overlap on the GPU (two host threads, or two streams) race on the
+// arena: serialise them.  A call synchronises its stream before it returns,
+// so it refuses (LASSIE_ERR_ARGS) a stream that is being captured.
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -88,6 +91,19 @@ extern "C" int lassie_solve_noalloc(const lassie_model *model, const double *d_k
         return set_error_noalloc(LASSIE_ERR_ARGS, "noalloc: precision");
     if (o.controller != LASSIE_CTRL_COMPAT)
         return set_error_noalloc(LASSIE_ERR_ARGS, "noalloc: LASSIE's controller only");
+    {
+        // the call ends with a synchronisation of the stream, which would
+        // invalidate a capture in progress
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess) {
+            cudaGetLastError();
+            return set_error_noalloc(LASSIE_ERR_CUDA, "noalloc: cudaStreamIsCapturing failed");
+        }
+        if (cap != cudaStreamCaptureStatusNone)
+            return set_error_noalloc(LASSIE_ERR_ARGS,
+                                     "noalloc: the stream is being captured; this call "
+                                     "synchronises its stream and cannot run inside a capture");
+    }
     std::vector<int32_t> ints;
     int32_t N = 0, R = 0, na = 0, nh = 0;
     int64_t offs[8];
