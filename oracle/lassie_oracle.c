@@ -249,6 +249,89 @@ void lo_lu_solve(int n, const double *lu, const int *piv, double *b) {
     }
 }
 
+/* ------------------------------------------------- quarter root, exactly
+   x^(1/4) rounded to nearest, for x > 0 finite: start from sqrt(sqrt(x))
+   (within an ulp or two) and move to a neighbour while the midpoint between
+   the two lies on the other side of x^(1/4), deciding each step by an exact
+   integer comparison of the midpoint's fourth power with x (the midpoint
+   m = M 2^e has a 54-bit odd M, so m^4 is never a double and no tie
+   occurs). */
+typedef struct {
+    uint64_t w[4]; /* little-endian 64-bit limbs */
+} lo_u256;
+
+static void u256_add_at(lo_u256 *a, int limb, unsigned __int128 v) {
+    for (int i = limb; i < 4 && v; i++) {
+        unsigned __int128 t = (unsigned __int128)a->w[i] + (uint64_t)v;
+        a->w[i] = (uint64_t)t;
+        v = (v >> 64) + (t >> 64);
+    }
+}
+
+static int u256_bitlen(const lo_u256 *a) {
+    for (int i = 3; i >= 0; i--)
+        if (a->w[i]) return 64 * i + 64 - __builtin_clzll(a->w[i]);
+    return 0;
+}
+
+/* sign of (M^4 2^(4e)) - (X 2^f), M < 2^55, X < 2^53, both > 0 */
+static int cmp_pow4(uint64_t M, int e, uint64_t X, int f) {
+    const unsigned __int128 m2 = (unsigned __int128)M * M; /* < 2^110 */
+    const uint64_t lo = (uint64_t)m2, hi = (uint64_t)(m2 >> 64);
+    lo_u256 P = {{0, 0, 0, 0}};
+    u256_add_at(&P, 0, (unsigned __int128)lo * lo);
+    u256_add_at(&P, 1, (unsigned __int128)lo * hi);
+    u256_add_at(&P, 1, (unsigned __int128)lo * hi);
+    u256_add_at(&P, 2, (unsigned __int128)hi * hi);
+    const int d = f - 4 * e; /* compare P with X 2^d */
+    const int bp = u256_bitlen(&P), bx = 64 - __builtin_clzll(X);
+    if (bp != bx + d) return bp > bx + d ? 1 : -1;
+    /* same bit length, d = bp - bx >= 0: X << d fits in 256 bits */
+    lo_u256 Q = {{0, 0, 0, 0}};
+    const int limb = d / 64, sh = d % 64;
+    Q.w[limb] = X << sh;
+    if (sh && limb + 1 < 4) Q.w[limb + 1] = X >> (64 - sh);
+    for (int i = 3; i >= 0; i--)
+        if (P.w[i] != Q.w[i]) return P.w[i] > Q.w[i] ? 1 : -1;
+    return 0;
+}
+
+/* v = V 2^ev with V a 53-bit (or shorter, subnormal) integer */
+static void split_double(double v, uint64_t *V, int *ev) {
+    int e;
+    const double fr = frexp(v, &e);
+    *V = (uint64_t)ldexp(fr, 53);
+    *ev = e - 53;
+}
+
+/* sign of ((a + b) / 2)^4 - x for adjacent positive doubles a < b */
+static int mid4_cmp(double a, double x) {
+    uint64_t A, X;
+    int ea, ex;
+    split_double(a, &A, &ea);
+    split_double(x, &X, &ex);
+    return cmp_pow4(2 * A + 1, ea - 1, X, ex);
+}
+
+double lo_qroot_rn(double x) {
+    if (!(x > 0) || isinf(x)) return sqrt(sqrt(x));
+    double y = sqrt(sqrt(x));
+    for (int it = 0; it < 8; it++) {
+        const double up = nextafter(y, INFINITY);
+        if (mid4_cmp(y, x) < 0) { /* x^(1/4) above the midpoint to up */
+            y = up;
+            continue;
+        }
+        const double dn = nextafter(y, 0.0);
+        if (dn > 0 && mid4_cmp(dn, x) > 0) { /* below the midpoint to dn */
+            y = dn;
+            continue;
+        }
+        break;
+    }
+    return y;
+}
+
 /* ------------------------------------------------------------- integrator */
 
 /* Simulation.cuh:632-925 with kernels.cuh:68-199, 289-300, 393-402, 462-477,
@@ -281,6 +364,27 @@ static uint64_t g_perturb_state = 0;
 void lo_set_solve_perturbation(double rel, uint64_t seed) {
     g_perturb_rel = rel;
     g_perturb_state = seed * 0x9E3779B97F4A7C15ull + 1;
+}
+
+/* The same for the RKF45 step-size factor: (atol/R)^(1/4) scaled by
+   (1 +- g_root_rel), a quarter root one ulp away from this one on every
+   evaluation (the reference's CUDA pow() is not correctly rounded on every
+   input). */
+static double g_root_rel = 0.0;
+static uint64_t g_root_state = 0;
+
+void lo_set_root_perturbation(double rel, uint64_t seed) {
+    g_root_rel = rel;
+    g_root_state = seed * 0xD1B54A32D192ED03ull + 7;
+}
+
+static double lo_root_perturb(double v) {
+    uint64_t z = g_root_state;
+    z ^= z << 13;
+    z ^= z >> 7;
+    z ^= z << 17;
+    g_root_state = z;
+    return v * ((z & 1) ? 1.0 + g_root_rel : 1.0 - g_root_rel);
 }
 
 static void lo_perturb(int n, double *dx) {
@@ -333,6 +437,8 @@ static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
         o.stiffness_tol = 1e-6;
         o.newton_iter = 10000;
         o.max_steps = 0;
+        o.use_pow = 0;
+        o.pad = 0;
     }
     lo_stats st;
     memset(&st, 0, sizeof(st));
@@ -446,7 +552,11 @@ static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
             }
             /* kernels.cuh:184-199 */
             double R = fabs(w1[s] - w2[s]) / dt;
-            delta[s] = 0.84 * sqrt(sqrt(tol[s] / R));
+            const double q = tol[s] / R;
+            double qr = o.use_pow == 1 ? pow(q, 0.25) : o.use_pow == 2 ? lo_qroot_rn(q)
+                                                                       : sqrt(sqrt(q));
+            if (g_root_rel > 0) qr = lo_root_perturb(qr);
+            delta[s] = 0.84 * qr;
             if (R <= tol[s] && !isnan(R) && !isinf(R) && w1[s] > 0) count++;
             /* thrust::min_element: first element, replaced only by a strictly
                smaller one (a leading NaN therefore sticks) */

@@ -13,8 +13,10 @@
  *     it, with no contraction (compiled with -ffp-contract=off);
  *   - the LU and the triangular solves accumulate with fma() in ascending
  *     pivot order (forward) and descending order (backward);
- *   - the RKF45 step-size factor (atol/R)^(1/4) is sqrt(sqrt(atol/R)), which
- *     is correctly rounded on every IEEE platform (the reference calls pow());
+ *   - the RKF45 step-size factor (atol/R)^(1/4) is sqrt(sqrt(atol/R)), the
+ *     same on every IEEE platform, or (use_pow) pow(atol/R, 0.25) as the
+ *     reference writes it, which the C library and CUDA both round
+ *     correctly on the golden cases;
  *   - the Newton norm squares are rounded to float before summation, as the
  *     reference's `square` functor does (Simulation.cuh:58-64).
  */
@@ -50,6 +52,11 @@ typedef struct {
     double stiffness_tol;  /* default 1e-6  (Simulation.cuh:308-315) */
     int64_t newton_iter;   /* default 10000 (Simulation.cuh:290-297) */
     int64_t max_steps;     /* loop-iteration cap; <=0 means unlimited */
+    int32_t use_pow;       /* (atol/R)^(1/4), the reference's pow() call
+                              (kernels.cuh:193): 0 (default) sqrt(sqrt());
+                              1 the C library's pow(); 2 correctly rounded
+                              (lo_qroot_rn) */
+    int32_t pad;
 } lo_opts;
 
 typedef struct {
@@ -74,6 +81,9 @@ typedef struct {
 /* Tests only: multiply each Newton correction componentwise by (1 +- rel)
    with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
 void lo_set_solve_perturbation(double rel, uint64_t seed);
+/* Tests only: scale every RKF45 quarter root (atol/R)^(1/4) by (1 +- rel)
+   with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
+void lo_set_root_perturbation(double rel, uint64_t seed);
 /* Tests only: pick the LU's rounding order (0 default; 1 the triangular
    solves, 2 the Schur update, 3 both, round products and sums separately
    instead of using fma); process-global, not thread safe. */
@@ -82,6 +92,9 @@ void lo_set_lu_variant(int v);
 int lo_model_build(int n_reactions, int n_species, const int32_t *left,
                    const int32_t *right, lo_model *out);
 void lo_model_free(lo_model *m);
+
+/* x^(1/4) rounded to nearest (x > 0 finite; otherwise sqrt(sqrt(x))) */
+double lo_qroot_rn(double x);
 
 /* dx = f(x) -- kernels.cuh:5-63 */
 void lo_rhs(const lo_model *m, const double *k, const double *x, double *dx);

@@ -34,7 +34,8 @@ class _Model(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("rkf_step", C.c_double), ("be_step", C.c_double),
                 ("newton_tol", C.c_double), ("stiffness_tol", C.c_double),
-                ("newton_iter", C.c_int64), ("max_steps", C.c_int64)]
+                ("newton_iter", C.c_int64), ("max_steps", C.c_int64),
+                ("use_pow", C.c_int32), ("pad", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -88,6 +89,9 @@ def lib():
             L.lo_lu_solve.argtypes = [C.c_int, _f64p, _i32p, _f64p]
             L.lo_set_solve_perturbation.argtypes = [C.c_double, C.c_uint64]
             L.lo_set_lu_variant.argtypes = [C.c_int]
+            L.lo_set_root_perturbation.argtypes = [C.c_double, C.c_uint64]
+            L.lo_qroot_rn.argtypes = [C.c_double]
+            L.lo_qroot_rn.restype = C.c_double
             L.lo_solve_compat.argtypes = [C.POINTER(_Model), _f64p, _f64p, C.c_void_p,
                                           C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Opts), _f64p, C.POINTER(Stats)]
@@ -150,8 +154,19 @@ class OracleModel:
         return J
 
 
-def make_opts(model=None, max_steps: int = 0) -> Opts:
+# the step-size factor (atol/R)^(1/4): sqrt(sqrt()), the C library's pow(),
+# or correctly rounded
+ROOTS = {"sqrt": 0, "libm": 1, "rn": 2}
+
+
+def make_opts(model=None, max_steps: int = 0, root: str = "sqrt") -> Opts:
+    """Options of a solve; ``root`` picks how the step-size factor
+    (atol/R)^(1/4) is computed (``ROOTS``): "rn" correctly rounded, which
+    is what the reference's pow() call returns on the golden cases."""
+    if root not in ROOTS:
+        raise ValueError("root must be one of " + ", ".join(ROOTS))
     o = Opts()
+    o.use_pow = ROOTS[root]
     o.rkf_step = getattr(model, "rkf_step", 1e-3)
     o.be_step = getattr(model, "be_step", 0.01)
     o.newton_tol = getattr(model, "newton_tol", 1e-6)
@@ -165,9 +180,9 @@ def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
-def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None):
-    """Integrate a ``lassie_gb300.model.Model`` with the oracle.
-    Returns (trajectory [nt, ncs], stats dict, status)."""
+def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None, root: str = "sqrt"):
+    """Integrate a ``lassie_gb300.model.Model`` with the oracle (``root`` as
+    in ``make_opts``).  Returns (trajectory [nt, ncs], stats dict, status)."""
     om = om or OracleModel(model.left, model.right)
     N = model.n_species
     k = np.ascontiguousarray(model.k, np.float64)
@@ -178,7 +193,7 @@ def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None):
     atol = None if model.atol is None else np.ascontiguousarray(model.atol[:N], np.float64)
     out = np.zeros((t.shape[0], cs.shape[0]))
     st = Stats()
-    o = make_opts(model, max_steps)
+    o = make_opts(model, max_steps, root)
     rc = lib().lo_solve_compat(C.byref(om._m), k, x0, _ptr(feed), _ptr(atol), t,
                                t.shape[0], _ptr(cs), cs.shape[0], C.byref(o), out,
                                C.byref(st))
@@ -238,7 +253,7 @@ def solve_recorded(model, cap: int = 1_000_000):
     return out, st.as_dict(), rc, kind[:n].copy(), dts[:n].copy(), samp[: t.shape[0]].copy()
 
 
-def solve_batch(models: Sequence, threads: int = 0, max_steps: int = 0):
+def solve_batch(models: Sequence, threads: int = 0, max_steps: int = 0, root: str = "sqrt"):
     """Solve independent instances (all species sampled, no feed, default
     atol) on ``threads`` host threads.  Returns (list of trajectories, list
     of stats dicts, statuses)."""
@@ -258,7 +273,7 @@ def solve_batch(models: Sequence, threads: int = 0, max_steps: int = 0):
     nt = np.array([m.t.shape[0] for m in models], np.int32)
     stats = (Stats * n)()
     status = np.zeros(n, np.int32)
-    o = make_opts(models[0] if n else None, max_steps)
+    o = make_opts(models[0] if n else None, max_steps, root)
     lib().lo_solve_batch(n, mp, arr(ks), arr(xs), arr(ts), nt, C.byref(o), arr(outs),
                          C.cast(stats, C.c_void_p), status, threads)
     return outs, [s.as_dict() for s in stats], status
@@ -291,6 +306,23 @@ class solve_perturbation:
 
     def __exit__(self, *exc):
         lib().lo_set_solve_perturbation(0.0, 0)
+        return False
+
+
+class root_perturbation:
+    """Context manager: inside it, every RKF45 quarter root (atol/R)^(1/4)
+    is scaled by (1 +- rel) with seeded signs -- a pow() that is off by an
+    ulp.  Single-threaded use only."""
+
+    def __init__(self, rel: float, seed: int = 1):
+        self.rel, self.seed = float(rel), int(seed)
+
+    def __enter__(self):
+        lib().lo_set_root_perturbation(self.rel, self.seed)
+        return self
+
+    def __exit__(self, *exc):
+        lib().lo_set_root_perturbation(0.0, 0)
         return False
 
 

@@ -8,8 +8,9 @@ reference binary needs a CUDA GPU, so this runs on the GPU machine:
     python tests/golden/make_golden.py <out_dir>
 
 Each fixture holds the dense stoichiometries, rate constants, initial state,
-sampling times, the reference's trajectory (``ref``), its integration time
-and the command's exit status.
+sampling times, the reference's trajectory (``ref``), its number of loop
+iterations (``ref_outer_iters``, the lines of its ProgressSimulation) and
+its integration time.
 """
 from __future__ import annotations
 
@@ -67,6 +68,10 @@ def main(out_dir: str) -> int:
             mt = re.search(r"LASSIE_REF integration_ms ([0-9.eE+-]+)", r.stderr)
             sol_path = os.path.join(outp, "output", "Solution")
             sol = read_solution(sol_path, m.n_species + 1) if os.path.exists(sol_path) else None
+            # the reference writes one ProgressSimulation line per loop
+            # iteration (Simulation.cuh:671-673)
+            prog = os.path.join(outp, "output", "ProgressSimulation")
+            outer = sum(1 for ln in open(prog) if ln.strip()) if os.path.exists(prog) else -1
         if r.returncode != 0 or sol is None:
             print(f"{name}: reference failed rc={r.returncode}\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
             status = 1
@@ -74,7 +79,7 @@ def main(out_dir: str) -> int:
         np.savez_compressed(
             os.path.join(out_dir, name + ".npz"), left=m.left, right=m.right, k=m.k,
             x0=m.x0, t=m.t, feed=(m.feed if m.feed is not None else np.zeros(0)),
-            ref_t=sol[:, 0], ref=sol[:, 1:], wall_s=wall,
+            ref_t=sol[:, 0], ref=sol[:, 1:], wall_s=wall, ref_outer_iters=outer,
             integration_ms=float(mt.group(1)) if mt else -1.0)
         print(f"{name}: N={m.n_species} nt={m.t.shape[0]} wall={wall:.2f}s "
               f"integration_ms={mt.group(1) if mt else '?'}")
