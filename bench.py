@@ -154,28 +154,66 @@ def max_rel_err(a_list, b_list):
     return worst, bad
 
 
-def cpu_baseline(n_total, threads=None, stride=64, t_frac=0.1, max_steps=25000):
-    """The oracle port on the host cores: every `stride`-th instance of the
-    workload on the first `t_frac` of its horizon (loop-iteration cap scaled
-    alike), extrapolated to the horizon; completed instances only."""
+# The CPU sample, the same for the reference arm and the cpu_baseline key:
+# every 128th instance of the workload (16 instances, one per host core of
+# the GPU machine) on the first 5 % of its horizon, loop-iteration cap scaled
+# alike; sims/s extrapolated to the whole horizon.  `--cpu-full-horizon`
+# runs the same 16 instances over the whole horizon once, which is how the
+# extrapolation is checked.
+CPU_STRIDE, CPU_T_FRAC = 128, 0.05
+
+
+def cpu_sample_models(n_total, t_frac=CPU_T_FRAC, stride=CPU_STRIDE):
     from lassie_gb300 import synth
-    from oracle import oracle as O
     idx = list(range(0, n_total, stride))
-    models = [synth.shorten(synth.make_c4_instance(q), 20.0 * t_frac,
-                            max(2, int(round(50 * t_frac))))
-              for q in idx]
+    if t_frac >= 1.0:
+        return [synth.make_c4_instance(q) for q in idx]
+    return [synth.shorten(synth.make_c4_instance(q), 20.0 * t_frac,
+                          max(2, int(round(50 * t_frac))))
+            for q in idx]
+
+
+def flush_host_caches(buf=[]):
+    """Write 256 MB of host memory (more than the host's caches) before a
+    timed CPU step, as the GPU arm flushes its L2."""
+    import numpy as np
+    if not buf:
+        buf.append(np.empty(256 * 1024 * 1024 // 8))
+    buf[0].fill(1.0)
+
+
+def cpu_baseline(n_total, threads=None, stride=CPU_STRIDE, t_frac=CPU_T_FRAC, max_steps=25000):
+    """The oracle port (the reference algorithm) on the host cores: every
+    `stride`-th instance of the workload on the first `t_frac` of its horizon
+    (loop-iteration cap scaled alike), extrapolated to the horizon; completed
+    instances only."""
+    from oracle import oracle as O
+    models = cpu_sample_models(n_total, t_frac, stride)
     threads = threads or os.cpu_count() or 1
+    frac = min(1.0, t_frac)
+    flush_host_caches()
     t0 = time.perf_counter()
-    _, _, status = O.solve_batch(models, threads=threads,
-                                 max_steps=max(1, int(max_steps * t_frac)))
+    _, stats, status = O.solve_batch(models, threads=threads,
+                                     max_steps=max(1, int(max_steps * frac)))
     dt = time.perf_counter() - t0
     done = sum(1 for s in status if s == 0)
-    sims = done / (dt / t_frac)
+    sims = done / (dt / frac)
     return {"value": sims, "unit": "sims/s", "cores": threads, "kind": "port",
             "sample": f"{len(models)} of the {n_total} instances (every {stride}th, "
-                      f"{done} completed), t in [0,{20.0 * t_frac:g}] (= {t_frac:g} of the "
-                      f"horizon), time scaled by {1 / t_frac:g}; {dt:.2f} s wall",
-            "seconds": dt}
+                      f"{done} completed), t in [0,{20.0 * frac:g}] (= {frac:g} of the "
+                      f"horizon), time scaled by {1 / frac:g}; {dt:.2f} s wall",
+            "seconds": dt, "be_steps": sum(st["be_steps"] for st in stats),
+            "capped": sum(1 for s in status if s != 0)}
+
+
+def run_cpu_full_horizon(args):
+    """The CPU sample over the whole horizon next to its extrapolated
+    short-horizon figure (one JSON line; tens of minutes)."""
+    short = cpu_baseline(args.instances, max_steps=args.max_steps)
+    full = cpu_baseline(args.instances, t_frac=1.0, max_steps=args.max_steps)
+    print(json.dumps({"cpu_sample_extrapolated": short, "cpu_sample_full_horizon": full,
+                      "full_over_extrapolated": full["value"] / short["value"]}), flush=True)
+    return 0
 
 
 def _lsoda_one(q):
@@ -237,13 +275,11 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from lassie_gb300 import synth  # noqa: F401
-    stride, t_frac = 128, 0.05
     for _ in range(args.warmup):
-        cpu_baseline(args.instances, stride=stride, t_frac=t_frac, max_steps=args.max_steps)
+        cpu_baseline(args.instances, max_steps=args.max_steps)
     vals, secs = [], []
     for _ in range(args.steps):
-        cb = cpu_baseline(args.instances, stride=stride, t_frac=t_frac, max_steps=args.max_steps)
+        cb = cpu_baseline(args.instances, max_steps=args.max_steps)
         vals.append(cb["value"])
         secs.append(cb["seconds"])
     v = statistics.mean(vals)
@@ -251,15 +287,24 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "sims/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * statistics.mean(secs), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "reference algorithm, CPU (oracle port)",
-                   "max_steps_per_instance": args.max_steps, "l2": "n/a (host)"},
+        "scaling": args.scaling, "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args),
+        "form": "reference algorithm, CPU (oracle port)",
         "cpu_baseline": {"value": v, "unit": "sims/s", "cores": cb["cores"], "kind": "port",
                          "sample": cb["sample"]},
         "e2e": {"value": v, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def workload_config(args):
+    """The `config` of both arms' lines: the workload and its loop cap."""
+    full = args.instances == 2048 and args.horizon == 20.0
+    return {"workload": WORKLOAD if full else
+            f"{WORKLOAD} -- reduced: {args.instances} instances, t in [0,{args.horizon:g}]",
+            "max_steps_per_instance": args.max_steps,
+            "l2": "flushed between steps (256 MB write)"}
 
 
 def rhs_bandwidth(torch, stream, n_inst=65536, reps=20, warm=3):
@@ -555,11 +600,19 @@ def main():
                          "kernels: the RHS and Newton-matrix kernels alone")
     ap.add_argument("--tensor-cores", action="store_true",
                     help="c3: rank-32 updates of the factorisation on the tensor cores")
+    ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
+                    help="weak: every rank integrates its own --instances instances "
+                         "(default); strong: the ranks split one batch of --instances")
+    ap.add_argument("--cpu-full-horizon", action="store_true",
+                    help="run the CPU sample over the whole horizon next to its "
+                         "extrapolated short-horizon figure, then exit (no GPU)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64-form, RHS and CPU-baseline measurements")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.cpu_full_horizon:
+        return run_cpu_full_horizon(args)
     if args.workload == "c3":
         return run_c3(args)
     if args.workload == "kernels":
@@ -579,9 +632,13 @@ def main():
     if not L.lassie_device_ok():
         raise RuntimeError("no sm_103 device")
 
-    # weak scaling: every rank integrates its own 2048 instances
-    ids = sharding.weak_shard(args.instances, rank)
-    models = synth.make_c4(args.instances, first=ids.start)
+    if args.scaling == "weak":
+        # weak scaling: every rank integrates its own 2048 instances
+        ids = list(sharding.weak_shard(args.instances, rank))
+    else:
+        # strong scaling: one fixed batch split over the ranks by cost
+        ids = sharding.cost_shard(synth.c4_sizes(args.instances), world)[rank]
+    models = [synth.make_c4_instance(q) for q in ids]
     if args.horizon != 20.0:
         models = [synth.shorten(m, args.horizon, max(2, int(round(50 * args.horizon / 20))))
                   for m in models]
@@ -645,16 +702,13 @@ def main():
 
     line = {"metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded, numpy default_rng(1000*4 + instance))",
-            "config": {"workload": WORKLOAD if (args.instances == 2048 and args.horizon == 20.0)
-                       else f"{WORKLOAD} -- reduced: {args.instances} instances, t in [0,{args.horizon:g}]",
-                       "instances_per_gpu": args.instances,
-                       "max_steps_per_instance": args.max_steps,
-                       "completed_instances": done_all, "capped_instances": capped,
-                       "form": "mixed (FP32 LU + FP64 refinement)",
-                       "parallelism": f"instances sharded over {world} GPU(s)",
-                       "l2": "flushed between steps (256 MB write)"},
+            "higher_is_better": True, "scaling": args.scaling, "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded, numpy default_rng(1000*4 + instance))",
+            "config": workload_config(args),
+            "run": {"instances_per_gpu": len(models), "completed_instances": done_all,
+                    "capped_instances": capped, "form": "mixed (FP32 LU + FP64 refinement)",
+                    "parallelism": f"instances sharded over {world} GPU(s) "
+                                   f"({args.scaling} scaling)"},
             "failed_instances": len(bad),
             "e2e": {"value": e2e_val, "unit": "sims/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -105,6 +105,13 @@ def make_sized(N: int, instance: int = 0) -> Model:
     return Model(left=left, right=right, k=k, x0=x0, t=np.linspace(0.0, 20.0, 50))
 
 
+def c4_sizes(n_instances: int = 2048, first: int = 0) -> List[int]:
+    """Species counts of the batched workload's instances (the first draw of
+    each instance's generator), without building the networks."""
+    return [int(np.random.default_rng(1000 * 4 + q).integers(32, 513))
+            for q in range(first, first + n_instances)]
+
+
 def make_c4(n_instances: int = 2048, first: int = 0) -> List[Model]:
     return [make_c4_instance(first + q) for q in range(n_instances)]
 

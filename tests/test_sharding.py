@@ -55,3 +55,16 @@ def test_gloo_max_over_ranks():
     assert res[0][2] == res[1][2] == 2.0
     assert res[0][3] == res[1][3] == 7.0
     assert set(res[0][1]).isdisjoint(res[1][1])
+
+
+def test_strong_split_of_the_batched_workload():
+    """bench.py --scaling strong: the 2048-instance batch split over 8 ranks
+    by cost covers every instance once, with the N^3 loads within 1 %."""
+    from lassie_gb300 import synth
+    sizes = synth.c4_sizes(2048)
+    assert sizes[:5] == [synth.make_c4_instance(q).n_species for q in range(5)]
+    for world in (2, 4, 8):
+        parts = sharding.cost_shard(sizes, world)
+        assert sorted(q for p in parts for q in p) == list(range(2048))
+        loads = [sum(sizes[q] ** 3 for q in p) for p in parts]
+        assert max(loads) / min(loads) < 1.01
