@@ -522,8 +522,10 @@ def run_c3(args):
     if horizon != 50.0:
         m = synth.shorten(m, horizon, max(2, int(round(100 * horizon / 50)) + 1))
     stream = torch.cuda.Stream()
+    # BF16 factors need more refinement sweeps than the default cap of 8
+    refine_max = 32 if args.tensor_cores == "bf16" else 0
     batch = solver.Batch([m], engine="mixed", max_steps=args.max_steps * 10, deadline_s=1800,
-                         tensor_cores=args.tensor_cores)
+                         tensor_cores=args.tensor_cores, refine_max=refine_max)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -548,7 +550,7 @@ def run_c3(args):
     wall = t1 - t0
     s0 = time.perf_counter()
     _, st_e2e = solver.simulate(m, engine="mixed", max_steps=args.max_steps * 10, deadline_s=1800,
-                                tensor_cores=args.tensor_cores)
+                                tensor_cores=args.tensor_cores, refine_max=refine_max)
     e2e = 1.0 / (time.perf_counter() - s0)
     peaks, peak_kind = load_peaks()
     n = float(m.n_species)
@@ -564,7 +566,7 @@ def run_c3(args):
             "config": {"workload": f"c3: 4096 species x 4096 reactions, 2 reactants + 2 products, "
                                    f"k~10^U(-4,2), t in [0,{horizon:g}]",
                        "form": "mixed (FP32 Gauss-Jordan inverse + FP64 refinement), wide engine",
-                       "tensor_cores": bool(args.tensor_cores),
+                       "tensor_cores": args.tensor_cores,
                        "l2": "flushed between steps (256 MB write)"},
             "status": st["status"],
             "steps_taken": {"be": st["be_steps"], "rkf": st["rkf_accepts"],
@@ -598,8 +600,11 @@ def main():
                     help="c4: the 2048-instance batch (default); c3: the 4096-species "
                          "network on the wide engine (t in [0, 50], or --horizon); "
                          "kernels: the RHS and Newton-matrix kernels alone")
-    ap.add_argument("--tensor-cores", action="store_true",
-                    help="c3: rank-32 updates of the factorisation on the tensor cores")
+    ap.add_argument("--tensor-cores", nargs="?", const="tf32", default="off",
+                    choices=["off", "tf32", "bf16"],
+                    help="c3: rank-32 updates of the factorisation on the tensor cores, with "
+                         "split TF32 operands (tf32, the flag alone) or BF16 operands and "
+                         "FP32 accumulation (bf16)")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="weak: every rank integrates its own --instances instances "
                          "(default); strong: the ranks split one batch of --instances")
@@ -707,6 +712,7 @@ def main():
             "config": workload_config(args),
             "run": {"instances_per_gpu": len(models), "completed_instances": done_all,
                     "capped_instances": capped, "form": "mixed (FP32 LU + FP64 refinement)",
+                    "tile_rows": {str(r): batch.tile_rows().count(r) for r in (8, 4, 2)},
                     "parallelism": f"instances sharded over {world} GPU(s) "
                                    f"({args.scaling} scaling)"},
             "failed_instances": len(bad),

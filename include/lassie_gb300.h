@@ -60,6 +60,12 @@ extern "C" {
 /* precision of the Newton matrix factorisation */
 #define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */
 #define LASSIE_PREC_MIXED 1 /* FP32 LU + FP64 iterative refinement */
+#define LASSIE_PREC_FLOAT 2 /* the reference's -p float mode (Simulation<float>,
+                               simulator.cu:289-294): state, rate constants,
+                               stages and Newton matrix in float, double
+                               temporaries where the reference has them;
+                               LASSIE's controller, networks of at most 512
+                               species */
 
 typedef struct lassie_model lassie_model;
 typedef struct lassie_batch lassie_batch;
@@ -87,10 +93,13 @@ typedef struct {
                              (the refinement still converges to the FP64 solve of
                              the current matrix); 0 factors at every step */
     int32_t tensor_cores; /* wide engine (networks above 512 species), mixed
-                             form: 1 runs the rank-32 updates of the
-                             factorisation on the tensor cores (tcgen05, TF32
-                             products of split operands), 0 (default) on the
-                             FP32 pipes */
+                             form: LASSIE_TC_TF32 runs the rank-32 updates of
+                             the factorisation on the tensor cores (tcgen05,
+                             TF32 products of split operands, close to FP32),
+                             LASSIE_TC_BF16 with BF16 operands and FP32
+                             accumulation (factors good to about 2^-9; the FP64
+                             refinement takes more sweeps), LASSIE_TC_OFF
+                             (default) on the FP32 pipes */
     int32_t controller;   /* LASSIE_CTRL_* (default LASSIE_CTRL_COMPAT) */
     /* LASSIE_CTRL_BDF only: */
     double rtol;          /* relative tolerance (1e-6) */
@@ -100,8 +109,20 @@ typedef struct {
     double first_step;    /* 0 = chosen from f(x0) */
     double max_step;      /* 0 = unbounded */
     int32_t max_order;    /* 1..5 (5) */
-    int32_t pad;
+    /* Rows per thread of the per-CTA factorisation's trailing-update tiles
+       (128 x 16*rows): 0 (default) lets the autotuner time 8, 4 and 2 per
+       network-size band on the device when the batch is created (once per
+       process, device, band and precision) and store its choice in the
+       batch; 8, 4 or 2 fix it.  Every choice gives the same factors bit for
+       bit (each entry sums the same products in the same order); only the
+       speed differs.  Replaces the fixed launch heuristic of the reference
+       (Simulation.cuh:583-600). */
+    int32_t tile_rows;
 } lassie_opts;
+
+#define LASSIE_TC_OFF 0
+#define LASSIE_TC_TF32 1
+#define LASSIE_TC_BF16 2
 
 #define LASSIE_ROOT_POW 0
 #define LASSIE_ROOT_SQRT 1
@@ -241,6 +262,15 @@ int lassie_adjoint_batch(const lassie_instance *inst, int32_t n, const double *c
    `stream`. */
 int lassie_tc_selftest(const float *d_a, const float *d_b, float *d_d, int *d_status,
                        void *stream);
+/* The same tile product with BF16 operands (each entry rounded to nearest
+   BF16) and FP32 accumulation, two kind::f16 MMAs of K = 16: the wide
+   engine's LASSIE_TC_BF16 rank updates (no reference counterpart). */
+int lassie_tc_selftest_bf16(const float *d_a, const float *d_b, float *d_d, int *d_status,
+                            void *stream);
+
+/* The trailing-update rows per thread that the batch uses for each
+   instance (8, 4 or 2; see lassie_opts.tile_rows), rows[n].  Host only. */
+int lassie_batch_tile_rows(const lassie_batch *batch, int32_t *rows);
 
 /* One integration that allocates no device memory (no counterpart in the
    reference, which allocates in every solve).  For callers that cannot call

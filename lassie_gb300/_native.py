@@ -22,6 +22,7 @@ ERR_STEP_TOO_SMALL = -27
 ERR_CUDA = -13
 PREC_FP64 = 0
 PREC_MIXED = 1
+PREC_FLOAT = 2
 CTRL_COMPAT = 0
 CTRL_BDF = 1
 ROOT_POW = 0
@@ -35,7 +36,7 @@ EXPORTS = (
     "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
     "lassie_batch_bytes", "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
     "lassie_newton_matrix_device", "lassie_jacobian_nnz", "lassie_jacobian_pattern",
-    "lassie_lu_solve", "lassie_adjoint_batch", "lassie_solve_noalloc", "lassie_tc_selftest",
+    "lassie_lu_solve", "lassie_adjoint_batch", "lassie_solve_noalloc", "lassie_batch_tile_rows", "lassie_tc_selftest", "lassie_tc_selftest_bf16",
 )
 
 
@@ -47,7 +48,7 @@ class Opts(C.Structure):
                 ("refine_max", C.c_int32), ("quarter_root", C.c_int32), ("lu_reuse", C.c_int32),
                 ("tensor_cores", C.c_int32), ("controller", C.c_int32),
                 ("rtol", C.c_double), ("atol", C.c_double), ("first_step", C.c_double),
-                ("max_step", C.c_double), ("max_order", C.c_int32), ("pad", C.c_int32)]
+                ("max_step", C.c_double), ("max_order", C.c_int32), ("tile_rows", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -126,6 +127,7 @@ def load():
         L.lassie_batch_read.argtypes = [vp, vp, vp]
         L.lassie_batch_launches.argtypes = [vp]
         L.lassie_batch_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
+        L.lassie_batch_tile_rows.argtypes = [vp, vp]
         L.lassie_batch_destroy.argtypes = [vp]
         L.lassie_batch_destroy.restype = None
         L.lassie_rhs_device.argtypes = [vp, i32, vp, vp, vp, vp]
@@ -139,6 +141,7 @@ def load():
         L.lassie_solve_noalloc.argtypes = [vp, vp, vp, vp, i32, C.POINTER(Opts), vp,
                                            C.POINTER(Stats), vp]
         L.lassie_tc_selftest.argtypes = [vp, vp, vp, vp, vp]
+        L.lassie_tc_selftest_bf16.argtypes = [vp, vp, vp, vp, vp]
         for name in EXPORTS:
             f = getattr(L, name)
             if f.restype is C.c_int and name not in ("lassie_device_ok",):

@@ -26,7 +26,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC",
               "-I" + INCLUDE, "-I" + CSRC] + ARCH
 
-SOURCES = ["compat_engine.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["compat_engine.cu", "capi.cu", "noalloc.cu", "float_mode.cu"]
+# The reference's single-precision mode is compiled with the reference's own
+# device flags (fast float division, pow and sqrt, flush-to-zero, FMA
+# contraction), so that its float expressions round as the reference's do.
+FILE_FLAGS = {"float_mode.cu": ["-std=c++17", "-O3", "--use_fast_math", "-lineinfo", "-Xcompiler",
+                                "-fPIC", "-I" + INCLUDE, "-I" + CSRC] + ARCH}
 
 
 def _nvcc() -> str:
@@ -62,7 +67,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         o = os.path.join(OUT, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc] + FILE_FLAGS.get(src, NVCC_FLAGS) + ["-c", s, "-o", o])
     if jobs:
         with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             for _ in ex.map(_run, jobs):

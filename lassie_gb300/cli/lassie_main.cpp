@@ -285,12 +285,12 @@ int main(int argc, char *argv[]) {
     lassie_opts opts;
     lassie_opts_default(&opts);
     opts.precision = engine == "fp64" ? LASSIE_PREC_FP64 : LASSIE_PREC_MIXED;
-    // the reference's -p float integrates with float state (Simulation<float>);
-    // this engine keeps the state, the RHS and the step control in FP64
-    // (-engine mixed factors in FP32), so -p float is accepted and reported
-    if (prec == "float")
-        std::fprintf(stderr, "Note: -p float is accepted for compatibility; the state is "
-                             "integrated in FP64 (-engine %s)\n", engine.c_str());
+    // -p float: the reference's single-precision loop (Simulation<float>,
+    // simulator.cu:289-294), whatever -engine says
+    if (prec == "float") {
+        if (controller == "bdf") fail(-6, "Error: -p float runs LASSIE's controller only");
+        opts.precision = LASSIE_PREC_FLOAT;
+    }
     opts.quarter_root = root_sqrt ? LASSIE_ROOT_SQRT : LASSIE_ROOT_POW;
     if (controller == "bdf") {
         opts.controller = LASSIE_CTRL_BDF;

@@ -9,6 +9,7 @@
 #include <mutex>
 #include <new>
 #include <numeric>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -42,6 +43,12 @@ cudaError_t lu_solve_launch(int N, void *A, int ld, const double *b, double *x, 
 int64_t lu_solve_smem(int N, int precision);
 int64_t adjoint_smem_bytes(int nmax, int rmax, int amax, int hmax);
 cudaError_t adjoint_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
+int64_t tune_factor_smem(int N, int precision);
+int64_t float_smem_bytes(int nmax, int rmax, int amax, int hmax);
+cudaError_t float_configure(int64_t smem);
+cudaError_t float_launch(const LaunchParams &P, int grid, int64_t smem, cudaStream_t stream);
+cudaError_t tune_factor_launch(int precision, int N, int rm, int reps, void *ws,
+                               int64_t ws_stride, int grid, int *fails, cudaStream_t stream);
 }  // namespace lassie
 
 using namespace lassie;
@@ -293,7 +300,7 @@ extern "C" void lassie_opts_default(lassie_opts *o) {
     o->first_step = 0.0;
     o->max_step = 0.0;
     o->max_order = 5;
-    o->pad = 0;
+    o->tile_rows = 0;
 }
 
 extern "C" const char *lassie_status_string(int s) {
@@ -399,16 +406,95 @@ static int validate_instance(const lassie_instance &q) {
     return LASSIE_OK;
 }
 
+// ------------------------------------------------------------ autotuner
+// The per-CTA factorisation's trailing update runs in 128 x 16*rows tiles;
+// rows = 8 suits large networks (register blocking), 4 or 2 keep more of the
+// CTA busy on small ones.  Per network-size band the candidates are timed on
+// the device -- every CTA of the batch's grid factoring a test matrix of the
+// band's size, three times, after a warm-up -- and the fastest is kept
+// unless the default (8) is within 5 %.  Choices are cached per device,
+// precision, size and grid, so a process decides once and later batches
+// repeat the decision.  Results do not depend on the choice.
+static const int kTuneBandEdge[] = {32, 64, 128, 256, 512};
+static const int kTuneBandSize[] = {24, 48, 96, 192, 384};  // size timed per band
+
+static int tune_band(int n) {
+    int b = 0;
+    while (b < 4 && n > kTuneBandEdge[b]) b++;
+    return b;
+}
+
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, int> g_tune_cache;
+
+static int tuned_tile_rows(lassie_batch *b, int precision, int N) {
+    const auto key = std::make_tuple(b->dev, precision, N, b->grid);
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) return it->second;
+    const int64_t smem = tune_factor_smem(N, precision);
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
+    int choice = 8;
+    if (smem <= max_optin - 1024) {
+        cudaEvent_t e0, e1;
+        if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+            const int rows[3] = {8, 4, 2};
+            float ms[3] = {0.f, 0.f, 0.f};
+            bool ok = true;
+            int *fails = reinterpret_cast<int *>(b->d_queue.p);
+            for (int c = 0; c < 3 && ok; c++) {
+                ok = tune_factor_launch(precision, N, rows[c], 1, b->d_ws.p, b->P.ws_stride,
+                                        b->grid, fails, nullptr) == cudaSuccess &&
+                     cudaEventRecord(e0, nullptr) == cudaSuccess &&
+                     tune_factor_launch(precision, N, rows[c], 3, b->d_ws.p, b->P.ws_stride,
+                                        b->grid, fails, nullptr) == cudaSuccess &&
+                     cudaEventRecord(e1, nullptr) == cudaSuccess &&
+                     cudaEventSynchronize(e1) == cudaSuccess &&
+                     cudaEventElapsedTime(&ms[c], e0, e1) == cudaSuccess;
+            }
+            if (ok) {
+                int best = 0;
+                for (int c = 1; c < 3; c++)
+                    if (ms[c] < ms[best]) best = c;
+                if (ms[best] < 0.95f * ms[0]) choice = rows[best];
+            }
+            cudaGetLastError();
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    g_tune_cache[key] = choice;
+    return choice;
+}
+
+static int tile_code(int rows) { return rows == 4 ? 1 : (rows == 2 ? 2 : 0); }
+
+extern "C" int lassie_batch_tile_rows(const lassie_batch *b, int32_t *rows) {
+    if (!b || (b->n > 0 && !rows)) return set_error(LASSIE_ERR_ARGS, "batch_tile_rows");
+    for (int q = 0; q < b->n; q++) {
+        const int c = (b->desc[q].flags >> 4) & 3;
+        rows[q] = c == 1 ? 4 : (c == 2 ? 2 : 8);
+    }
+    return LASSIE_OK;
+}
+
 extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const lassie_opts *opts,
                                    lassie_batch **out) {
     if (!out || (n > 0 && !inst) || n < 0) return set_error(LASSIE_ERR_ARGS, "batch_create");
     lassie_opts o;
     if (opts) o = *opts;
     else lassie_opts_default(&o);
-    if (o.precision != LASSIE_PREC_FP64 && o.precision != LASSIE_PREC_MIXED)
+    if (o.precision != LASSIE_PREC_FP64 && o.precision != LASSIE_PREC_MIXED &&
+        o.precision != LASSIE_PREC_FLOAT)
         return set_error(LASSIE_ERR_ARGS, "precision");
     if (o.controller != LASSIE_CTRL_COMPAT && o.controller != LASSIE_CTRL_BDF)
         return set_error(LASSIE_ERR_ARGS, "controller");
+    const bool fmode = o.precision == LASSIE_PREC_FLOAT;
+    if (fmode && o.controller != LASSIE_CTRL_COMPAT)
+        return set_error(LASSIE_ERR_ARGS, "the float mode runs LASSIE's controller only");
+    if (o.tile_rows != 0 && o.tile_rows != 8 && o.tile_rows != 4 && o.tile_rows != 2)
+        return set_error(LASSIE_ERR_ARGS, "tile_rows must be 0 (autotuned), 8, 4 or 2");
     const bool bdf = o.controller == LASSIE_CTRL_BDF;
     if (bdf) {
         if (!(o.rtol > 0.0) || !(o.atol >= 0.0) || o.max_order < 1 || o.max_order > 5 ||
@@ -516,7 +602,21 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->dev);
     int64_t ws_stride = 0, ws_total = 0;
-    if (b->nmax > kThreads) {
+    if (fmode && b->nmax > kThreads) {
+        delete b;
+        return set_error(LASSIE_ERR_TOO_LARGE, "the float mode runs networks of at most " +
+                                                   std::to_string(kThreads) + " species");
+    }
+    if (fmode) {
+        b->smem = float_smem_bytes(b->nmax, b->rmax, b->amax, b->hmax);
+        if (n > 0 && b->smem > max_optin - 1024) {
+            delete b;
+            return set_error(LASSIE_ERR_TOO_LARGE, "float mode: shared memory");
+        }
+        b->grid = std::max(1, std::min(n, b->sm_count));
+        ws_stride = ((int64_t)b->nmax * round_up4(b->nmax) * 4 + 255) / 256 * 256;
+        ws_total = ws_stride * b->grid;
+    } else if (b->nmax > kThreads) {
         // one network above kThreads species: the whole GPU integrates it
         if (n != 1) {
             delete b;
@@ -571,6 +671,23 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         delete b;
         return rc;
     }
+    b->P.ws_stride = ws_stride;
+    if (!b->wide && !bdf && !fmode && n > 0) {
+        // trailing-update tiles per instance: fixed by the caller or autotuned
+        // per size band (LASSIE's loop; the BDF controller keeps the default)
+        int band_rows[5] = {0, 0, 0, 0, 0};
+        for (int q = 0; q < n; q++) {
+            int rows = o.tile_rows;
+            if (rows == 0) {
+                const int band = tune_band(b->desc[q].n);
+                if (!band_rows[band])
+                    band_rows[band] =
+                        tuned_tile_rows(b, o.precision, std::min(kTuneBandSize[band], b->nmax));
+                rows = band_rows[band];
+            }
+            b->desc[q].flags |= tile_code(rows) << 4;
+        }
+    }
     auto cpy = [&](DevBuf &d, const void *h, size_t bytes) {
         return cudaMemcpy(d.p, h, bytes, cudaMemcpyHostToDevice);
     };
@@ -583,7 +700,8 @@ extern "C" int lassie_batch_create(const lassie_instance *inst, int32_t n, const
         return set_error(LASSIE_ERR_CUDA, std::string("batch upload: ") +
                                               cudaGetErrorString(cudaGetLastError()));
     }
-    if (!b->wide && compat_configure(o.precision, b->smem) != cudaSuccess) {
+    if (!b->wide && (fmode ? float_configure(b->smem) : compat_configure(o.precision, b->smem)) !=
+                        cudaSuccess) {
         delete b;
         return set_error(LASSIE_ERR_CUDA, std::string("kernel configure: ") +
                                               cudaGetErrorString(cudaGetLastError()));
@@ -628,6 +746,8 @@ extern "C" int lassie_batch_run(lassie_batch *b, void *stream) {
         CU(cudaMemsetAsync(b->d_ws.p, 0, 256, b->stream));
         CU(cudaMemsetAsync((unsigned char *)b->d_ws.p + b->wide_flags, 0, 16, b->stream));
         CU(wide_launch(b->P, b->grid, b->smem, b->stream));
+    } else if (b->opts.precision == LASSIE_PREC_FLOAT) {
+        CU(float_launch(b->P, b->grid, b->smem, b->stream));
     } else {
         CU(compat_launch(b->P, b->grid, b->smem, b->stream));
     }
@@ -721,6 +841,8 @@ extern "C" int lassie_adjoint_batch(const lassie_instance *inst, int32_t n,
     // the recorded forward and its reverse are LASSIE's loop
     if (o.controller != LASSIE_CTRL_COMPAT)
         return set_error(LASSIE_ERR_ARGS, "adjoint_batch: LASSIE's controller only");
+    if (o.precision == LASSIE_PREC_FLOAT)
+        return set_error(LASSIE_ERR_ARGS, "adjoint_batch: the float mode has no adjoint");
     const int K = ckpt_every > 0 ? ckpt_every : 8;
     const int cap = max_record > 0 ? max_record : 100000;
     lassie_batch *b = nullptr;

@@ -465,6 +465,20 @@ __device__ __forceinline__ void load4(const double *p, double *o) {
     o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
 }
 
+// RM consecutive panel entries (RM = 8, 4 or 2; p aligned to RM elements).
+template <int RM, typename T>
+__device__ __forceinline__ void load_rows(const T *p, T *o) {
+    if constexpr (RM == 8) {
+        load8(p, o);
+    } else if constexpr (RM == 4) {
+        load4(p, o);
+    } else {
+        static_assert(RM == 2, "8, 4 or 2 rows per thread");
+        o[0] = p[0];
+        o[1] = p[1];
+    }
+}
+
 __device__ __forceinline__ void store4(float *p, const float *v) {
     reinterpret_cast<float4 *>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
 }
@@ -487,11 +501,59 @@ __device__ __forceinline__ void store4(double *p, const double *v) {
 //          columns tx*4..; L21 is read from lt and U12 from a staged tile
 //          (utile), both with 16-byte loads.
 // Returns 0, or j+1 if the pivot of column j is exactly zero (uniform).
+// One column tile of the LU's trailing update A22 -= L21 * U12, RM rows per
+// thread (passes of 16*RM rows); every entry sums the same products in the
+// same order whatever RM is.
+template <typename LT, int RM>
+__device__ __forceinline__ void lu_trailing(LT *M, int ld, int N, const int *perm, const LT *lt,
+                                            int mp, const LT *utile, int j0, int pb, int c0,
+                                            int m2, int tn0, int tx, int ty) {
+    constexpr int PB = LuShape<LT>::PB, TN = 128, TM = kWarps * RM;
+    for (int tm0 = 0; tm0 < m2; tm0 += TM) {
+        const int rl = pb + tm0 + ty * RM;  // row relative to j0
+        const int col0 = c0 + tn0 + tx * 4;
+        LT acc[RM][4];
+#pragma unroll
+        for (int a = 0; a < RM; a++) {
+            const int r = j0 + rl + a;
+            if (r < N && col0 < ld) {
+                load4(M + (int64_t)perm[r] * ld + col0, acc[a]);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
+            }
+        }
+#pragma unroll 4
+        for (int q = 0; q < PB; q++) {
+            LT av[RM], bv[4];
+            load_rows<RM>(lt + q * mp + rl, av);
+            load4(utile + q * TN + tx * 4, bv);
+#pragma unroll
+            for (int a = 0; a < RM; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = lt_fma(-av[a], bv[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int a = 0; a < RM; a++) {
+            const int r = j0 + rl + a;
+            if (r < N) {
+#pragma unroll
+                for (int b = 0; b < 4; b++)
+                    if (col0 + b < N) M[(int64_t)perm[r] * ld + col0 + b] = acc[a][b];
+            }
+        }
+    }
+}
+
+// rm: rows per thread of the trailing update's tiles (8, 4 or 2; see
+// lu_trailing); the factors do not depend on it (the autotuner picks it per
+// network size).
 template <typename LT>
 __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, LT *utile,
-                                      LT *rowbuf, double *red, int *ired, long long *cyc) {
+                                      LT *rowbuf, double *red, int *ired, long long *cyc,
+                                      int rm = 8) {
     constexpr int PB = LuShape<LT>::PB;
-    constexpr int TN = 128, TM = 128;
+    constexpr int TN = 128;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     LT *pivrow = rowbuf, *swaprow = rowbuf + PB;
     for (int i = tid; i < N; i += kThreads) perm[i] = i;
@@ -660,41 +722,9 @@ __device__ __noinline__ int lu_factor(LT *M, int ld, int N, int *perm, LT *lt, L
                     utile[idx] = (col < N) ? M[(int64_t)perm[j0 + q] * ld + col] : LT(0);
                 }
                 __syncthreads();
-                for (int tm0 = 0; tm0 < m2; tm0 += TM) {
-                    const int rl = pb + tm0 + ty * 8;  // row relative to j0
-                    const int col0 = c0 + tn0 + tx * 4;
-                    LT acc[8][4];
-#pragma unroll
-                    for (int a = 0; a < 8; a++) {
-                        const int r = j0 + rl + a;
-                        if (r < N && col0 < ld) {
-                            load4(M + (int64_t)perm[r] * ld + col0, acc[a]);
-                        } else {
-#pragma unroll
-                            for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
-                        }
-                    }
-#pragma unroll 4
-                    for (int q = 0; q < PB; q++) {
-                        LT av[8], bv[4];
-                        load8(lt + q * mp + rl, av);
-                        load4(utile + q * TN + tx * 4, bv);
-#pragma unroll
-                        for (int a = 0; a < 8; a++)
-#pragma unroll
-                            for (int b = 0; b < 4; b++)
-                                acc[a][b] = lt_fma(-av[a], bv[b], acc[a][b]);
-                    }
-#pragma unroll
-                    for (int a = 0; a < 8; a++) {
-                        const int r = j0 + rl + a;
-                        if (r < N) {
-#pragma unroll
-                            for (int b = 0; b < 4; b++)
-                                if (col0 + b < N) M[(int64_t)perm[r] * ld + col0 + b] = acc[a][b];
-                        }
-                    }
-                }
+                if (rm == 4) lu_trailing<LT, 4>(M, ld, N, perm, lt, mp, utile, j0, pb, c0, m2, tn0, tx, ty);
+                else if (rm == 2) lu_trailing<LT, 2>(M, ld, N, perm, lt, mp, utile, j0, pb, c0, m2, tn0, tx, ty);
+                else lu_trailing<LT, 8>(M, ld, N, perm, lt, mp, utile, j0, pb, c0, m2, tn0, tx, ty);
                 __syncthreads();
             }
         }
@@ -762,6 +792,50 @@ __device__ bool cta_block_inverse(const T *Dsrc, int ds, int nb, T *Dinv, T *xs)
     return __syncthreads_and(ok) != 0;
 }
 
+// One column tile of the Gauss-Jordan update over all rows, RM rows per
+// thread (passes of 16*RM rows): M[r, C] -= M[r, J] * B for rows that are
+// not pivots, pivot rows take B.  Every entry sums the same products in the
+// same order whatever RM is.
+template <int RM>
+__device__ __forceinline__ void gje_trailing(float *M, int ld, int N, const float *lt, int mp,
+                                             const float *utile, const int *pos, int ty, int tx,
+                                             int col0, bool inJ) {
+    constexpr int PB = 32, TN = 128, TM = kWarps * RM;
+    for (int tm0 = 0; tm0 < N; tm0 += TM) {
+        const int rl = tm0 + ty * RM;
+        float acc[RM][4];
+#pragma unroll
+        for (int a = 0; a < RM; a++) {
+            const int r = rl + a;
+            if (r < N && col0 < ld && !inJ) {
+                load4(M + (int64_t)r * ld + col0, acc[a]);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+            }
+        }
+#pragma unroll 4
+        for (int q = 0; q < PB; q++) {
+            float av[RM], bv[4];
+            load_rows<RM>(lt + q * mp + rl, av);
+            load4(utile + q * TN + tx * 4, bv);
+#pragma unroll
+            for (int a = 0; a < RM; a++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = __fmaf_rn(-av[a], bv[b], acc[a][b]);
+        }
+#pragma unroll
+        for (int a = 0; a < RM; a++) {
+            const int r = rl + a;
+            if (r < N && col0 < ld) {
+                const int pr = pos[r];
+                if (pr >= 0) load4(utile + pr * TN + tx * 4, acc[a]);
+                store4(M + (int64_t)r * ld + col0, acc[a]);
+            }
+        }
+    }
+}
+
 // FP32 form: in-place Gauss-Jordan inverse of M (row-major, N <= kThreads)
 // with partial pivoting by rows, in kPB-column panels J:
 //   pivot rows P_J: per column, the largest |value| among the rows that are
@@ -775,10 +849,11 @@ __device__ bool cta_block_inverse(const T *Dsrc, int ds, int nb, T *Dinv, T *xs)
 // perm[j] = pivot row of column j; the result X satisfies
 // inv(M)[j][perm[k]] = X[perm[j]][k] (gje_apply).  pos: N ints of scratch.
 // Returns 0, or j+1 if column j has no nonzero candidate.
+// rm: rows per thread of the update tiles (8, 4 or 2; see gje_trailing).
 __device__ __noinline__ int gje_factor(float *M, int ld, int N, int *perm, int *pos, float *lt,
                                        float *utile, float *dblk, float *rowbuf, double *red,
-                                       int *ired, long long *cyc) {
-    constexpr int PB = 32, TN = 128, TM = 128;
+                                       int *ired, long long *cyc, int rm = 8) {
+    constexpr int PB = 32, TN = 128;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int mp = ((N + 31) & ~31) + 4;  // lt: panel snapshot, column-major
     float *pivrow = rowbuf;
@@ -902,39 +977,9 @@ __device__ __noinline__ int gje_factor(float *M, int ld, int N, int *perm, int *
             __syncthreads();
             const int col0 = tn0 + tx * 4;
             const bool inJ = col0 >= j0 && col0 < j0 + PB;
-            for (int tm0 = 0; tm0 < N; tm0 += TM) {
-                const int rl = tm0 + ty * 8;
-                float acc[8][4];
-#pragma unroll
-                for (int a = 0; a < 8; a++) {
-                    const int r = rl + a;
-                    if (r < N && col0 < ld && !inJ) {
-                        load4(M + (int64_t)r * ld + col0, acc[a]);
-                    } else {
-#pragma unroll
-                        for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
-                    }
-                }
-#pragma unroll 4
-                for (int q = 0; q < PB; q++) {
-                    float av[8], bv[4];
-                    load8(lt + q * mp + rl, av);
-                    load4(utile + q * TN + tx * 4, bv);
-#pragma unroll
-                    for (int a = 0; a < 8; a++)
-#pragma unroll
-                        for (int b = 0; b < 4; b++) acc[a][b] = __fmaf_rn(-av[a], bv[b], acc[a][b]);
-                }
-#pragma unroll
-                for (int a = 0; a < 8; a++) {
-                    const int r = rl + a;
-                    if (r < N && col0 < ld) {
-                        const int pr = pos[r];
-                        if (pr >= 0) load4(utile + pr * TN + tx * 4, acc[a]);
-                        store4(M + (int64_t)r * ld + col0, acc[a]);
-                    }
-                }
-            }
+            if (rm == 4) gje_trailing<4>(M, ld, N, lt, mp, utile, pos, ty, tx, col0, inJ);
+            else if (rm == 2) gje_trailing<2>(M, ld, N, lt, mp, utile, pos, ty, tx, col0, inJ);
+            else gje_trailing<8>(M, ld, N, lt, mp, utile, pos, ty, tx, col0, inJ);
             __syncthreads();
         }
         if (tid < pb) pos[perm[j0 + tid]] = -2;
@@ -1295,6 +1340,14 @@ __device__ __noinline__ void lu_solve_fast_T(const float *M, int ld, int N, cons
 }
 
 
+// ------------------------------------------------ tuned factorisations
+// Rows per thread of the trailing-update tiles, from bits 4-5 of an
+// instance's flags (0: 8, 1: 4, 2: 2), as the batch's autotuner chose them.
+__device__ __forceinline__ int tile_rows_of(int flags) {
+    const int c = (flags >> 4) & 3;
+    return c == 1 ? 4 : (c == 2 ? 2 : 8);
+}
+
 // ----------------------------------------------------------- integrator
 
 struct Vecs {
@@ -1466,8 +1519,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     // FP32 form: inverted diagonal blocks of the factors follow the matrix
     float *dinv = reinterpret_cast<float *>(M + (int64_t)N * ld);
     int *wflag = ired + kWarps + 1;  // wide engine: join results
-    const int refine_max = P.refine_max > 0 ? P.refine_max : 8;
+    // the per-CTA form stops on the state's resolution, which small species
+    // may reach a few sweeps after the rest
+    const int refine_max = P.refine_max > 0 ? P.refine_max : (kWide ? 8 : 12);
     const bool root_sqrt = (D.flags & 1) != 0;
+    const int tile_rows = tile_rows_of(D.flags);
     long long c_mark = 0;
 
     int64_t outer = 0;  // every thread keeps the loop count (uniform control)
@@ -1616,10 +1672,12 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                 if constexpr (kMixed) {
                     // FP32: Gauss-Jordan inverse (each solve is a matrix-vector product)
                     fail = gje_factor(M, ld, N, perm, pos, lt, utile, dblk, rowbuf, red, ired,
-                                      reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0;
+                                      reinterpret_cast<long long *>(&st.cycles_lu_panel),
+                                      tile_rows) != 0;
                 } else {
                     fail = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired,
-                                         reinterpret_cast<long long *>(&st.cycles_lu_panel)) != 0;
+                                         reinterpret_cast<long long *>(&st.cycles_lu_panel),
+                                         tile_rows) != 0;
                 }
                 soft = false;
             }
@@ -1727,6 +1785,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                             le >= -1022 ? (long long)(le + 1023) << 52
                                         : (le >= -1074 ? 1LL << (le + 1074) : 0LL);
                         double cmax, xmax;
+                        bool still_moving = true;
                         if constexpr (kWide) {
                             // scaling, matrix-vector product and update on the grid
                             const long long c_tri = clock64();
@@ -1745,7 +1804,8 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                                   reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt),
                                   false);
                         if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
-                        long long cmb = 0, xmb = 0;
+                        long long cmb = 0;
+                        bool moved = false;
                         for (int s = tid; s < N; s += kThreads) {
                             double c = (double)reinterpret_cast<const float *>(lt)[perm[s]] * isc;
                             // the part of this row's right-hand side that the
@@ -1756,23 +1816,40 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                                 if (fabs(mdiag[s]) >= 0.5)
                                     c += (rs - (double)(float)rs) * isc / mdiag[s];
                             }
-                            const double nx = dx[s] + c;
+                            const double ox = dx[s];
+                            const double nx = ox + c;
                             dx[s] = nx;
                             cmb = max(cmb, absbits_nonan(c));
-                            xmb = max(xmb, absbits_nonan(nx));
+                            // does this correction still change the state
+                            // the Newton update will form?
+                            if (V.fd[s] == 0 && !((yv[s] + nx) == (yv[s] + ox))) moved = true;
                         }
                         cmax = __longlong_as_double(cmb);
-                        xmax = __longlong_as_double(xmb);
-                        block_max2(cmax, xmax, red);
+                        xmax = 0.0;
+                        cmax = block_max(cmax, red);
+                        still_moving = __syncthreads_or(moved) != 0;
                         }
                         if (tid == 0) st.refine_sweeps++;
                         if (sweep > 0) rate = fmax(rate, cmax / prev);
-                        // stop when this correction, or the next one predicted
-                        // from the contraction so far, is below FP64 resolution
-                        // of dx
-                        const bool small_next =
-                            sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
-                        if (!finite || !(cmax > 1e-15 * xmax) || small_next) {
+                        bool done;
+                        if constexpr (kWide) {
+                            // stop when this correction, or the next one
+                            // predicted from the contraction so far, is below
+                            // FP64 resolution of dx
+                            const bool small_next =
+                                sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
+                            done = !(cmax > 1e-15 * xmax) || small_next;
+                        } else {
+                            // stop when this correction changes no species
+                            // of the state y + dx in FP64 (subnormal species
+                            // included).  A normwise test would leave species
+                            // far below the others with large relative errors,
+                            // and LASSIE's loop decides on absolute quantities
+                            // (RKF45 atol 1e-12, species that must stay
+                            // positive).
+                            done = !still_moving;
+                        }
+                        if (!finite || done) {
                             converged = true;
                             break;
                         }
@@ -2343,7 +2420,7 @@ __global__ void __launch_bounds__(kThreads, 1) wide_kernel(LaunchParams P) {
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        W.tc_on = 1;
+        W.tc_on = P.tensor_cores == 2 ? 2 : 1;
         W.tc_bar = &tc_bar;
         W.tc_phase = &tc_phase;
         W.tc_tmem = tc_slot;
@@ -2411,8 +2488,9 @@ cudaError_t wide_launch(const LaunchParams &P, int grid, int64_t smem, cudaStrea
 // ------------------------------------------------ tensor-core self-test
 
 // D = A * B (A: 128 x 32, B: 32 x kTcN, D: 128 x kTcN, row-major FP32) through
-// tc_tile_product on one CTA; status[0] = 1 on success, 2 if the MMA wait
-// ran out.
+// tc_tile_product (kBf16: tc_tile_product_bf16) on one CTA; status[0] = 1 on
+// success, 2 if the MMA wait ran out.
+template <bool kBf16>
 __global__ void __launch_bounds__(kThreads, 1) tc_selftest_kernel(const float *A, const float *B,
                                                                   float *D, int *status) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -2420,6 +2498,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_selftest_kernel(const float *A
     float *sAl = sAh + kTcM * kTcK;
     float *sBh = sAl + kTcM * kTcK;
     float *sBl = sBh + kTcN * kTcK;
+    uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
     uint64_t *bar = reinterpret_cast<uint64_t *>(sBl + kTcN * kTcK);
     uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
     const int tid = threadIdx.x;
@@ -2431,23 +2510,35 @@ __global__ void __launch_bounds__(kThreads, 1) tc_selftest_kernel(const float *A
     const uint32_t tmem = *slot;
     for (int q = tid; q < kTcM * kTcK; q += kThreads) {
         const int r = q / kTcK, k = q - r * kTcK;
-        const float x = A[q], hi = tf32_hi(x);
-        const int o = tc_off(r, k) / 4;
-        sAh[o] = hi;
-        sAl[o] = x - hi;
+        const float x = A[q];
+        if constexpr (kBf16) {
+            sA16[tc_off16(r, k) / 2] = bf16_bits(x);
+        } else {
+            const float hi = tf32_hi(x);
+            const int o = tc_off(r, k) / 4;
+            sAh[o] = hi;
+            sAl[o] = x - hi;
+        }
     }
     for (int q = tid; q < kTcN * kTcK; q += kThreads) {
         const int n = q / kTcK, k = q - n * kTcK;
-        const float x = B[k * kTcN + n], hi = tf32_hi(x);
-        const int o = tc_off(n, k) / 4;
-        sBh[o] = hi;
-        sBl[o] = x - hi;
+        const float x = B[k * kTcN + n];
+        if constexpr (kBf16) {
+            sB16[tc_off16(n, k) / 2] = bf16_bits(x);
+        } else {
+            const float hi = tf32_hi(x);
+            const int o = tc_off(n, k) / 4;
+            sBh[o] = hi;
+            sBl[o] = x - hi;
+        }
     }
     tc_proxy_fence();
     __syncthreads();
     uint32_t phase = 0;
     float out[32];
-    const bool ok = tc_tile_product(sAh, sAl, sBh, sBl, bar, tmem, phase, out);
+    bool ok;
+    if constexpr (kBf16) ok = tc_tile_product_bf16(sA16, sB16, bar, tmem, phase, out);
+    else ok = tc_tile_product(sAh, sAl, sBh, sBl, bar, tmem, phase, out);
     if (ok) {
         const int w = tid >> 5, row = (w & 3) * 32 + (tid & 31), c0 = (w >> 2) * 32;
         for (int i = 0; i < 32; i++) D[row * kTcN + c0 + i] = out[i];
@@ -2457,14 +2548,25 @@ __global__ void __launch_bounds__(kThreads, 1) tc_selftest_kernel(const float *A
     if (tid == 0) status[0] = ok ? 1 : 2;
 }
 
+template <bool kBf16>
+static int tc_selftest_launch(const float *dA, const float *dB, float *dD, int *dstatus,
+                              void *stream) {
+    const int smem = kTcSmemBytes;
+    if (cudaFuncSetAttribute(tc_selftest_kernel<kBf16>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+        return LASSIE_ERR_CUDA;
+    tc_selftest_kernel<kBf16><<<1, kThreads, smem, (cudaStream_t)stream>>>(dA, dB, dD, dstatus);
+    return cudaGetLastError() == cudaSuccess ? LASSIE_OK : LASSIE_ERR_CUDA;
+}
+
 extern "C" int lassie_tc_selftest(const float *dA, const float *dB, float *dD, int *dstatus,
                                   void *stream) {
-    const int smem = kTcSmemBytes;
-    if (cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
-        return LASSIE_ERR_CUDA;
-    tc_selftest_kernel<<<1, kThreads, smem, (cudaStream_t)stream>>>(dA, dB, dD, dstatus);
-    return cudaGetLastError() == cudaSuccess ? LASSIE_OK : LASSIE_ERR_CUDA;
+    return tc_selftest_launch<false>(dA, dB, dD, dstatus, stream);
+}
+
+extern "C" int lassie_tc_selftest_bf16(const float *dA, const float *dB, float *dD, int *dstatus,
+                                       void *stream) {
+    return tc_selftest_launch<true>(dA, dB, dD, dstatus, stream);
 }
 
 // ------------------------------------------ single-evaluation kernels
@@ -2873,6 +2975,77 @@ __global__ void __launch_bounds__(kThreads, 1) lu_solve_kernel(int N, LT *A, int
         lu_solve<LT>(A, ld, N, perm, bvec);
     }
     for (int s = threadIdx.x; s < N; s += kThreads) x[s] = (double)bvec[s];
+}
+
+// Autotuner probe: every CTA factors the same diagonally dominant N x N
+// test matrix `reps` times in its own workspace slot, with rm rows per
+// thread in the trailing update (the per-CTA LU in FP64, the Gauss-Jordan
+// inverse in FP32) -- the work and the contention of a batch of such
+// networks.  *fails counts factorisations that met a zero pivot (none do).
+template <typename LT>
+__global__ void __launch_bounds__(kThreads, 1) tune_factor_kernel(int N, int rm, int reps,
+                                                                  unsigned char *ws,
+                                                                  int64_t ws_stride, int *fails) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int PB = LuShape<LT>::PB;
+    __shared__ double red[2 * kWarps + 1];
+    __shared__ int ired[kWarps + 2 + PB];
+    __shared__ long long cyc[3];
+    const SmemLayout L(N, 1, 1, 1, (int)sizeof(LT), PB, 128);
+    int *perm = reinterpret_cast<int *>(smem + L.perm);
+    int *pos = reinterpret_cast<int *>(smem + L.slot);
+    LT *lt = reinterpret_cast<LT *>(smem + L.lt);
+    LT *utile = reinterpret_cast<LT *>(smem + L.utile);
+    LT *rowbuf = reinterpret_cast<LT *>(smem + L.rowbuf);
+    LT *dblk = reinterpret_cast<LT *>(smem + L.dblk);
+    const int ld = round_up4(N);
+    LT *M = reinterpret_cast<LT *>(ws + (int64_t)blockIdx.x * ws_stride);
+    if (threadIdx.x == 0) cyc[0] = cyc[1] = cyc[2] = 0;
+    for (int r = 0; r < reps; r++) {
+        for (int q = threadIdx.x; q < N * ld; q += kThreads) {
+            const int i = q / ld, j = q - i * ld;
+            uint32_t h = (uint32_t)q * 2654435761u;
+            h ^= h >> 15;
+            h *= 2246822519u;
+            h ^= h >> 13;
+            const float v = ((float)(h & 0xffffu) * (1.0f / 65536.0f) - 0.5f) * 0.02f;
+            M[q] = (LT)(j >= N ? 0.0f : (i == j ? 1.0f + v : v));
+        }
+        __syncthreads();
+        int f;
+        if constexpr (std::is_same<LT, float>::value)
+            f = gje_factor(M, ld, N, perm, pos, lt, utile, dblk, rowbuf, red, ired, cyc, rm);
+        else
+            f = lu_factor<LT>(M, ld, N, perm, lt, utile, rowbuf, red, ired, cyc, rm);
+        if (threadIdx.x == 0 && f) atomicAdd(fails, 1);
+        __syncthreads();
+    }
+}
+
+int64_t tune_factor_smem(int N, int precision) {
+    return precision == LASSIE_PREC_FP64
+               ? SmemLayout(N, 1, 1, 1, 8, LuShape<double>::PB, 128).total
+               : SmemLayout(N, 1, 1, 1, 4, LuShape<float>::PB, 128).total;
+}
+
+cudaError_t tune_factor_launch(int precision, int N, int rm, int reps, void *ws,
+                               int64_t ws_stride, int grid, int *fails, cudaStream_t stream) {
+    const int64_t smem = tune_factor_smem(N, precision);
+    cudaError_t e;
+    if (precision == LASSIE_PREC_FP64) {
+        e = cudaFuncSetAttribute(tune_factor_kernel<double>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        tune_factor_kernel<double><<<grid, kThreads, smem, stream>>>(
+            N, rm, reps, (unsigned char *)ws, ws_stride, fails);
+    } else {
+        e = cudaFuncSetAttribute(tune_factor_kernel<float>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        tune_factor_kernel<float><<<grid, kThreads, smem, stream>>>(
+            N, rm, reps, (unsigned char *)ws, ws_stride, fails);
+    }
+    return cudaGetLastError();
 }
 
 int64_t lu_solve_smem(int N, int precision) {

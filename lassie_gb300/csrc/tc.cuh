@@ -1,9 +1,15 @@
 // Tensor-core (tcgen05) helpers for the rank-32 updates of the Gauss-Jordan
-// factorisation: D[128 x NT] = A[128 x 32] * B[32 x NT] in FP32 through TF32
-// MMAs with the operands split as x = hi + lo (hi = x rounded to TF32,
-// lo = x - hi, exact), D = Ah*Bh + Ah*Bl + Al*Bh: three MMAs per 8-wide K
-// step, close to an FP32 product (the dropped Al*Bl term is below 2^-22
-// relative).  Included by compat_engine.cu inside its namespace.
+// factorisation: D[128 x NT] = A[128 x 32] * B[32 x NT] in FP32, in one of
+// two forms:
+//   * TF32 MMAs with the operands split as x = hi + lo (hi = x rounded to
+//     TF32, lo = x - hi, exact), D = Ah*Bh + Ah*Bl + Al*Bh: three MMAs per
+//     8-wide K step, close to an FP32 product (the dropped Al*Bl term is
+//     below 2^-22 relative);
+//   * BF16 operands (x rounded to nearest BF16), FP32 accumulation: one
+//     kind::f16 MMA per 16-wide K step, each product exact and rounded once
+//     into the FP32 sum -- the operands carry 8 significant bits, so the
+//     factors are good to about 2^-9 and the FP64 refinement does the rest.
+// Included by compat_engine.cu inside its namespace.
 //
 // Operands sit in shared memory in the canonical K-major layout without
 // swizzling: 8-row x 16-byte core matrices, core matrices adjacent in K
@@ -59,6 +65,33 @@ __device__ __forceinline__ int tc_off(int r, int k) {
     return (r >> 3) * (kTcK / 4) * 128 + (k >> 2) * 128 + (r & 7) * 16 + (k & 3) * 4;
 }
 
+// The same for 16-bit elements: a core matrix row holds 8 elements of K.
+__device__ __forceinline__ int tc_off16(int r, int k) {
+    return (r >> 3) * (kTcK / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// Instruction descriptor: kind::f16, D in FP32, A and B BF16 and K-major,
+// M = kTcM, N = n.
+__device__ __forceinline__ uint32_t tc_idesc_bf16(int n) {
+    uint32_t d = 0;
+    d |= 1u << 4;                      // D format: F32
+    d |= 1u << 7;                      // A format: BF16
+    d |= 1u << 10;                     // B format: BF16
+    d |= (uint32_t)(n >> 3) << 17;     // N / 8
+    d |= (uint32_t)(kTcM >> 4) << 24;  // M / 16
+    return d;
+}
+
+// x rounded to the nearest BF16 (ties to even), as its 16 bits; inf/NaN
+// keep their class.
+__device__ __forceinline__ uint16_t bf16_bits(float x) {
+    uint32_t b = __float_as_uint(x);
+    if ((b & 0x7f800000u) == 0x7f800000u)
+        return (uint16_t)((b >> 16) | ((b & 0xffffu) ? 0x40u : 0u));
+    b += 0x7fffu + ((b >> 16) & 1u);
+    return (uint16_t)(b >> 16);
+}
+
 __device__ __forceinline__ void tc_mbar_init(uint64_t *bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -99,6 +132,15 @@ __device__ __forceinline__ void tc_mma_tf32(uint32_t dtmem, uint64_t adesc, uint
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_mma_f16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                           uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
@@ -173,6 +215,37 @@ __device__ __forceinline__ bool tc_tile_product(const float *sAh, const float *s
             acc = 1;
             tc_mma_tf32(tmem, ah, bl, idesc, 1);
             tc_mma_tf32(tmem, al, bh, idesc, 1);
+        }
+        tc_commit(bar);
+    }
+    const bool ok = tc_mbar_wait(bar, phase);
+    tc_fence_after();
+    if (ok) {
+        const int w = tid >> 5, quad = w & 3, chunk = w >> 2;
+        tc_ld32(tmem + ((uint32_t)(quad * 32) << 16) + chunk * 32, out);
+    }
+    phase ^= 1u;
+    tc_fence_before();
+    return __syncthreads_and(ok) != 0;
+}
+
+// The BF16 form: sA (A as 128 x 32) and sB (B as kTcN x 32) hold BF16 bits
+// stored with tc_off16; otherwise as tc_tile_product (two MMAs, K = 16 each).
+__device__ __forceinline__ bool tc_tile_product_bf16(const uint16_t *sA, const uint16_t *sB,
+                                                     uint64_t *bar, uint32_t tmem,
+                                                     uint32_t &phase, float *out) {
+    static_assert(kThreads == 4 * kTcN, "four warpgroups, one 32-column chunk each");
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        tc_fence_after();
+        const uint32_t idesc = tc_idesc_bf16(kTcN);
+        const uint32_t sbo = (kTcK / 8) * 128;
+#pragma unroll
+        for (int ks = 0; ks < kTcK / 16; ks++) {
+            const uint32_t koff = ks * 2 * 128;  // two core matrices per K = 16 step
+            const uint64_t a = tc_desc(smem_u32(sA) + koff, 128, sbo);
+            const uint64_t b = tc_desc(smem_u32(sB) + koff, 128, sbo);
+            tc_mma_f16(tmem, a, b, idesc, ks > 0 ? 1u : 0u);
         }
         tc_commit(bar);
     }

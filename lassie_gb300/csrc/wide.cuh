@@ -348,8 +348,12 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
 // pivot rows take B, columns in J start from 0, the rest subtract from M.
 // False if a tensor-core wait ran out (the control block's abort flag is
 // then set).
+// W.tc_on == 2: the BF16 form (operands rounded to BF16, one kind::f16 MMA
+// per 16-wide K step, FP32 accumulation).
 __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *smem) {
     float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
+    uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
+    const bool bf16 = W.tc_on == 2;
     const int tid = threadIdx.x;
     const int N = W.N, ld = W.ld;
     const int nrt = (N + kTcM - 1) / kTcM, nct = (ld + kTcN - 1) / kTcN;
@@ -358,6 +362,38 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
     for (int t = blockIdx.x; t < nrt * nct && ok; t += gridDim.x) {
         const int r0 = (t / nct) * kTcM, c0 = (t % nct) * kTcN;
         __syncthreads();
+        if (bf16) {
+            // A: 128 rows x 32, B: kTcN columns x 32, 4 elements per thread
+            for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
+                const int r = q >> 3, k4 = (q & 7) * 4;
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                if (r0 + r < N) load4(W.AJ + (int64_t)(r0 + r) * kWPB + k4, v);
+                uint2 pk;
+                pk.x = (uint32_t)bf16_bits(v[0]) | ((uint32_t)bf16_bits(v[1]) << 16);
+                pk.y = (uint32_t)bf16_bits(v[2]) | ((uint32_t)bf16_bits(v[3]) << 16);
+                *reinterpret_cast<uint2 *>(sA16 + tc_off16(r, k4) / 2) = pk;
+            }
+            for (int q = tid; q < kTcN * (kTcK / 4); q += kThreads) {
+                const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
+                const int c = c0 + n;
+                const bool inJ = c >= j0 && c < j0 + kWPB;
+                uint16_t h[4];
+#pragma unroll
+                for (int b = 0; b < 4; b++) {
+                    const int k = k4 + b;
+                    float x = 0.f;
+                    if (k < pb && c < ld) {
+                        if (inJ) x = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : 0.f;
+                        else x = W.PR[(int64_t)k * ld + c];
+                    }
+                    h[b] = bf16_bits(x);
+                }
+                uint2 pk;
+                pk.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+                pk.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
+                *reinterpret_cast<uint2 *>(sB16 + tc_off16(n, k4) / 2) = pk;
+            }
+        } else {
         for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
             const int r = q >> 3, k4 = (q & 7) * 4;
             float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -392,10 +428,12 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
             store4(sBh + o, h);
             store4(sBl + o, l);
         }
+        }
         tc_proxy_fence();
         __syncthreads();
         float out[32];
-        ok = tc_tile_product(sAh, sAl, sBh, sBl, W.tc_bar, W.tc_tmem, phase, out);
+        ok = bf16 ? tc_tile_product_bf16(sA16, sB16, W.tc_bar, W.tc_tmem, phase, out)
+                  : tc_tile_product(sAh, sAl, sBh, sBl, W.tc_bar, W.tc_tmem, phase, out);
         if (!ok) break;
         const int w = tid >> 5;
         const int row = r0 + (w & 3) * 32 + (tid & 31), cb = c0 + (w >> 2) * 32;

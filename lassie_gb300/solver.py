@@ -17,7 +17,9 @@ import numpy as np
 from . import _native as nat
 from .model import Model
 
-ENGINES = {"fp64": nat.PREC_FP64, "mixed": nat.PREC_MIXED}
+# fp64: the plain FP64 GPU form; mixed: FP32 factors + FP64 refinement;
+# float: the reference's single-precision mode (-p float)
+ENGINES = {"fp64": nat.PREC_FP64, "mixed": nat.PREC_MIXED, "float": nat.PREC_FLOAT}
 
 
 def _p(a: Optional[np.ndarray]):
@@ -57,6 +59,10 @@ class NativeModel:
 
 
 ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
+# rank-32 updates of the wide engine's factorisation: FP32 pipes, tensor
+# cores with split TF32 operands (True or "tf32"), or BF16 operands with FP32
+# accumulation ("bf16")
+TENSOR_CORES = {False: 0, True: 1, "off": 0, "tf32": 1, "bf16": 2}
 
 
 BDF_KEYS = ("rtol", "atol", "first_step", "max_step", "max_order")
@@ -64,8 +70,8 @@ BDF_KEYS = ("rtol", "atol", "first_step", "max_step", "max_order")
 
 def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int = 0,
               deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow",
-              lu_reuse: bool = True, tensor_cores: bool = False,
-              bdf: Optional[Dict] = None) -> nat.Opts:
+              lu_reuse: bool = True, tensor_cores=False,
+              bdf: Optional[Dict] = None, tile_rows: int = 0) -> nat.Opts:
     """Options of a solve.  ``bdf`` (a dict, possibly empty, of rtol, atol,
     first_step, max_step, max_order) selects the BDF controller with rtol/atol
     error control instead of LASSIE's loop; ``engine`` then picks its Newton
@@ -84,7 +90,8 @@ def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int =
     o.refine_max = int(refine_max)
     o.quarter_root = ROOTS[root]
     o.lu_reuse = 1 if lu_reuse else 0
-    o.tensor_cores = 1 if tensor_cores else 0
+    o.tensor_cores = TENSOR_CORES[tensor_cores]
+    o.tile_rows = int(tile_rows)
     if bdf is not None:
         unknown = set(bdf) - set(BDF_KEYS)
         if unknown:
@@ -124,14 +131,14 @@ class _Packed:
 
 def simulate(m: Model, engine: str = "mixed", max_steps: int = 0, deadline_s: float = 0.0,
              nm: Optional[NativeModel] = None, root: str = "pow",
-             lu_reuse: bool = True, tensor_cores: bool = False,
-             bdf: Optional[Dict] = None) -> Tuple[np.ndarray, Dict]:
+             lu_reuse: bool = True, tensor_cores=False,
+             bdf: Optional[Dict] = None, refine_max: int = 0) -> Tuple[np.ndarray, Dict]:
     """Integrate one model on the GPU.  Returns (trajectory [nt, ncs], stats)."""
     nm = nm or NativeModel.of(m)
     pk = _Packed(m, nm)
     st = nat.Stats()
-    o = make_opts(m, engine, max_steps, deadline_s, root=root, lu_reuse=lu_reuse,
-                  tensor_cores=tensor_cores, bdf=bdf)
+    o = make_opts(m, engine, max_steps, deadline_s, refine_max=refine_max, root=root,
+                  lu_reuse=lu_reuse, tensor_cores=tensor_cores, bdf=bdf)
     rc = nat.load().lassie_solve(nm.handle, _p(pk.k), _p(pk.x0), _p(pk.feed), _p(pk.atol),
                                  _p(pk.t), pk.t.shape[0], _p(pk.cs),
                                  0 if pk.cs is None else pk.cs.shape[0], C.byref(o),
@@ -150,7 +157,7 @@ class Batch:
     def __init__(self, models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                  deadline_s: float = 0.0, native: Optional[Sequence[NativeModel]] = None,
                  refine_max: int = 0, root: str = "pow", lu_reuse: bool = True,
-                 tensor_cores: bool = False, bdf: Optional[Dict] = None):
+                 tensor_cores=False, bdf: Optional[Dict] = None, tile_rows: int = 0):
         L = nat.load()
         cache: Dict[int, NativeModel] = {}
         self.packs = []
@@ -166,7 +173,7 @@ class Batch:
         self.n = len(models)
         self._inst = (nat.Instance * max(self.n, 1))(*[p.instance() for p in self.packs])
         self.opts = make_opts(models[0] if self.n else None, engine, max_steps, deadline_s,
-                              refine_max, root, lu_reuse, tensor_cores, bdf)
+                              refine_max, root, lu_reuse, tensor_cores, bdf, tile_rows)
         h = C.c_void_p()
         nat.check(L.lassie_batch_create(C.cast(self._inst, C.c_void_p), self.n,
                                         C.byref(self.opts), C.byref(h)), "lassie_batch_create")
@@ -178,6 +185,14 @@ class Batch:
 
     def sync(self) -> None:
         nat.check(nat.load().lassie_batch_sync(self.handle), "lassie_batch_sync")
+
+    def tile_rows(self) -> List[int]:
+        """Rows per thread of each instance's factorisation tiles (8, 4 or 2),
+        as fixed by the options or chosen by the autotuner."""
+        rows = (C.c_int32 * max(self.n, 1))()
+        nat.check(nat.load().lassie_batch_tile_rows(self.handle, C.cast(rows, C.c_void_p)),
+                  "lassie_batch_tile_rows")
+        return [int(rows[q]) for q in range(self.n)]
 
     def launches(self) -> int:
         return int(nat.load().lassie_batch_launches(self.handle))
@@ -205,8 +220,8 @@ class Batch:
 
 def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                    deadline_s: float = 0.0, root: str = "pow",
-                   lu_reuse: bool = True,
-                   bdf: Optional[Dict] = None) -> Tuple[List[np.ndarray], List[Dict]]:
+                   lu_reuse: bool = True, bdf: Optional[Dict] = None,
+                   tile_rows: int = 0) -> Tuple[List[np.ndarray], List[Dict]]:
     """Integrate independent instances in one persistent launch (host buffers
     in and out, ``lassie_solve_batch``)."""
     L = nat.load()
@@ -221,7 +236,7 @@ def simulate_batch(models: Sequence[Model], engine: str = "mixed", max_steps: in
     inst = (nat.Instance * max(n, 1))(*[p.instance() for p in packs])
     stats = (nat.Stats * max(n, 1))()
     o = make_opts(models[0] if n else None, engine, max_steps, deadline_s, root=root,
-                  lu_reuse=lu_reuse, bdf=bdf)
+                  lu_reuse=lu_reuse, bdf=bdf, tile_rows=tile_rows)
     rc = L.lassie_solve_batch(C.cast(inst, C.c_void_p), n, C.byref(o), C.cast(stats, C.c_void_p))
     if rc not in (nat.OK, nat.ERR_MAX_STEPS, nat.ERR_DEADLINE, nat.ERR_STEP_TOO_SMALL):
         nat.check(rc, "lassie_solve_batch")

@@ -387,6 +387,27 @@ static double lo_root_perturb(double v) {
     return v * ((z & 1) ? 1.0 + g_root_rel : 1.0 - g_root_rel);
 }
 
+/* Trace (tests only): when set, every Newton right-hand side and correction
+   and every accepted RKF45 state is appended to the caller's buffer, to
+   compare two builds of this file step by step.  Process-global. */
+static double *g_trace = NULL;
+static int64_t g_trace_cap = 0, g_trace_n = 0;
+
+void lo_set_trace(double *buf, int64_t cap) {
+    g_trace = buf;
+    g_trace_cap = buf ? cap : 0;
+    g_trace_n = 0;
+}
+
+int64_t lo_trace_len(void) { return g_trace_n; }
+
+static void lo_trace(const double *v, int n) {
+    if (g_trace && g_trace_n + n <= g_trace_cap) {
+        memcpy(g_trace + g_trace_n, v, sizeof(double) * (size_t)n);
+        g_trace_n += n;
+    }
+}
+
 static void lo_perturb(int n, double *dx) {
     for (int s = 0; s < n; s++) {
         uint64_t z = g_perturb_state;
@@ -565,6 +586,7 @@ static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
         if (count == N) {
             /* accept: Simulation.cuh:742-768 */
             memcpy(y1, w1, sizeof(double) * N);
+            lo_trace(y1, N);
             if (rec) {
                 if (*rec->nsteps >= rec->cap) {
                     status = LO_ERR_MAX_STEPS;
@@ -616,7 +638,9 @@ static int lo_solve_impl(const lo_model *m, const double *k, const double *x0,
                         break;
                     }
                     memcpy(dx, xr, sizeof(double) * N);
+                    lo_trace(xr, N);
                     lo_lu_solve(N, M, piv, dx);
+                    lo_trace(dx, N);
                     if (g_perturb_rel > 0) lo_perturb(N, dx);
                     /* kernels.cuh:462-477 and Simulation.cuh:883-890 */
                     double sum = 0.0;
@@ -728,4 +752,328 @@ int lo_solve_batch(int n_inst, const lo_model *const *models,
     free(th);
     pthread_mutex_destroy(&c.mu);
     return LO_OK;
+}
+
+/* ------------------------------------------------- single-precision mode
+   The reference's -p float (Simulation<float>, simulator.cu:289-294):
+   Simulation.cuh:632-925 with T = float.  The state, rate constants, stage
+   vectors, step sizes and the Newton matrix are float; C's promotion rules
+   put the RHS term products and the RKF45 combinations in double exactly as
+   in kernels.cuh (double temporaries, float stores).  IEEE float division,
+   powf and sqrtf here; the reference's --use_fast_math build uses faster
+   approximations of the first two, so the two agree until the first step
+   decision that those last bits move.  The Newton matrix is factored with
+   partial pivoting (largest |value|, first on ties) and solved by row
+   interchanges, forward and backward substitution; the norm sums the float
+   squares in index order. */
+
+static double lo_powf_d(float base, int ex) { /* myPow<float> */
+    float potenza = 1.0f;
+    while (ex > 0) {
+        potenza = potenza * base;
+        ex--;
+    }
+    return potenza;
+}
+
+static float lo_rhs_f(const lo_model *m, const float *c, const float *y0, int i) {
+    float y1 = 0;
+    for (int e = m->sp_ptr[i]; e < m->sp_ptr[i + 1]; e++) {
+        const int y = m->sp_rxn[e];
+        const int signum = m->sp_coef[e];
+        const int b = m->rxn_ptr[y], en = m->rxn_ptr[y + 1];
+        double temp = 0;
+        if (en > b) {
+            for (int j = b; j < en; j++) {
+                if (j == b)
+                    temp += signum * c[y] * lo_powf_d(y0[m->rxn_species[j]], m->rxn_stoich[j]);
+                else
+                    temp *= lo_powf_d(y0[m->rxn_species[j]], m->rxn_stoich[j]);
+            }
+            y1 = y1 + temp;
+        } else {
+            y1 = y1 + signum * c[y];
+        }
+    }
+    return y1;
+}
+
+static float lo_jac_f(const lo_model *m, const float *c, const float *y0, int row, int gid) {
+    float y1 = 0;
+    for (int e = m->sp_ptr[row]; e < m->sp_ptr[row + 1]; e++) {
+        const int y = m->sp_rxn[e];
+        const int signum = m->sp_coef[e];
+        const int b = m->rxn_ptr[y], en = m->rxn_ptr[y + 1];
+        double temp = 0;
+        for (int j = b; j < en; j++) {
+            const int sp = m->rxn_species[j], st = m->rxn_stoich[j];
+            if (st == 1 && sp == gid) {
+                temp = temp + signum * c[y];
+                for (int jj = b; jj < en; jj++)
+                    if (m->rxn_species[jj] != gid) temp = temp * y0[m->rxn_species[jj]];
+            } else if (st > 1 && sp == gid) {
+                temp = temp + signum * c[y] * st * lo_powf_d(y0[sp], st - 1);
+                for (int jj = b; jj < en; jj++)
+                    if (m->rxn_species[jj] != gid) temp = temp * y0[m->rxn_species[jj]];
+            }
+        }
+        y1 = y1 + temp;
+    }
+    return y1;
+}
+
+static int lo_bad_f(float v) { return isnan(v) || isinf(v) || v < 0; }
+
+int lo_solve_compat_f32(const lo_model *m, const double *k, const double *x0,
+                        const double *feed_in, const double *atol, const double *tv, int nt,
+                        const int *cs, int ncs, const lo_opts *opts_in, double *out,
+                        lo_stats *st_out) {
+    lo_opts o;
+    if (opts_in)
+        o = *opts_in;
+    else {
+        o.rkf_step = 1e-3;
+        o.be_step = 0.01;
+        o.newton_tol = 1e-6;
+        o.stiffness_tol = 1e-6;
+        o.newton_iter = 10000;
+        o.max_steps = 0;
+        o.use_pow = 0;
+        o.pad = 0;
+    }
+    lo_stats st;
+    memset(&st, 0, sizeof(st));
+    const int N = m->n_species, R = m->n_reactions;
+    if (nt < 0 || (nt > 0 && (!tv || !out))) return LO_ERR_ARGS;
+    float *buf = (float *)calloc((size_t)16 * N + R + (size_t)N * N, sizeof(float));
+    int *piv = (int *)calloc((size_t)N + 1, sizeof(int));
+    if (!buf || !piv) {
+        free(buf);
+        free(piv);
+        return LO_ERR_ALLOC;
+    }
+    float *y1 = buf, *u = buf + N, *k1 = buf + 2 * N, *k2 = buf + 3 * N, *k3 = buf + 4 * N,
+          *k4 = buf + 5 * N, *k5 = buf + 6 * N, *k6 = buf + 7 * N, *w1 = buf + 8 * N,
+          *w2 = buf + 9 * N, *fd = buf + 10 * N, *tol = buf + 11 * N, *yv = buf + 12 * N,
+          *x = buf + 13 * N, *dx = buf + 14 * N, *c = buf + 16 * N, *M = c + R;
+    for (int j = 0; j < R; j++) c[j] = (float)k[j];
+    for (int s = 0; s < N; s++) {
+        y1[s] = (float)x0[s];
+        fd[s] = feed_in ? (float)feed_in[s] : 0.0f;
+        tol[s] = atol ? (float)atol[s] : (float)1e-12;
+    }
+    const float isStiff = (float)o.stiffness_tol, tollN = (float)o.newton_tol;
+    int i = 0, status = LO_OK;
+    float t1 = nt > 0 ? (float)tv[0] : 0.0f, t = 0, dt = (float)o.rkf_step;
+    float newDtBDF = (float)o.be_step;
+    while (i < nt) {
+        if (o.max_steps > 0 && st.outer_iters >= o.max_steps) {
+            status = LO_ERR_MAX_STEPS;
+            break;
+        }
+        st.outer_iters++;
+        if (fabs(t1 - t) < 1e-5) {
+            for (int j = 0; j < ncs; j++) out[(size_t)i * ncs + j] = y1[cs ? cs[j] : j];
+            i++;
+            if (i >= nt) break;
+            t1 = (float)tv[i];
+        }
+        for (int s = 0; s < N; s++) k1[s] = lo_rhs_f(m, c, y1, s);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k1[s] = fd[s];
+            else {
+                k1[s] = k1[s] * dt;
+                u[s] = y1[s] + k1[s] / 4.0;
+            }
+        }
+        for (int s = 0; s < N; s++) k2[s] = lo_rhs_f(m, c, u, s);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k2[s] = fd[s];
+            else {
+                k2[s] = k2[s] * dt;
+                u[s] = y1[s] + (3.0 * k1[s]) / 32.0 + (9.0 * k2[s]) / 32.0;
+            }
+        }
+        for (int s = 0; s < N; s++) k3[s] = lo_rhs_f(m, c, u, s);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k3[s] = fd[s];
+            else {
+                k3[s] = k3[s] * dt;
+                u[s] = y1[s] + (1932.0 * k1[s]) / 2197.0 - (7200.0 * k2[s]) / 2197.0 +
+                       (7296.0 * k3[s]) / 2197.0;
+            }
+        }
+        for (int s = 0; s < N; s++) k4[s] = lo_rhs_f(m, c, u, s);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k4[s] = fd[s];
+            else {
+                k4[s] = k4[s] * dt;
+                u[s] = y1[s] + (439.0 * k1[s]) / 216.0 - (8.0 * k2[s]) + (3680.0 * k3[s]) / 513.0 -
+                       (845.0 * k4[s]) / 4104.0;
+            }
+        }
+        for (int s = 0; s < N; s++) k5[s] = lo_rhs_f(m, c, u, s);
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k5[s] = fd[s];
+            else {
+                k5[s] = k5[s] * dt;
+                u[s] = y1[s] - (8.0 * k1[s]) / 27.0 + (2.0 * k2[s]) - (3544.0 * k3[s]) / 2565.0 +
+                       (1859.0 * k4[s]) / 4104.0 - (11.0 * k5[s]) / 40.0;
+            }
+        }
+        for (int s = 0; s < N; s++) k6[s] = lo_rhs_f(m, c, u, s);
+        int count = 0;
+        double dmin = 0.0;
+        for (int s = 0; s < N; s++) {
+            if (fd[s] != 0.0) k6[s] = fd[s];
+            else k6[s] = k6[s] * dt;
+            if (fd[s] != 0.0) {
+                w1[s] = fd[s];
+                w2[s] = fd[s];
+            } else {
+                w1[s] = y1[s] + (25.0 * k1[s]) / 216.0 + (1408.0 * k3[s]) / 2565.0 +
+                        (2197.0 * k4[s]) / 4104.0 - k5[s] / 5.0;
+                w2[s] = y1[s] + (16.0 * k1[s]) / 135.0 + (6656.0 * k3[s]) / 12825.0 +
+                        (28561.0 * k4[s]) / 56430.0 - (9.0 * k5[s] / 50.0) + (2.0 * k6[s]) / 55.0;
+            }
+            const float Rr = fabsf(w1[s] - w2[s]) / dt;
+            const float ex = 0.25f;
+            float qr = powf(tol[s] / Rr, ex);
+            if (g_root_rel > 0) qr = (float)lo_root_perturb((double)qr);
+            const float delta = 0.84 * qr;
+            if (Rr <= tol[s] && !isnan(Rr) && !isinf(Rr) && w1[s] > 0) count++;
+            const double dd = (double)delta;
+            if (s == 0 || dd < dmin) dmin = dd;
+        }
+        if (count == N) {
+            memcpy(y1, w1, sizeof(float) * N);
+            float d_temp = (float)dmin;
+            d_temp = dt * d_temp;
+            if ((t + d_temp) > t1) dt = fabsf(t1 - t);
+            else dt = d_temp;
+            t = t + dt;
+            st.rkf_accepts++;
+            continue;
+        }
+        {
+            const float d_temp = (float)dmin;
+            const float dt_old = dt;
+            dt = dt * d_temp;
+            if (!((dt < isStiff) | isnan(dt) | isinf(dt) | (fabsf(dt_old - dt) < 1e-3))) {
+                st.rkf_retries++;
+                continue;
+            }
+        }
+        dt = newDtBDF;
+        if ((t + dt) > t1) dt = fabsf(t1 - t);
+        memcpy(yv, y1, sizeof(float) * N);
+        st.be_steps++;
+        int64_t itN = 0;
+        float errN = 1000;
+        int luFail = 0;
+        while ((itN < o.newton_iter) & (errN > tollN)) {
+            for (int s = 0; s < N; s++) x[s] = lo_rhs_f(m, c, yv, s);
+            for (int s = 0; s < N; s++) x[s] = -(yv[s] - y1[s] - dt * x[s]);
+            if (itN == 0) {
+                for (int r = 0; r < N; r++)
+                    for (int g = 0; g < N; g++) {
+                        const float J = lo_jac_f(m, c, yv, r, g);
+                        const float I = (r == g) ? 1.0f : 0.0f;
+                        M[(size_t)r * N + g] = I - dt * J;
+                    }
+                st.lu_factorisations++;
+                for (int j = 0; j < N && !luFail; j++) {
+                    int p = j;
+                    float best = fabsf(M[(size_t)j * N + j]);
+                    for (int r = j + 1; r < N; r++) {
+                        const float v = fabsf(M[(size_t)r * N + j]);
+                        if (v > best) {
+                            best = v;
+                            p = r;
+                        }
+                    }
+                    piv[j] = p;
+                    if (!(best > 0.0f)) {
+                        luFail = 1;
+                        break;
+                    }
+                    if (p != j)
+                        for (int cc = 0; cc < N; cc++) {
+                            const float tmp = M[(size_t)j * N + cc];
+                            M[(size_t)j * N + cc] = M[(size_t)p * N + cc];
+                            M[(size_t)p * N + cc] = tmp;
+                        }
+                    const float d = M[(size_t)j * N + j];
+                    for (int r = j + 1; r < N; r++) M[(size_t)r * N + j] /= d;
+                    for (int r = j + 1; r < N; r++)
+                        for (int cc = j + 1; cc < N; cc++)
+                            M[(size_t)r * N + cc] -= M[(size_t)r * N + j] * M[(size_t)j * N + cc];
+                }
+            }
+            if (luFail) {
+                for (int s = 0; s < N; s++)
+                    if (lo_bad_f(yv[s])) yv[s] = y1[s];
+                newDtBDF = dt * 0.1f;
+                st.lu_failures++;
+                break;
+            }
+            memcpy(dx, x, sizeof(float) * N);
+            for (int j = 0; j < N; j++) {
+                const int p = piv[j];
+                if (p != j) {
+                    const float tmp = dx[j];
+                    dx[j] = dx[p];
+                    dx[p] = tmp;
+                }
+            }
+            for (int r = 0; r < N; r++) {
+                float acc = dx[r];
+                for (int j = 0; j < r; j++) acc -= M[(size_t)r * N + j] * dx[j];
+                dx[r] = acc;
+            }
+            for (int r = N - 1; r >= 0; r--) {
+                float acc = dx[r];
+                for (int j = r + 1; j < N; j++) acc -= M[(size_t)r * N + j] * dx[j];
+                dx[r] = acc / M[(size_t)r * N + r];
+            }
+            if (g_perturb_rel > 0)
+                for (int s = 0; s < N; s++) {
+                    uint64_t z = g_perturb_state;
+                    z ^= z << 13;
+                    z ^= z >> 7;
+                    z ^= z << 17;
+                    g_perturb_state = z;
+                    dx[s] = dx[s] * ((z & 1) ? 1.0f + (float)g_perturb_rel : 1.0f - (float)g_perturb_rel);
+                }
+            float sum = 0.0f;
+            for (int s = 0; s < N; s++) {
+                const float old = yv[s];
+                if (fd[s] == 0) yv[s] = yv[s] + dx[s];
+                else yv[s] = fd[s];
+                dx[s] = yv[s] - old;
+                sum = sum + dx[s] * dx[s];
+            }
+            errN = sqrtf(sum);
+            itN = itN + 1;
+            st.newton_iters++;
+        }
+        if (!luFail) {
+            int anybad = 0;
+            for (int s = 0; s < N; s++) anybad |= lo_bad_f(yv[s]);
+            if (anybad) {
+                for (int s = 0; s < N; s++)
+                    if (lo_bad_f(yv[s])) yv[s] = y1[s];
+                newDtBDF = dt * 0.1f;
+                st.nan_reverts++;
+            }
+        }
+        memcpy(y1, yv, sizeof(float) * N);
+        t = t + dt;
+    }
+    st.t_final = t;
+    st.dt_be_final = newDtBDF;
+    if (st_out) *st_out = st;
+    free(buf);
+    free(piv);
+    return status;
 }

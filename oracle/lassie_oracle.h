@@ -84,6 +84,10 @@ void lo_set_solve_perturbation(double rel, uint64_t seed);
 /* Tests only: scale every RKF45 quarter root (atol/R)^(1/4) by (1 +- rel)
    with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
 void lo_set_root_perturbation(double rel, uint64_t seed);
+/* Tests only: append every Newton right-hand side and correction and every
+   accepted RKF45 state to buf (at most cap doubles); NULL turns it off. */
+void lo_set_trace(double *buf, int64_t cap);
+int64_t lo_trace_len(void);
 /* Tests only: pick the LU's rounding order (0 default; 1 the triangular
    solves, 2 the Schur update, 3 both, round products and sums separately
    instead of using fma); process-global, not thread safe. */
@@ -113,6 +117,16 @@ int lo_solve_compat(const lo_model *m, const double *k, const double *x0,
                     const double *feed, const double *atol, const double *t,
                     int nt, const int *cs, int ncs, const lo_opts *opts,
                     double *out, lo_stats *stats);
+
+/* The reference's -p float loop (Simulation<float>): as lo_solve_compat with
+   float state, rate constants, stages, step sizes and Newton matrix and the
+   reference's double temporaries; IEEE float division, powf and sqrtf.  The
+   perturbation probes apply with float-sized factors (rel = 2^-23 moves a
+   float by an ulp). */
+int lo_solve_compat_f32(const lo_model *m, const double *k, const double *x0,
+                        const double *feed, const double *atol, const double *t,
+                        int nt, const int *cs, int ncs, const lo_opts *opts,
+                        double *out, lo_stats *stats);
 
 /* As lo_solve_compat, recording the step sequence: kind[n] (0 accepted
    RKF45, 1 backward Euler, 2 state unchanged, 3 reverted species) and dt[n]

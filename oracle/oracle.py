@@ -89,6 +89,8 @@ def lib():
             L.lo_lu_solve.argtypes = [C.c_int, _f64p, _i32p, _f64p]
             L.lo_set_solve_perturbation.argtypes = [C.c_double, C.c_uint64]
             L.lo_set_lu_variant.argtypes = [C.c_int]
+            L.lo_set_trace.argtypes = [C.c_void_p, C.c_int64]
+            L.lo_trace_len.restype = C.c_int64
             L.lo_set_root_perturbation.argtypes = [C.c_double, C.c_uint64]
             L.lo_qroot_rn.argtypes = [C.c_double]
             L.lo_qroot_rn.restype = C.c_double
@@ -96,6 +98,8 @@ def lib():
                                           C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
                                           C.POINTER(Opts), _f64p, C.POINTER(Stats)]
             L.lo_solve_compat.restype = C.c_int
+            L.lo_solve_compat_f32.argtypes = L.lo_solve_compat.argtypes
+            L.lo_solve_compat_f32.restype = C.c_int
             L.lo_solve_compat_rec.argtypes = [C.POINTER(_Model), _f64p, _f64p, C.c_void_p,
                                               C.c_void_p, _f64p, C.c_int, C.c_void_p, C.c_int,
                                               C.POINTER(Opts), _f64p, C.POINTER(Stats), C.c_int,
@@ -180,9 +184,11 @@ def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
-def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None, root: str = "sqrt"):
+def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None, root: str = "sqrt",
+          precision: str = "double"):
     """Integrate a ``lassie_gb300.model.Model`` with the oracle (``root`` as
-    in ``make_opts``).  Returns (trajectory [nt, ncs], stats dict, status)."""
+    in ``make_opts``; ``precision`` "float": the reference's -p float loop).
+    Returns (trajectory [nt, ncs], stats dict, status)."""
     om = om or OracleModel(model.left, model.right)
     N = model.n_species
     k = np.ascontiguousarray(model.k, np.float64)
@@ -194,7 +200,8 @@ def solve(model, max_steps: int = 0, om: Optional[OracleModel] = None, root: str
     out = np.zeros((t.shape[0], cs.shape[0]))
     st = Stats()
     o = make_opts(model, max_steps, root)
-    rc = lib().lo_solve_compat(C.byref(om._m), k, x0, _ptr(feed), _ptr(atol), t,
+    fn = lib().lo_solve_compat_f32 if precision == "float" else lib().lo_solve_compat
+    rc = fn(C.byref(om._m), k, x0, _ptr(feed), _ptr(atol), t,
                                t.shape[0], _ptr(cs), cs.shape[0], C.byref(o), out,
                                C.byref(st))
     return out, st.as_dict(), rc

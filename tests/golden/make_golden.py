@@ -5,7 +5,9 @@ by ``oracle/build_ref.sh`` with 17-digit Solution output) on seeded small
 models and stores inputs and outputs as ``tests/golden/<case>.npz``.  The
 reference binary needs a CUDA GPU, so this runs on the GPU machine:
 
-    python tests/golden/make_golden.py <out_dir>
+    python tests/golden/make_golden.py <out_dir> [--float]
+
+(--float: the reference's -p float runs, stored under tests/golden/float/).
 
 Each fixture holds the dense stoichiometries, rate constants, initial state,
 sampling times, the reference's trajectory (``ref``), its number of loop
@@ -54,15 +56,17 @@ def read_solution(path: str, ncols: int) -> np.ndarray:
     return np.asarray(rows)
 
 
-def main(out_dir: str) -> int:
+def main(out_dir: str, precision: str = "double") -> int:
+    """precision "float": the reference's -p float runs (Simulation<float>)."""
     os.makedirs(out_dir, exist_ok=True)
     status = 0
+    extra = ["-p", "float"] if precision == "float" else []
     for name, m in cases():
         with tempfile.TemporaryDirectory() as tmp:
             inp, outp = os.path.join(tmp, "in"), os.path.join(tmp, "out")
             write_folder(m, inp)
             t0 = time.time()
-            r = subprocess.run([REF, inp, outp], stdout=subprocess.PIPE,
+            r = subprocess.run([REF, inp, outp] + extra, stdout=subprocess.PIPE,
                                stderr=subprocess.PIPE, text=True, timeout=1200)
             wall = time.time() - t0
             mt = re.search(r"LASSIE_REF integration_ms ([0-9.eE+-]+)", r.stderr)
@@ -87,4 +91,7 @@ def main(out_dir: str) -> int:
 
 
 if __name__ == "__main__":
-    sys.exit(main(sys.argv[1] if len(sys.argv) > 1 else os.path.join(ROOT, "tests", "golden")))
+    args = [a for a in sys.argv[1:] if a != "--float"]
+    prec = "float" if "--float" in sys.argv[1:] else "double"
+    default = os.path.join(ROOT, "tests", "golden", "float" if prec == "float" else "")
+    sys.exit(main(args[0] if args else default, prec))

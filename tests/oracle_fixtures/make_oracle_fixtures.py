@@ -1,10 +1,18 @@
 """Fixtures computed by the CPU oracle (oracle/) for cases too slow to run
-inside the test suite: the 4096-species workload on t in [0, 0.02] (two
-backward-Euler steps with 4096 x 4096 LU factorisations, about two minutes
-on one core).  The GPU machine has no reference checkout, and its tests must
-not spend minutes in the oracle, so the trajectory is stored:
+inside the test suite.  The GPU machine's tests must not spend minutes in
+the oracle, so the trajectories are stored:
 
-    python tests/oracle_fixtures/make_oracle_fixtures.py
+  * c3_t002: the 4096-species workload on t in [0, 0.02] (two
+    backward-Euler steps with 4096 x 4096 LU factorisations, about two
+    minutes on one core);
+  * c3_t05: the same network on t in [0, 0.5] (11 samples, about fifty
+    backward-Euler steps, tens of minutes);
+  * c2_full: the stiff 512-species network over its whole horizon
+    t in [0, 100] with its 200 samples;
+  * c5_full: the 256-species adjoint network (base rate constants) over its
+    whole horizon, 40 samples in (0, 10].
+
+    python tests/oracle_fixtures/make_oracle_fixtures.py [name ...]
 
 Each fixture holds the sampling times, the oracle's trajectory and status
 and its step counts; the network and its parameters are regenerated from
@@ -30,17 +38,28 @@ def c3_short():
     return synth.shorten(synth.make_c3(), 0.02, 3)
 
 
-CASES = {"c3_t002": c3_short}
+def c3_t05():
+    return synth.shorten(synth.make_c3(), 0.5, 11)
+
+
+def c5_full():
+    return synth.make_c5(1)[0][0]
+
+
+CASES = {"c3_t002": c3_short, "c3_t05": c3_t05, "c2_full": synth.make_c2, "c5_full": c5_full}
 
 
 def main():
-    for name, make in CASES.items():
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        make = CASES[name]
         m = make()
         t0 = time.time()
         out, st, rc = O.solve(m)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), t=m.t, out=out, status=rc,
                             be_steps=st["be_steps"], rkf_accepts=st["rkf_accepts"],
-                            newton_iters=st["newton_iters"], seconds=time.time() - t0)
+                            newton_iters=st["newton_iters"], nan_reverts=st["nan_reverts"],
+                            seconds=time.time() - t0)
         print(name, rc, st, "%.1fs" % (time.time() - t0), flush=True)
 
 

@@ -161,3 +161,28 @@ def test_adjoint_refuses_the_bdf_controller(native):
     rc = native.lassie_adjoint_batch(C.byref(inst), 1, C.cast(tp, C.c_void_p), C.byref(opts), 0, 0,
                                      loss.ctypes.data, C.cast(gp, C.c_void_p), None, None)
     assert rc == nat.ERR_ARGS
+
+
+def test_tile_rows_option_checked_on_host(native):
+    """lassie_opts.tile_rows: 0 (autotuned) by default; 8, 4 or 2 fix the
+    factorisation's tile rows; anything else is refused before any device
+    query."""
+    from lassie_gb300 import solver
+    o = nat.Opts()
+    native.lassie_opts_default(C.byref(o))
+    assert o.tile_rows == 0
+    m = synth.make_c1()
+    nm = solver.NativeModel.of(m)
+    pk = solver._Packed(m, nm)
+    inst = nat.Instance()
+    inst.model, inst.k, inst.x0 = nm.handle, pk.k.ctypes.data, pk.x0.ctypes.data
+    inst.t, inst.nt = pk.t.ctypes.data, pk.t.shape[0]
+    inst.out, inst.cs, inst.ncs = pk.out.ctypes.data, None, 0
+    for rows, want in ((3, (nat.ERR_ARGS,)), (16, (nat.ERR_ARGS,)), (-1, (nat.ERR_ARGS,)),
+                       (4, (nat.OK, nat.ERR_NO_DEVICE))):
+        opts = solver.make_opts(m, tile_rows=rows)
+        h = C.c_void_p()
+        rc = native.lassie_batch_create(C.byref(inst), 1, C.byref(opts), C.byref(h))
+        if rc == 0:
+            native.lassie_batch_destroy(h)
+        assert rc in want, (rows, rc)

@@ -75,3 +75,19 @@ def test_compile_model_orders():
     for j in range(cm.n_reactions):
         sp = cm.rxn_species[cm.rxn_ptr[j]:cm.rxn_ptr[j + 1]]
         assert np.all(np.diff(sp) > 0)
+
+
+def test_synthetic_powers_are_correctly_rounded():
+    """10^u and exp(x) of the generators are correctly rounded (checked
+    against 50-digit decimal arithmetic), so a seed gives the same network on
+    every machine."""
+    from decimal import Decimal, getcontext
+    from lassie_gb300 import synth
+    getcontext().prec = 50
+    rng = np.random.default_rng(11)
+    u = np.concatenate([rng.uniform(-8, 8, 3000), [-6.0, -4.0, 0.0, 0.5, 2.0, 6.0]])
+    want = np.array([float(Decimal(10) ** Decimal(x)) for x in u])
+    assert np.array_equal(synth.pow10(u), want)
+    x = np.concatenate([rng.normal(0, 3, 3000), [0.0, -1.0, 1.0]])
+    want = np.array([float(Decimal(v).exp()) for v in x])
+    assert np.array_equal(synth.exp_rn(x), want)

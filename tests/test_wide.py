@@ -69,24 +69,34 @@ def test_wide_c3_matches_stored_oracle_trajectory(gpu):
     assert st["newton_iters"] == int(d["newton_iters"])
 
 
+# BF16 factors are good to about 2^-9, so the refinement may take more
+# sweeps than the default cap of 8
+TC_MODES = [("tf32", 0), ("bf16", 32)]
+
+
 @pytest.mark.parametrize("N,inst", CASES[:1], ids=["n600-1"])
-def test_wide_tensor_cores_match_oracle(gpu, N, inst):
-    """Rank-32 updates on the tensor cores (tcgen05, TF32 products of split
-    operands): the refinement brings the solves to the FP64 solution, so the
-    trajectory meets the same bar as the FP32-pipe factorisation."""
+@pytest.mark.parametrize("mode,refine_max", TC_MODES, ids=[m for m, _ in TC_MODES])
+def test_wide_tensor_cores_match_oracle(gpu, N, inst, mode, refine_max):
+    """Rank-32 updates on the tensor cores (tcgen05; TF32 products of split
+    operands, or BF16 operands with FP32 accumulation): the refinement
+    brings the solves to the FP64 solution, so the trajectory meets the same
+    bar as the FP32-pipe factorisation."""
     m = synth.shorten(synth.make_sized(N, inst), 0.2, 5)
     ref, st_ref, rc = O.solve(m)
-    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt", tensor_cores=True)
+    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt", tensor_cores=mode,
+                              refine_max=refine_max)
     assert st["status"] == 0
     assert within(out, ref), float(np.max(np.abs(out - ref) - RTOL * np.abs(ref)))
     assert (st["be_steps"], st["rkf_accepts"], st["newton_iters"]) == \
         (st_ref["be_steps"], st_ref["rkf_accepts"], st_ref["newton_iters"])
 
 
-def test_wide_c3_tensor_cores_match_stored_oracle_trajectory(gpu):
+@pytest.mark.parametrize("mode,refine_max", TC_MODES, ids=[m for m, _ in TC_MODES])
+def test_wide_c3_tensor_cores_match_stored_oracle_trajectory(gpu, mode, refine_max):
     d = np.load(os.path.join(HERE, "oracle_fixtures", "c3_t002.npz"))
     m = synth.shorten(synth.make_c3(), 0.02, 3)
-    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt", tensor_cores=True)
+    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt", tensor_cores=mode,
+                              refine_max=refine_max)
     assert st["status"] == 0
     assert within(out, d["out"]), float(np.max(np.abs(out - d["out"]) - RTOL * np.abs(d["out"])))
     assert st["newton_iters"] == int(d["newton_iters"])
