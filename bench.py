@@ -39,6 +39,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -120,14 +122,38 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def load_traffic():
-    """Per-launch DRAM bytes of the integrator kernel from the committed ncu
-    summary (scaled to the full batch), or None."""
+def load_traffic(alg_flops):
+    """DRAM bytes of one integrator launch: the bytes per algorithmic FLOP of
+    a committed ncu capture of the kernel on a small case
+    (profiles/compat_kernel_traffic.json), times this launch's algorithmic
+    FLOPs -- the kernel's traffic grows with its factorisations and sweeps.
+    None without the file."""
     p = os.path.join(ROOT, "profiles", "compat_kernel_traffic.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            return json.load(f).get("dram_bytes_per_full_launch")
-    return None
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        per_flop = json.load(f).get("dram_bytes_per_algorithmic_flop")
+    return None if per_flop is None else per_flop * alg_flops
+
+
+def pipe_work(stats, models):
+    """Work of the mixed batched integrator on the pipes that bound it.
+    FP32 (the FMA pipes): the Gauss-Jordan inverses, 2 N^3 per factorisation,
+    and the refinement's matrix-vector products, 2 N^2 per sweep.  FP64: one
+    RHS evaluation costs about nnz_A + 2 nnz_H operations (products of the
+    reactant powers, then the signed species sums) -- six per RKF45 attempt
+    and one per Newton iteration -- and one refinement residual about the
+    same through J v plus 3 N."""
+    f32 = f64 = 0.0
+    for s, m in zip(stats, models):
+        n = float(m.n_species)
+        na = float(np.count_nonzero(m.left))
+        nh = float(np.count_nonzero(np.asarray(m.right) - np.asarray(m.left)))
+        f32 += s["lu_factorisations"] * 2.0 * n ** 3 + s["refine_sweeps"] * 2.0 * n * n
+        attempts = s["rkf_accepts"] + s["rkf_retries"] + s["be_steps"]
+        f64 += (6.0 * attempts + s["newton_iters"]) * (na + 2.0 * nh)
+        f64 += s["refine_sweeps"] * (na + 2.0 * nh + 3.0 * n)
+    return f32, f64
 
 
 def lu_flops(stats, models, engine):
@@ -600,11 +626,11 @@ def main():
                     help="c4: the 2048-instance batch (default); c3: the 4096-species "
                          "network on the wide engine (t in [0, 50], or --horizon); "
                          "kernels: the RHS and Newton-matrix kernels alone")
-    ap.add_argument("--tensor-cores", nargs="?", const="tf32", default="off",
+    ap.add_argument("--tensor-cores", nargs="?", const="tf32", default="tf32",
                     choices=["off", "tf32", "bf16"],
-                    help="c3: rank-32 updates of the factorisation on the tensor cores, with "
-                         "split TF32 operands (tf32, the flag alone) or BF16 operands and "
-                         "FP32 accumulation (bf16)")
+                    help="c3: rank-32 updates of the factorisation on the FP32 pipes (off) or "
+                         "on the tensor cores, with split TF32 operands (tf32, the default) or "
+                         "BF16 operands and FP32 accumulation (bf16)")
     ap.add_argument("--scaling", default="weak", choices=["weak", "strong"],
                     help="weak: every rank integrates its own --instances instances "
                          "(default); strong: the ranks split one batch of --instances")
@@ -699,11 +725,28 @@ def main():
     k_ms = statistics.mean(kernel_ms)
     achieved = flops / (k_ms * 1e-3) / 1e12
     peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
+    # the pipes that bound it: FP32 FMA (152 SMs x 128 lanes x 2 FLOP x the
+    # maximum SM clock) and FP64 (the GB300's FP64 rate, 1.25 TFLOP/s nominal)
+    f32, f64 = pipe_work(stats, models)
+    sm_ghz = float(peaks.get("sm_max_mhz", 2070.0)) / 1000.0
+    fp32_peak = 152 * 128 * 2 * sm_ghz / 1000.0
     roofline = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": load_traffic(),
+                "frac": achieved / peak, "traffic": load_traffic(flops),
                 "kernel": "compat_kernel<float>", "kernel_ms": k_ms,
                 "algorithmic_flops_per_launch": flops,
-                "peak_kind": f"{peak_kind} bf16 sustained"}
+                "peak_kind": f"{peak_kind} bf16 sustained",
+                "pipes": {
+                    "fp32_fma": {"achieved_tflops": f32 / (k_ms * 1e-3) / 1e12,
+                                 "peak_tflops": fp32_peak,
+                                 "frac": f32 / (k_ms * 1e-3) / 1e12 / fp32_peak,
+                                 "flops_per_launch": f32,
+                                 "peak_kind": "nominal: 152 SMs x 128 FP32 lanes x 2 x max clock"},
+                    "fp64": {"achieved_tflops": f64 / (k_ms * 1e-3) / 1e12,
+                             "peak_tflops": 1.25,
+                             "frac": f64 / (k_ms * 1e-3) / 1e12 / 1.25,
+                             "flops_per_launch": f64, "peak_kind": "nominal GB300 FP64"},
+                    "note": "latency-bound: one 512-thread CTA per instance; issue and "
+                            "pipe activity in the ncu summaries under profiles/"}}
 
     line = {"metric": METRIC, "value": value, "unit": "sims/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,

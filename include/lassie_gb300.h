@@ -98,8 +98,8 @@ typedef struct {
                              TF32 products of split operands, close to FP32),
                              LASSIE_TC_BF16 with BF16 operands and FP32
                              accumulation (factors good to about 2^-9; the FP64
-                             refinement takes more sweeps), LASSIE_TC_OFF
-                             (default) on the FP32 pipes */
+                             refinement takes more sweeps), LASSIE_TC_OFF on
+                             the FP32 pipes; default LASSIE_TC_TF32 */
     int32_t controller;   /* LASSIE_CTRL_* (default LASSIE_CTRL_COMPAT) */
     /* LASSIE_CTRL_BDF only: */
     double rtol;          /* relative tolerance (1e-6) */

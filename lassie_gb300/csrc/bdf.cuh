@@ -39,6 +39,7 @@
 constexpr int kBdfMaxOrder = 5;
 constexpr int kBdfNewtonMaxIter = 4;
 constexpr int kBdfFallback = 4;  // Newton failures in a row before FP64 factors (mixed)
+constexpr int kBdfFp64Steps = 32;  // accepted steps on FP64 factors before FP32 again
 constexpr int kBdfVecs = kBdfMaxOrder + 3 + 12;  // differences + work vectors
 constexpr double kBdfMinFactor = 0.2, kBdfMaxFactor = 10.0;
 constexpr double kBdfEps = 2.220446049250313e-16;  // 2^-52
@@ -198,11 +199,14 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     }
     int status = LASSIE_OK;
     int q = 1;
-    // mixed form: after kBdfFallback Newton failures in a row the instance
-    // factors in FP64 from then on (the workspace has FP64 room; the FP32
-    // panel buffers are as large as the FP64 ones, the solve vector is res)
+    // mixed form: a Newton failure on FP32 factors retries the step on FP64
+    // factors at the same size; after kBdfFallback FP32 failures without an
+    // FP32 success in between, the instance factors in FP64 for the next
+    // kBdfFp64Steps accepted steps, each further stretch twice as long (the
+    // workspace has FP64 room; the FP32 panel buffers are as large as the
+    // FP64 ones, the solve vector is res)
     bool fp64_lu = !kMixed;
-    int fail_run = 0;
+    int fail_run = 0, fp64_left = 0, fp64_stretch = kBdfFp64Steps;
     double h = 0.0;
     int64_t attempts = 0, rhs_evals = 0, jac_evals = 0;
     if (isample < nt) {
@@ -434,9 +438,21 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                 }
                 if (!converged) {
                     if (tid == 0) st.lu_failures++;
-                    if (kMixed && !fp64_lu && ++fail_run >= kBdfFallback) {
+                    if (kMixed && !fp64_lu) {
+                        // the FP32 inverse may be what failed: the same step
+                        // once more on FP64 factors before the step shrinks;
+                        // after kBdfFallback such failures without an FP32
+                        // success in between, a longer FP64 stretch
                         fp64_lu = true;
-                        if (tid == 0) st.nan_reverts++;  // counts the switch
+                        if (++fail_run >= kBdfFallback) {
+                            fp64_left = fp64_stretch;
+                            fp64_stretch = min(2 * fp64_stretch, 1 << 20);
+                            if (tid == 0) st.nan_reverts++;  // counts the stretches
+                        } else {
+                            fp64_left = 1;
+                        }
+                        lu_valid = false;
+                        continue;
                     }
                     bdf_change_d(Dd, vstride, N, q, 0.5);
                     h = h * 0.5;
@@ -464,7 +480,11 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                     continue;
                 }
                 accepted = true;
-                fail_run = 0;
+                if (!fp64_lu) fail_run = 0;
+                if (kMixed && fp64_lu && --fp64_left <= 0) {
+                    fp64_lu = false;  // back to FP32 factors at the next factorisation
+                    lu_valid = false;
+                }
                 if (tid == 0) st.be_steps++;
                 n_equal++;
                 tc = t_new;

@@ -293,7 +293,7 @@ extern "C" void lassie_opts_default(lassie_opts *o) {
     o->refine_max = 0;
     o->quarter_root = LASSIE_ROOT_POW;
     o->lu_reuse = 1;
-    o->tensor_cores = 0;
+    o->tensor_cores = LASSIE_TC_TF32;
     o->controller = LASSIE_CTRL_COMPAT;
     o->rtol = 1e-6;
     o->atol = 1e-9;

@@ -1519,9 +1519,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     // FP32 form: inverted diagonal blocks of the factors follow the matrix
     float *dinv = reinterpret_cast<float *>(M + (int64_t)N * ld);
     int *wflag = ired + kWarps + 1;  // wide engine: join results
-    // the per-CTA form stops on the state's resolution, which small species
-    // may reach a few sweeps after the rest
-    const int refine_max = P.refine_max > 0 ? P.refine_max : (kWide ? 8 : 12);
+    const int refine_max = P.refine_max > 0 ? P.refine_max : 8;
     const bool root_sqrt = (D.flags & 1) != 0;
     const int tile_rows = tile_rows_of(D.flags);
     long long c_mark = 0;
@@ -1691,6 +1689,25 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         };
         if (tid == 0) st.be_steps++;
         bool expired = false;
+        // mixed form: a step that reused an earlier step's factors and ends
+        // with negative or non-finite species is solved once more from y1
+        // with fresh factors before the reference's revert applies (stale
+        // factors converge in norm but can leave species far below the others
+        // inexact); fresh_only forces the fresh factorisation
+        bool fresh_only = false, step_reused = false;
+        for (int pass = 0; pass < 2; pass++) {
+        if (pass > 0) {
+            for (int s = tid; s < N; s += kThreads) yv[s] = V.y1[s];
+            __syncthreads();
+            itN = 0;
+            errN = 1000;
+            luFail = false;
+            reused = false;
+            soft = false;
+            fresh_only = true;
+            lu_valid = false;
+        }
+        step_reused = false;
         while ((itN < D.newton_iter) & (errN > D.newton_tol)) {
             if (wide_abort) break;
             if (deadline && (itN & 63) == 63) {
@@ -1719,8 +1736,10 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             if (itN == 0) {
                 reused = false;
                 if constexpr (kMixed)
-                    reused = P.lu_reuse && lu_valid && dt == lu_dt && lu_rate <= kReuseRate;
+                    reused = !fresh_only && P.lu_reuse && lu_valid && dt == lu_dt &&
+                             lu_rate <= kReuseRate;
                 if (reused) {
+                    step_reused = true;
                     // factors of an earlier step precondition this step's
                     // refinement; the diagonal is this step's
                     c_mark = clock64();
@@ -1785,7 +1804,6 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                             le >= -1022 ? (long long)(le + 1023) << 52
                                         : (le >= -1074 ? 1LL << (le + 1074) : 0LL);
                         double cmax, xmax;
-                        bool still_moving = true;
                         if constexpr (kWide) {
                             // scaling, matrix-vector product and update on the grid
                             const long long c_tri = clock64();
@@ -1804,8 +1822,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                                   reinterpret_cast<float *>(bvec), reinterpret_cast<float *>(lt),
                                   false);
                         if (tid == 0) st.cycles_solve_tri += clock64() - c_tri;
-                        long long cmb = 0;
-                        bool moved = false;
+                        long long cmb = 0, xmb = 0;
                         for (int s = tid; s < N; s += kThreads) {
                             double c = (double)reinterpret_cast<const float *>(lt)[perm[s]] * isc;
                             // the part of this row's right-hand side that the
@@ -1816,39 +1833,35 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
                                 if (fabs(mdiag[s]) >= 0.5)
                                     c += (rs - (double)(float)rs) * isc / mdiag[s];
                             }
-                            const double ox = dx[s];
-                            const double nx = ox + c;
+                            const double nx = dx[s] + c;
                             dx[s] = nx;
                             cmb = max(cmb, absbits_nonan(c));
-                            // does this correction still change the state
-                            // the Newton update will form?
-                            if (V.fd[s] == 0 && !((yv[s] + nx) == (yv[s] + ox))) moved = true;
+                            xmb = max(xmb, absbits_nonan(nx));
                         }
                         cmax = __longlong_as_double(cmb);
-                        xmax = 0.0;
-                        cmax = block_max(cmax, red);
-                        still_moving = __syncthreads_or(moved) != 0;
+                        xmax = __longlong_as_double(xmb);
+                        block_max2(cmax, xmax, red);
                         }
                         if (tid == 0) st.refine_sweeps++;
                         if (sweep > 0) rate = fmax(rate, cmax / prev);
-                        bool done;
-                        if constexpr (kWide) {
-                            // stop when this correction, or the next one
-                            // predicted from the contraction so far, is below
-                            // FP64 resolution of dx
-                            const bool small_next =
-                                sweep > 0 && !(cmax * (cmax / prev) > 1e-16 * xmax);
-                            done = !(cmax > 1e-15 * xmax) || small_next;
-                        } else {
-                            // stop when this correction changes no species
-                            // of the state y + dx in FP64 (subnormal species
-                            // included).  A normwise test would leave species
-                            // far below the others with large relative errors,
-                            // and LASSIE's loop decides on absolute quantities
-                            // (RKF45 atol 1e-12, species that must stay
-                            // positive).
-                            done = !still_moving;
-                        }
+                        // stop when this correction, or the next one predicted
+                        // from the contraction so far, is below FP64 resolution
+                        // of dx.  Fresh factors contract geometrically (their
+                        // error is rounding noise): the last ratio predicts the
+                        // next one.  Reused factors precondition another
+                        // matrix, whose iteration need not contract evenly: the
+                        // prediction takes the worst ratio of the solve and
+                        // waits for three corrections.  (A test on the state's
+                        // last bits instead -- stop when no species of y + dx
+                        // moves -- was measured and dropped: species many
+                        // orders below the others cannot be resolved through
+                        // the FP32 inverse, extra sweeps only scatter their
+                        // sign, and the batch took three times the FP64 form's
+                        // negative-species reverts.)
+                        const double r_est = soft ? rate : cmax / prev;
+                        const bool small_next =
+                            sweep >= (soft ? 2 : 1) && !(cmax * r_est > 1e-16 * xmax);
+                        const bool done = !(cmax > 1e-15 * xmax) || small_next;
                         if (!finite || done) {
                             converged = true;
                             break;
@@ -1913,6 +1926,11 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
             errN = sqrt(block_sum(sq, red));
             itN = itN + 1;
             if (tid == 0) st.newton_iters++;
+        }
+        if (!kMixed || pass > 0 || !step_reused || luFail || expired || wide_abort) break;
+        bool stale_bad = false;
+        for (int s = tid; s < N; s += kThreads) stale_bad |= bad_value(yv[s]);
+        if (!__syncthreads_or(stale_bad)) break;
         }
         bool reverted = false;
         if (!luFail) {

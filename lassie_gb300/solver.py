@@ -59,9 +59,9 @@ class NativeModel:
 
 
 ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
-# rank-32 updates of the wide engine's factorisation: FP32 pipes, tensor
-# cores with split TF32 operands (True or "tf32"), or BF16 operands with FP32
-# accumulation ("bf16")
+# rank-32 updates of the wide engine's factorisation: FP32 pipes ("off"),
+# tensor cores with split TF32 operands ("tf32", the default, or True), or
+# BF16 operands with FP32 accumulation ("bf16")
 TENSOR_CORES = {False: 0, True: 1, "off": 0, "tf32": 1, "bf16": 2}
 
 
@@ -70,7 +70,7 @@ BDF_KEYS = ("rtol", "atol", "first_step", "max_step", "max_order")
 
 def make_opts(m: Optional[Model] = None, engine: str = "mixed", max_steps: int = 0,
               deadline_s: float = 0.0, refine_max: int = 0, root: str = "pow",
-              lu_reuse: bool = True, tensor_cores=False,
+              lu_reuse: bool = True, tensor_cores="tf32",
               bdf: Optional[Dict] = None, tile_rows: int = 0) -> nat.Opts:
     """Options of a solve.  ``bdf`` (a dict, possibly empty, of rtol, atol,
     first_step, max_step, max_order) selects the BDF controller with rtol/atol
@@ -131,7 +131,7 @@ class _Packed:
 
 def simulate(m: Model, engine: str = "mixed", max_steps: int = 0, deadline_s: float = 0.0,
              nm: Optional[NativeModel] = None, root: str = "pow",
-             lu_reuse: bool = True, tensor_cores=False,
+             lu_reuse: bool = True, tensor_cores="tf32",
              bdf: Optional[Dict] = None, refine_max: int = 0) -> Tuple[np.ndarray, Dict]:
     """Integrate one model on the GPU.  Returns (trajectory [nt, ncs], stats)."""
     nm = nm or NativeModel.of(m)
@@ -157,7 +157,7 @@ class Batch:
     def __init__(self, models: Sequence[Model], engine: str = "mixed", max_steps: int = 0,
                  deadline_s: float = 0.0, native: Optional[Sequence[NativeModel]] = None,
                  refine_max: int = 0, root: str = "pow", lu_reuse: bool = True,
-                 tensor_cores=False, bdf: Optional[Dict] = None, tile_rows: int = 0):
+                 tensor_cores="tf32", bdf: Optional[Dict] = None, tile_rows: int = 0):
         L = nat.load()
         cache: Dict[int, NativeModel] = {}
         self.packs = []

@@ -360,10 +360,20 @@ typedef struct {
    safe: set it, solve on one thread, reset it to 0. */
 static double g_perturb_rel = 0.0;
 static uint64_t g_perturb_state = 0;
+static int g_perturb_normwise = 0;
 
 void lo_set_solve_perturbation(double rel, uint64_t seed) {
     g_perturb_rel = rel;
     g_perturb_state = seed * 0x9E3779B97F4A7C15ull + 1;
+    g_perturb_normwise = 0;
+}
+
+/* The same with every component moved by +- rel * max|dx| (seeded signs):
+   a solver whose error is bounded normwise, as an iterative refinement that
+   stops on max|correction| <= rel * max|dx| is. */
+void lo_set_solve_perturbation_normwise(double rel, uint64_t seed) {
+    lo_set_solve_perturbation(rel, seed);
+    g_perturb_normwise = rel > 0;
 }
 
 /* The same for the RKF45 step-size factor: (atol/R)^(1/4) scaled by
@@ -409,13 +419,20 @@ static void lo_trace(const double *v, int n) {
 }
 
 static void lo_perturb(int n, double *dx) {
+    double mx = 0.0;
+    if (g_perturb_normwise)
+        for (int s = 0; s < n; s++)
+            if (fabs(dx[s]) > mx) mx = fabs(dx[s]);
     for (int s = 0; s < n; s++) {
         uint64_t z = g_perturb_state;
         z ^= z << 13;
         z ^= z >> 7;
         z ^= z << 17;
         g_perturb_state = z;
-        dx[s] = dx[s] * ((z & 1) ? 1.0 + g_perturb_rel : 1.0 - g_perturb_rel);
+        if (g_perturb_normwise)
+            dx[s] = dx[s] + ((z & 1) ? g_perturb_rel : -g_perturb_rel) * mx;
+        else
+            dx[s] = dx[s] * ((z & 1) ? 1.0 + g_perturb_rel : 1.0 - g_perturb_rel);
     }
 }
 

@@ -81,6 +81,9 @@ typedef struct {
 /* Tests only: multiply each Newton correction componentwise by (1 +- rel)
    with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
 void lo_set_solve_perturbation(double rel, uint64_t seed);
+/* Tests only: move each Newton correction component by +- rel * max|dx|
+   instead (a normwise-accurate solver); rel = 0 turns it off. */
+void lo_set_solve_perturbation_normwise(double rel, uint64_t seed);
 /* Tests only: scale every RKF45 quarter root (atol/R)^(1/4) by (1 +- rel)
    with seeded signs (rel = 0 turns it off); process-global, not thread safe. */
 void lo_set_root_perturbation(double rel, uint64_t seed);

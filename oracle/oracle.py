@@ -88,6 +88,7 @@ def lib():
             L.lo_lu_factor.restype = C.c_int
             L.lo_lu_solve.argtypes = [C.c_int, _f64p, _i32p, _f64p]
             L.lo_set_solve_perturbation.argtypes = [C.c_double, C.c_uint64]
+            L.lo_set_solve_perturbation_normwise.argtypes = [C.c_double, C.c_uint64]
             L.lo_set_lu_variant.argtypes = [C.c_int]
             L.lo_set_trace.argtypes = [C.c_void_p, C.c_int64]
             L.lo_trace_len.restype = C.c_int64
@@ -309,6 +310,24 @@ class solve_perturbation:
 
     def __enter__(self):
         lib().lo_set_solve_perturbation(self.rel, self.seed)
+        return self
+
+    def __exit__(self, *exc):
+        lib().lo_set_solve_perturbation(0.0, 0)
+        return False
+
+
+class normwise_perturbation:
+    """Context manager: inside it, every oracle Newton correction component
+    moves by +- rel * max|dx| with seeded signs -- a linear solver accurate
+    to rel normwise, as the mixed form's refinement is.  Single-threaded
+    use only."""
+
+    def __init__(self, rel: float, seed: int = 1):
+        self.rel, self.seed = float(rel), int(seed)
+
+    def __enter__(self):
+        lib().lo_set_solve_perturbation_normwise(self.rel, self.seed)
         return self
 
     def __exit__(self, *exc):

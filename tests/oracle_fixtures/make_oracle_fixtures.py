@@ -47,6 +47,24 @@ def c5_full():
 
 
 CASES = {"c3_t002": c3_short, "c3_t05": c3_t05, "c2_full": synth.make_c2, "c5_full": c5_full}
+# cases whose fixture also holds the oracle's spread: the first sample at
+# which any run with a last-bit different solve leaves rtol 1e-6 /
+# atol 1e-9, and the largest excess (FP64 solvers: five one-ulp
+# perturbations and three LU rounding orders; normwise: five runs with
+# corrections moved by 2^-53 max|dx|)
+SPREAD = ("c5_full",)
+
+
+def spread(m, base, runs):
+    first, worst = base.shape[0], 0.0
+    for ctx in runs:
+        with ctx:
+            p, _, _ = O.solve(m)
+        e = np.max(np.abs(p - base) - 1e-9 - 1e-6 * np.abs(base), axis=1)
+        if np.any(e > 0):
+            first = min(first, int(np.argmax(e > 0)))
+        worst = max(worst, float(e.max()))
+    return first, worst
 
 
 def main():
@@ -56,10 +74,17 @@ def main():
         m = make()
         t0 = time.time()
         out, st, rc = O.solve(m)
+        extra = {}
+        if name in SPREAD:
+            f1, w1 = spread(m, out, [O.solve_perturbation(2.0 ** -52, q) for q in range(1, 6)]
+                            + [O.lu_variant(v) for v in (1, 2, 3)])
+            f2, w2 = spread(m, out, [O.normwise_perturbation(2.0 ** -53, q) for q in range(1, 6)])
+            extra = dict(first_divergence=f1, worst_excess=w1, first_divergence_normwise=f2,
+                         worst_excess_normwise=w2)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), t=m.t, out=out, status=rc,
                             be_steps=st["be_steps"], rkf_accepts=st["rkf_accepts"],
                             newton_iters=st["newton_iters"], nan_reverts=st["nan_reverts"],
-                            seconds=time.time() - t0)
+                            seconds=time.time() - t0, **extra)
         print(name, rc, st, "%.1fs" % (time.time() - t0), flush=True)
 
 

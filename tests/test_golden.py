@@ -84,6 +84,7 @@ def spread(m, root="rn"):
 
 def test_fixture_set_complete():
     assert set(cases()) == set(WITHIN_SPREAD) | set(FULL_AGREEMENT)
+    assert len(float_cases()) == len(cases())
 
 
 @pytest.mark.parametrize("name", FULL_AGREEMENT)
@@ -143,3 +144,43 @@ def test_correctly_rounded_quarter_root():
         hi = (Fraction(y) + Fraction(np.nextafter(y, np.inf))) / 2
         assert lo ** 4 < Fraction(float(x)) < hi ** 4, x
     assert L.lo_qroot_rn(0.0) == 0.0 and L.lo_qroot_rn(float("inf")) == float("inf")
+
+
+# ------------------------------------------------ the reference's -p float
+FLOAT_DIR = os.path.join(HERE, "float")
+FRTOL, FATOL = 1e-5, 1e-9
+
+
+def float_cases():
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(FLOAT_DIR, "*.npz")))
+
+
+def fexcess(a, b):
+    return np.max(np.abs(a - b) - FATOL - FRTOL * np.abs(b), axis=1)
+
+
+@pytest.mark.parametrize("name", float_cases())
+def test_float_oracle_against_the_reference_float_mode(name):
+    """The oracle's float restatement (IEEE float division and powf) against
+    the reference's -p float outputs (--use_fast_math division and pow):
+    within the float tolerance before the first sample at which the float
+    oracle's own spread (quarter root or Newton corrections moved by one
+    float ulp) leaves it, and within twice the spread's excess after it."""
+    d = np.load(os.path.join(FLOAT_DIR, name + ".npz"))
+    m = Model(left=d["left"], right=d["right"], k=d["k"], x0=d["x0"], t=d["t"])
+    if d["feed"].size:
+        m.feed = d["feed"]
+    base, st, rc = O.solve(m, precision="float")
+    assert rc == 0
+    first, worst = base.shape[0], 0.0
+    for ctx in ([O.root_perturbation(2.0 ** -23, s) for s in range(1, 6)]
+                + [O.solve_perturbation(2.0 ** -23, s) for s in range(1, 6)]):
+        with ctx:
+            p, _, _ = O.solve(m, precision="float")
+        e = fexcess(p, base)
+        if np.any(e > 0):
+            first = min(first, int(np.argmax(e > 0)))
+        worst = max(worst, float(e.max()))
+    e = fexcess(d["ref"], base)
+    assert np.all(e[:first] <= 0), (first, e)
+    assert e.max() <= 2 * worst, (float(e.max()), worst)

@@ -62,7 +62,8 @@ def test_wide_c3_matches_stored_oracle_trajectory(gpu):
     d = np.load(os.path.join(HERE, "oracle_fixtures", "c3_t002.npz"))
     m = synth.shorten(synth.make_c3(), 0.02, 3)
     assert np.array_equal(m.t, d["t"])
-    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt")
+    # the rank-32 updates on the FP32 pipes (the tensor-core forms below)
+    out, st = solver.simulate(m, engine="mixed", deadline_s=300, root="sqrt", tensor_cores="off")
     assert st["status"] == 0 and int(d["status"]) == 0
     assert within(out, d["out"]), float(np.max(np.abs(out - d["out"]) - RTOL * np.abs(d["out"])))
     assert st["be_steps"] == int(d["be_steps"])
