@@ -39,7 +39,6 @@
 constexpr int kBdfMaxOrder = 5;
 constexpr int kBdfNewtonMaxIter = 4;
 constexpr int kBdfFallback = 4;  // Newton failures in a row before FP64 factors (mixed)
-constexpr int kBdfFp64Steps = 32;  // accepted steps on FP64 factors before FP32 again
 constexpr int kBdfVecs = kBdfMaxOrder + 3 + 12;  // differences + work vectors
 constexpr double kBdfMinFactor = 0.2, kBdfMaxFactor = 10.0;
 constexpr double kBdfEps = 2.220446049250313e-16;  // 2^-52
@@ -201,12 +200,11 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     int q = 1;
     // mixed form: a Newton failure on FP32 factors retries the step on FP64
     // factors at the same size; after kBdfFallback FP32 failures without an
-    // FP32 success in between, the instance factors in FP64 for the next
-    // kBdfFp64Steps accepted steps, each further stretch twice as long (the
-    // workspace has FP64 room; the FP32 panel buffers are as large as the
-    // FP64 ones, the solve vector is res)
+    // FP32 success in between, the instance factors in FP64 for the rest of
+    // its integration (the workspace has FP64 room; the FP32 panel buffers
+    // are as large as the FP64 ones, the solve vector is res)
     bool fp64_lu = !kMixed;
-    int fail_run = 0, fp64_left = 0, fp64_stretch = kBdfFp64Steps;
+    int fail_run = 0, fp64_left = 0;
     double h = 0.0;
     int64_t attempts = 0, rhs_evals = 0, jac_evals = 0;
     if (isample < nt) {
@@ -445,9 +443,8 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                         // success in between, a longer FP64 stretch
                         fp64_lu = true;
                         if (++fail_run >= kBdfFallback) {
-                            fp64_left = fp64_stretch;
-                            fp64_stretch = min(2 * fp64_stretch, 1 << 20);
-                            if (tid == 0) st.nan_reverts++;  // counts the stretches
+                            fp64_left = 1 << 30;  // FP64 factors from here on
+                            if (tid == 0) st.nan_reverts++;  // counts the switch
                         } else {
                             fp64_left = 1;
                         }

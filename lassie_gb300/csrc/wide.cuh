@@ -25,11 +25,18 @@
 
 constexpr int kWPB = 32;   // Gauss-Jordan panel width
 constexpr int kWT = 128;   // rank-update tile: kWT rows x kWT columns per CTA pass
+// Super-panel: kWSP columns (kWSP / kWPB panels) are eliminated within
+// their own columns first; the rest of the matrix then takes one rank-kWSP
+// update instead of kWSP / kWPB rank-kWPB ones, so it is read and written
+// once per kWSP columns.  One column tile wide.
+constexpr int kWSP = 128;
+static_assert(kWSP == kWT && kWSP % kWPB == 0, "a super-panel is one column tile");
 
 enum WideTask : int { kTaskExit = 0, kTaskAssemble = 1, kTaskPanel = 2, kTaskUpdate = 3,
                       kTaskMatvec = 4, kTaskRates = 5, kTaskRkf = 6, kTaskRkfFinal = 7,
                       kTaskSolve = 8, kTaskSolveUpdate = 9, kTaskJv = 10, kTaskResidual = 11,
-                      kTaskNewtonRhs = 12 };
+                      kTaskNewtonRhs = 12, kTaskPivotLevel = 13, kTaskPanelS = 14,
+                      kTaskUpdateS = 15 };
 
 // Most CTAs of one wide launch (per-CTA partial results of the RKF45 error).
 constexpr int kWideMaxGrid = 256;
@@ -41,7 +48,7 @@ struct WideCtl {
     int abort;          // a wait ran out of time
     int task;
     int j0, pb;         // current panel
-    int pad0, pad1;
+    int pad0, pad1;     // pivot level: candidates, source list; panel/update: super-panel start
     double h;           // step of the matrix being assembled (RKF45: the step)
     const double *x;    // state the Jacobian (or the RHS) is evaluated at
     Vecs vecs;          // the leader's current RKF45 vectors (and Newton aliases)
@@ -61,10 +68,13 @@ struct WideWs {
     int *piv;         // [N] pivot row of each column
     int *pos;         // [N] position of a row among the current panel's pivots, or -1
     int *used;        // [N] 1 once a row has been a pivot (fresh pivot search)
-    LT *PN;           // [kWPB][N] panel copy for the pivot search (column-major)
+    LT *PN;           // [kWPB][N] scratch; its first 2N ints are the pivot candidate lists
+    int *cand;        // [2][N] candidate rows of the pivot search (two lists, alternating)
     LT *Dinv;         // [kWPB][kWPB]
     LT *PR;           // [kWPB][ld]
     LT *AJ;           // [N][kWPB] panel columns before the update
+    LT *AJS;          // [N][kWSP] super-panel columns before its panels
+    LT *PRS;          // [kWSP][ld] DS^-1 * M[P_S, :] (DS: the super-panel's pivot block)
     LT *vin, *vout;   // [N] matrix-vector product input (gathered) and output
     int *flags;       // [0]: pivot order valid (set by the leader)
     long long *part;  // [2][kWideMaxGrid]: per-CTA RKF45 accept flag, min delta bits
@@ -77,7 +87,8 @@ struct WideWs {
 };
 
 struct WideLayout {
-    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJ, vin, vout, flags, part, total;
+    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJ, AJS, PRS, vin, vout, flags, part,
+        total;
     __host__ __device__ static int64_t al(int64_t v) { return (v + 255) & ~int64_t(255); }
     __host__ __device__ WideLayout(int N, int R, int nnz_a, int lt) {
         const int64_t ld = (N + 3) & ~3;
@@ -94,6 +105,8 @@ struct WideLayout {
         Dinv = o;  o = al(o + int64_t(kWPB) * kWPB * lt);
         PR = o;    o = al(o + int64_t(kWPB) * ld * lt);
         AJ = o;    o = al(o + int64_t(N) * kWPB * lt);
+        AJS = o;   o = al(o + int64_t(N) * kWSP * lt);
+        PRS = o;   o = al(o + int64_t(kWSP) * ld * lt);
         vin = o;   o = al(o + int64_t(N) * lt);
         vout = o;  o = al(o + int64_t(N) * lt);
         flags = o; o = al(o + 16);
@@ -115,9 +128,12 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
     W.pos = reinterpret_cast<int *>(base + L.pos);
     W.used = reinterpret_cast<int *>(base + L.used);
     W.PN = reinterpret_cast<LT *>(base + L.PN);
+    W.cand = reinterpret_cast<int *>(base + L.PN);
     W.Dinv = reinterpret_cast<LT *>(base + L.Dinv);
     W.PR = reinterpret_cast<LT *>(base + L.PR);
     W.AJ = reinterpret_cast<LT *>(base + L.AJ);
+    W.AJS = reinterpret_cast<LT *>(base + L.AJS);
+    W.PRS = reinterpret_cast<LT *>(base + L.PRS);
     W.vin = reinterpret_cast<LT *>(base + L.vin);
     W.vout = reinterpret_cast<LT *>(base + L.vout);
     W.flags = reinterpret_cast<int *>(base + L.flags);
@@ -131,13 +147,27 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
     return W;
 }
 
-// Dynamic shared memory of the wide kernel: the rank-update tiles, or the
-// matrix-vector input, whichever is larger, plus the pivot-block inverse.
+// Pivot search: candidate rows one CTA chooses from at once (their panel
+// values in shared memory), and the rows per group of a tournament level.
+__host__ __device__ constexpr int tour_max(int lt) { return lt == 4 ? 1024 : 512; }
+constexpr int kTourGroup = 128;
+__host__ __device__ constexpr int64_t tour_smem_bytes(int lt) {
+    return int64_t(tour_max(lt)) * (kWPB + 1) * lt + int64_t(tour_max(lt)) * 4 +
+           int64_t(2) * kWarps * (lt + 4);
+}
+
+// Dynamic shared memory of the wide kernel: the rank-update tiles, the
+// matrix-vector input or the pivot search's candidates, whichever is
+// largest, plus the pivot-block inverse.
 __host__ __device__ inline int64_t wide_smem_bytes(int N, int lt) {
     int64_t tiles = (int64_t(kWPB) * (kWT + 4) + int64_t(kWPB) * kWT) * lt;
     if (lt == 4 && tiles < 4 * kWT * kWPB * 4) tiles = 4 * kWT * kWPB * 4;  // tensor-core operands
     const int64_t vin = int64_t((N + 3) & ~3) * lt;
-    return (tiles > vin ? tiles : vin) + int64_t(kWPB) * kWPB * lt;
+    int64_t big = tiles > vin ? tiles : vin;
+    if (big < tour_smem_bytes(lt)) big = tour_smem_bytes(lt);
+    const int64_t ds = int64_t(kWSP) * kWSP * lt + kWSP * 4;  // task_panel_s
+    if (big < ds) big = ds;
+    return big + int64_t(kWPB) * kWPB * lt;
 }
 
 // ---------------------------------------------------------------- sync
@@ -236,18 +266,20 @@ __device__ void task_assemble(const WideWs<LT> &W, const Net &m, const double *x
     }
 }
 
-// PR = D^-1 * M[P_J, :] and the snapshot AJ = M[:, J], spread over every
-// thread of the grid: PR by (group of 4 pivot rows, column), AJ by (row,
-// 4 panel columns).
+// PR = D^-1 * M[P_J, C] for the columns C of the super-panel's tile (s0 ..)
+// and the snapshot AJ = M[:, J], spread over every thread of the grid: PR by
+// (group of 4 pivot rows, column), AJ by (row, 4 panel columns).  The
+// super-panel's first panel also takes the snapshot AJS = M[:, S].
 template <typename LT>
-__device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD) {
+__device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD, int s0) {
     const int tid = threadIdx.x;
     for (int q = tid; q < kWPB * kWPB; q += kThreads) sD[q] = W.Dinv[q];
     __syncthreads();
     const int N = W.N, ld = W.ld;
+    const int cw = min(s0 + kWSP, ld) - s0;
     const int gt = blockIdx.x * kThreads + tid, nt = gridDim.x * kThreads;
-    for (int q = gt; q < (kWPB / 4) * ld; q += nt) {
-        const int g = q / ld, c = q - g * ld;
+    for (int q = gt; q < (kWPB / 4) * cw; q += nt) {
+        const int g = q / cw, c = s0 + (q - g * cw);
         if (c >= j0 && c < j0 + kWPB) continue;
         LT a[kWPB];
 #pragma unroll
@@ -273,22 +305,37 @@ __device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD) {
         }
         store4(W.AJ + (int64_t)i * kWPB + k4, v);
     }
+    if (j0 == s0) {
+        const int sw = min(kWSP, N - s0);
+        for (int q = gt; q < N * (kWSP / 4); q += nt) {
+            const int i = q / (kWSP / 4), k4 = (q - i * (kWSP / 4)) * 4;
+            const LT *src = W.A + (int64_t)i * ld + s0 + k4;
+            LT v[4];
+            if (k4 + 4 <= sw) {
+                load4(src, v);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 4; b++) v[b] = (k4 + b < sw) ? src[b] : LT(0);
+            }
+            store4(W.AJS + (int64_t)i * kWSP + k4, v);
+        }
+    }
 }
 
-// The rank-kWPB update of every row and column, in kWT x kWT tiles; thread
-// (ty, tx) owns rows ty*8.. and columns tx*4.. of a tile.  Columns in J start
-// from 0 and use D^-1 in place of PR; the current panel's pivot rows take
-// their new values (PR, D^-1) directly.
+// The rank-kWPB update of every row in the super-panel's column tile, in
+// kWT x kWT tiles; thread (ty, tx) owns rows ty*8.. and columns tx*4.. of a
+// tile.  Columns in J start from 0 and use D^-1 in place of PR; the current
+// panel's pivot rows take their new values (PR, D^-1) directly.
 template <typename LT>
-__device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
+__device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s0) {
     constexpr int AS = kWT + 4;           // sAJ row stride (16-byte rows)
     LT *sAJ = smem;                       // [kWPB][AS]: panel columns, column-major
     LT *sB = smem + kWPB * AS;            // [kWPB][kWT]
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const int N = W.N, ld = W.ld;
-    const int nrt = (N + kWT - 1) / kWT, nct = (ld + kWT - 1) / kWT;
-    for (int t = blockIdx.x; t < nrt * nct; t += gridDim.x) {
-        const int r0 = (t / nct) * kWT, c0 = (t % nct) * kWT;
+    const int nrt = (N + kWT - 1) / kWT;
+    for (int t = blockIdx.x; t < nrt; t += gridDim.x) {
+        const int r0 = t * kWT, c0 = s0;  // the super-panel's column tile
         __syncthreads();
         for (int q = tid; q < kWT * kWPB; q += kThreads) {
             const int r = q / kWPB, k = q - r * kWPB;
@@ -350,17 +397,17 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem) {
 // then set).
 // W.tc_on == 2: the BF16 form (operands rounded to BF16, one kind::f16 MMA
 // per 16-wide K step, FP32 accumulation).
-__device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *smem) {
+__device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *smem, int s0) {
     float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
     uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
     const bool bf16 = W.tc_on == 2;
     const int tid = threadIdx.x;
     const int N = W.N, ld = W.ld;
-    const int nrt = (N + kTcM - 1) / kTcM, nct = (ld + kTcN - 1) / kTcN;
+    const int nrt = (N + kTcM - 1) / kTcM;
     uint32_t phase = *W.tc_phase;
     bool ok = true;
-    for (int t = blockIdx.x; t < nrt * nct && ok; t += gridDim.x) {
-        const int r0 = (t / nct) * kTcM, c0 = (t % nct) * kTcN;
+    for (int t = blockIdx.x; t < nrt && ok; t += gridDim.x) {
+        const int r0 = t * kTcM, c0 = s0;  // the super-panel's column tile
         __syncthreads();
         if (bf16) {
             // A: 128 rows x 32, B: kTcN columns x 32, 4 elements per thread
@@ -458,6 +505,227 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
                     } else {
                         load4(dst + c, v);
                     }
+#pragma unroll
+                    for (int b = 0; b < 4; b++) v[b] -= out[4 * g + b];
+                }
+                store4(dst + c, v);
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        *W.tc_phase = phase;
+        if (!ok) atomicExch(&W.ctl->abort, 1);
+    }
+    __syncthreads();
+    return ok;
+}
+
+// ---------------------------------------------------------------- super-panel
+//
+// After the panels of super-panel S (columns s0 .. s0+sw-1, pivot rows P_S)
+// have been eliminated within S's column tile, the columns of S hold the
+// in-place inverse of its block, X[P_S[r]][s0 + k] = DS^-1[r][k] with
+// DS[k][r] = M[P_S[k]][s0 + r] before S; every other column C then takes
+//     PRS = DS^-1 * M[P_S, C],   M[i, C] -= AJS[i, :] * PRS   (i not in P_S),
+//     M[P_S, C] = PRS,
+// the same matrix the panels' rank-kWPB updates would give, in one pass.
+
+// PRS over the columns outside S's tile (rows >= sw zero): DS^-1 and P_S
+// staged in shared memory, by (group of 8 rows, column) over the grid.
+template <typename LT>
+__device__ void task_panel_s(const WideWs<LT> &W, int s0, int sw, LT *smem) {
+    constexpr int RG = 8, KC = 16;
+    LT *sDS = smem;                                               // [kWSP][kWSP]
+    int *spiv = reinterpret_cast<int *>(sDS + kWSP * kWSP);       // [kWSP]
+    const int tid = threadIdx.x, N = W.N, ld = W.ld;
+    (void)N;
+    for (int q = tid; q < kWSP; q += kThreads) spiv[q] = q < sw ? W.piv[s0 + q] : 0;
+    __syncthreads();
+    for (int q = tid; q < kWSP * kWSP; q += kThreads) {
+        const int r = q / kWSP, k = q - r * kWSP;
+        sDS[q] = (r < sw && k < sw) ? W.A[(int64_t)spiv[r] * ld + s0 + k] : LT(0);
+    }
+    __syncthreads();
+    const int tw = min(s0 + kWSP, ld) - s0, cw = ld - tw;  // columns outside the tile
+    const int gt = blockIdx.x * kThreads + tid, nt = gridDim.x * kThreads;
+    for (int q = gt; q < (kWSP / RG) * cw; q += nt) {
+        const int g = q / cw, cc = q - g * cw;
+        const int c = cc < s0 ? cc : cc + tw;
+        LT acc[RG];
+#pragma unroll
+        for (int r = 0; r < RG; r++) acc[r] = LT(0);
+        if (g * RG < sw) {
+            for (int k0 = 0; k0 < sw; k0 += KC) {
+                LT b[KC];
+#pragma unroll
+                for (int k = 0; k < KC; k++)
+                    b[k] = (k0 + k < sw) ? W.A[(int64_t)spiv[k0 + k] * ld + c] : LT(0);
+#pragma unroll
+                for (int r = 0; r < RG; r++)
+#pragma unroll
+                    for (int k = 0; k < KC; k++)
+                        acc[r] = lt_fma(sDS[(g * RG + r) * kWSP + k0 + k], b[k], acc[r]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RG; r++) W.PRS[(int64_t)(g * RG + r) * ld + c] = acc[r];
+    }
+}
+
+// The rank-kWSP update of every column tile but S's, on the FP32 (or FP64)
+// pipes: task_update's tiles with K in chunks of kWPB.
+template <typename LT>
+__device__ void task_update_s(const WideWs<LT> &W, int s0, int sw, LT *smem) {
+    constexpr int AS = kWT + 4;
+    LT *sAJ = smem;                       // [kWPB][AS]
+    LT *sB = smem + kWPB * AS;            // [kWPB][kWT]
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int N = W.N, ld = W.ld;
+    const int nrt = (N + kWT - 1) / kWT, nct = (ld + kWT - 1) / kWT, st = s0 / kWT;
+    if (nct < 2) return;
+    for (int t = blockIdx.x; t < nrt * (nct - 1); t += gridDim.x) {
+        const int ct = t % (nct - 1);
+        const int r0 = (t / (nct - 1)) * kWT, c0 = (ct < st ? ct : ct + 1) * kWT;
+        const int col = c0 + tx * 4, rl0 = ty * 8;
+        const bool live = col < ld;
+        LT acc[8][4];
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            const int row = r0 + rl0 + a;
+            if (live && row < N && W.pos[row] < 0) {
+                load4(W.A + (int64_t)row * ld + col, acc[a]);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
+            }
+        }
+        for (int k0 = 0; k0 < sw; k0 += kWPB) {
+            __syncthreads();
+            for (int q = tid; q < kWT * kWPB; q += kThreads) {
+                const int r = q / kWPB, k = q - r * kWPB;
+                sAJ[k * AS + r] = (r0 + r < N) ? W.AJS[(int64_t)(r0 + r) * kWSP + k0 + k] : LT(0);
+            }
+            for (int q = tid; q < kWPB * kWT; q += kThreads) {
+                const int k = q / kWT, cc = q - k * kWT;
+                const int c = c0 + cc;
+                sB[q] = (c < ld) ? W.PRS[(int64_t)(k0 + k) * ld + c] : LT(0);
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int k = 0; k < kWPB; k++) {
+                LT av[8], bv[4];
+                load8(sAJ + k * AS + rl0, av);
+                load4(sB + k * kWT + tx * 4, bv);
+#pragma unroll
+                for (int a = 0; a < 8; a++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[a][b] = lt_fma(-av[a], bv[b], acc[a][b]);
+            }
+        }
+        if (!live) continue;
+#pragma unroll
+        for (int a = 0; a < 8; a++) {
+            const int row = r0 + rl0 + a;
+            if (row >= N) break;
+            const int pr = W.pos[row];
+            if (pr >= 0) load4(W.PRS + (int64_t)pr * ld + col, acc[a]);
+            store4(W.A + (int64_t)row * ld + col, acc[a]);
+        }
+    }
+}
+
+// task_update_s on the tensor cores: per 128 x 128 tile, K chunks of kTcK
+// staged as task_update_tc stages its operands (A from AJS, B from PRS),
+// accumulated in tensor memory, read back once.  False if a tensor-core wait
+// ran out (the control block's abort flag is then set).
+__device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *smem) {
+    float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
+    uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
+    const bool bf16 = W.tc_on == 2;
+    const int tid = threadIdx.x;
+    const int N = W.N, ld = W.ld;
+    const int nrt = (N + kTcM - 1) / kTcM, nct = (ld + kTcN - 1) / kTcN, st = s0 / kTcN;
+    uint32_t phase = *W.tc_phase;
+    bool ok = true;
+    for (int t = blockIdx.x; nct > 1 && t < nrt * (nct - 1) && ok; t += gridDim.x) {
+        const int ct = t % (nct - 1);
+        const int r0 = (t / (nct - 1)) * kTcM, c0 = (ct < st ? ct : ct + 1) * kTcN;
+        for (int k0 = 0; k0 < sw && ok; k0 += kTcK) {
+            if (bf16) {
+                for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
+                    const int r = q >> 3, k4 = (q & 7) * 4;
+                    float v[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (r0 + r < N) load4(W.AJS + (int64_t)(r0 + r) * kWSP + k0 + k4, v);
+                    uint2 pk;
+                    pk.x = (uint32_t)bf16_bits(v[0]) | ((uint32_t)bf16_bits(v[1]) << 16);
+                    pk.y = (uint32_t)bf16_bits(v[2]) | ((uint32_t)bf16_bits(v[3]) << 16);
+                    *reinterpret_cast<uint2 *>(sA16 + tc_off16(r, k4) / 2) = pk;
+                }
+                for (int q = tid; q < kTcN * (kTcK / 4); q += kThreads) {
+                    const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
+                    const int c = c0 + n;
+                    uint16_t h[4];
+#pragma unroll
+                    for (int b = 0; b < 4; b++)
+                        h[b] = bf16_bits(c < ld ? W.PRS[(int64_t)(k0 + k4 + b) * ld + c] : 0.f);
+                    uint2 pk;
+                    pk.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+                    pk.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
+                    *reinterpret_cast<uint2 *>(sB16 + tc_off16(n, k4) / 2) = pk;
+                }
+            } else {
+                for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
+                    const int r = q >> 3, k4 = (q & 7) * 4;
+                    float v[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (r0 + r < N) load4(W.AJS + (int64_t)(r0 + r) * kWSP + k0 + k4, v);
+                    float h[4], l[4];
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        h[b] = tf32_hi(v[b]);
+                        l[b] = v[b] - h[b];
+                    }
+                    const int o = tc_off(r, k4) / 4;
+                    store4(sAh + o, h);
+                    store4(sAl + o, l);
+                }
+                for (int q = tid; q < kTcN * (kTcK / 4); q += kThreads) {
+                    const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
+                    const int c = c0 + n;
+                    float h[4], l[4];
+#pragma unroll
+                    for (int b = 0; b < 4; b++) {
+                        const float x = c < ld ? W.PRS[(int64_t)(k0 + k4 + b) * ld + c] : 0.f;
+                        h[b] = tf32_hi(x);
+                        l[b] = x - h[b];
+                    }
+                    const int o = tc_off(n, k4) / 4;
+                    store4(sBh + o, h);
+                    store4(sBl + o, l);
+                }
+            }
+            tc_proxy_fence();
+            __syncthreads();
+            ok = bf16 ? tc_chunk_mma_bf16(sA16, sB16, W.tc_bar, W.tc_tmem, phase, k0 > 0)
+                      : tc_chunk_mma(sAh, sAl, sBh, sBl, W.tc_bar, W.tc_tmem, phase, k0 > 0);
+        }
+        if (!ok) break;
+        float out[32];
+        tc_tile_read(W.tc_tmem, out);
+        const int w = tid >> 5;
+        const int row = r0 + (w & 3) * 32 + (tid & 31), cb = c0 + (w >> 2) * 32;
+        if (row < N && cb < ld) {
+            const int pr = W.pos[row];
+            float *dst = W.A + (int64_t)row * ld;
+#pragma unroll
+            for (int g = 0; g < 8; g++) {
+                const int c = cb + 4 * g;
+                if (c >= ld) break;
+                float v[4];
+                if (pr >= 0) {
+                    load4(W.PRS + (int64_t)pr * ld + c, v);
+                } else {
+                    load4(dst + c, v);
 #pragma unroll
                     for (int b = 0; b < 4; b++) v[b] -= out[4 * g + b];
                 }
@@ -628,6 +896,154 @@ __device__ void task_residual(long long *part, const Net &m, const Vecs &V, doub
     if (threadIdx.x == 0) part[blockIdx.x] = __double_as_longlong(rm);
 }
 
+// ---------------------------------------------------------------- pivot search
+//
+// Partial pivoting chooses each panel column's pivot among all rows not yet
+// used, which makes a leader-only pass over the whole panel per column.
+// With more candidates than one CTA holds in shared memory (tour_max), the
+// search is a tournament: every CTA runs partial pivoting on groups of
+// kTourGroup candidates and keeps each group's chosen rows, until the
+// survivors fit the leader, which runs partial pivoting on their panel rows.
+// The chosen rows of a group span the group's panel rows, so the survivors
+// keep the panel's rank; with at most tour_max candidates the choice is
+// plain partial pivoting.
+
+// Ordered compaction by the whole CTA: writes the kept entries of 0..n-1 to
+// out in order -- with in == nullptr row i where used[i] == 0, otherwise
+// in[i] where in[i] >= 0 -- and returns their count (uniform).
+__device__ int cta_compact(const int *in, const int *used, int n, int *out) {
+    __shared__ int sscan[kWarps];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int chunk = (n + kThreads - 1) / kThreads;
+    const int b = min(n, tid * chunk), e = min(n, b + chunk);
+    auto keep = [&](int i) { return in ? in[i] >= 0 : used[i] == 0; };
+    int cnt = 0;
+    for (int i = b; i < e; i++) cnt += keep(i) ? 1 : 0;
+    int x = cnt;  // inclusive scan over the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sscan[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < kWarps ? sscan[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < kWarps) sscan[lane] = w;
+    }
+    __syncthreads();
+    int off = x - cnt + (warp > 0 ? sscan[warp - 1] : 0);
+    for (int i = b; i < e; i++)
+        if (keep(i)) out[off++] = in ? in[i] : i;
+    const int total = sscan[kWarps - 1];
+    __syncthreads();
+    return total;
+}
+
+// Partial pivoting restricted to the C candidate rows rows[0..C)
+// (C <= tour_max): their values in the panel columns j0 .. j0+pb-1 are
+// staged in shared memory; per column the candidate not chosen yet with the
+// largest |value| (ties to the earlier candidate, NaN never wins) becomes
+// the next pivot and the column is eliminated from the others.  sel[k]
+// (shared) = the k-th chosen row; returns how many were chosen (uniform),
+// fewer than pb only when a column has no nonzero candidate left.
+template <typename LT>
+__device__ int cta_select(const WideWs<LT> &W, const int *rows, int C, int j0, int pb,
+                          unsigned char *smem, int *sel) {
+    static_assert(kWPB == 32 && kThreads * 2 >= 1024, "one panel row per 32 lanes, 2 rows a thread");
+    constexpr int SP = kWPB + 1;  // row stride: lanes on consecutive rows hit distinct banks
+    constexpr int RPT = 2;        // candidates per thread
+    const int tmax = tour_max((int)sizeof(LT));
+    LT *sp = reinterpret_cast<LT *>(smem);
+    int *srow = reinterpret_cast<int *>(sp + (int64_t)tmax * SP);
+    LT *sv = reinterpret_cast<LT *>(srow + tmax);
+    int *si = reinterpret_cast<int *>(sv + 2 * kWarps);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ld = W.ld;
+    for (int q = tid; q < C * kWPB; q += kThreads) {
+        const int r = q >> 5, c = q & 31;
+        const int row = rows[r];
+        if (c == 0) srow[r] = row;
+        sp[r * SP + c] = c < pb ? W.A[(int64_t)row * ld + j0 + c] : LT(0);
+    }
+    __syncthreads();
+    bool alive[RPT];
+#pragma unroll
+    for (int i = 0; i < RPT; i++) alive[i] = tid + i * kThreads < C;
+    int n = 0;
+    for (int k = 0; k < pb; k++) {
+        PivT<LT> best{LT(-1), 1 << 30};
+#pragma unroll
+        for (int i = 0; i < RPT; i++) {
+            const int r = tid + i * kThreads;
+            if (!alive[i]) continue;
+            const LT v = fabs(sp[r * SP + k]);
+            if (!isnan(v)) best = piv_better(best, PivT<LT>{v, r});
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            PivT<LT> other{__shfl_xor_sync(0xffffffffu, best.v, o),
+                           __shfl_xor_sync(0xffffffffu, best.i, o)};
+            best = piv_better(best, other);
+        }
+        // per-warp results in alternating slots: one barrier per column
+        const int b = (k & 1) * kWarps;
+        if (lane == 0) {
+            sv[b + warp] = best.v;
+            si[b + warp] = best.i;
+        }
+        __syncthreads();
+        PivT<LT> all{LT(-1), 1 << 30};
+        if (lane < kWarps) all = PivT<LT>{sv[b + lane], si[b + lane]};
+        for (int o = kWarps / 2; o > 0; o >>= 1) {
+            PivT<LT> other{__shfl_xor_sync(0xffffffffu, all.v, o),
+                           __shfl_xor_sync(0xffffffffu, all.i, o)};
+            all = piv_better(all, other);
+        }
+        const int p = __shfl_sync(0xffffffffu, all.i, 0);
+        const LT pv = __shfl_sync(0xffffffffu, all.v, 0);
+        if (p >= C || !(pv > LT(0))) break;  // uniform
+        if (tid == 0) sel[k] = srow[p];
+        n = k + 1;
+        // the pivot row was last written before this column's barrier
+        const LT rd = LT(1) / sp[p * SP + k];
+#pragma unroll
+        for (int i = 0; i < RPT; i++) {
+            const int r = tid + i * kThreads;
+            if (!alive[i]) continue;
+            if (r == p) {
+                alive[i] = false;
+                continue;
+            }
+            const LT l = sp[r * SP + k] * rd;
+            for (int c = k + 1; c < pb; c++)
+                sp[r * SP + c] = lt_fma(-l, sp[p * SP + c], sp[r * SP + c]);
+        }
+    }
+    __syncthreads();
+    return n;
+}
+
+// One tournament level: the C candidates of list `src` in groups of
+// kTourGroup, each group's chosen rows (kWPB slots, -1 for none) into the
+// other list at 32 * group.
+template <typename LT>
+__device__ void task_pivot_level(const WideWs<LT> &W, int j0, int pb, int C, int src,
+                                 unsigned char *smem) {
+    __shared__ int sel[kWPB];
+    const int *in = W.cand + (int64_t)src * W.N;
+    int *out = W.cand + (int64_t)(src ^ 1) * W.N;
+    const int ng = (C + kTourGroup - 1) / kTourGroup;
+    for (int g = blockIdx.x; g < ng; g += gridDim.x) {
+        const int c = min(kTourGroup, C - g * kTourGroup);
+        const int n = cta_select<LT>(W, in + (int64_t)g * kTourGroup, c, j0, pb, smem, sel);
+        if (threadIdx.x < kWPB) out[g * kWPB + threadIdx.x] = (int)threadIdx.x < n ? sel[threadIdx.x] : -1;
+        __syncthreads();
+    }
+}
+
 // Worker CTA: serve tasks until the leader sends kTaskExit (or a wait runs
 // out of time).
 template <typename LT>
@@ -656,17 +1072,30 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
         gen++;
         switch (s_task) {
         case kTaskAssemble: task_assemble<LT>(W, m, s_x, s_h, mdiag); break;
-        case kTaskPanel: task_panel<LT>(W, s_j0, s_pb, sD); break;
+        case kTaskPanel: task_panel<LT>(W, s_j0, s_pb, sD, W.ctl->pad0); break;
         case kTaskUpdate:
             if constexpr (std::is_same<LT, float>::value) {
                 if (W.tc_on) {
-                    task_update_tc(W, s_j0, s_pb, sm);
+                    task_update_tc(W, s_j0, s_pb, sm, W.ctl->pad0);
                     break;
                 }
             }
-            task_update<LT>(W, s_j0, s_pb, sm);
+            task_update<LT>(W, s_j0, s_pb, sm, W.ctl->pad0);
+            break;
+        case kTaskPanelS: task_panel_s<LT>(W, s_j0, s_pb, sm); break;
+        case kTaskUpdateS:
+            if constexpr (std::is_same<LT, float>::value) {
+                if (W.tc_on) {
+                    task_update_s_tc(W, s_j0, s_pb, sm);
+                    break;
+                }
+            }
+            task_update_s<LT>(W, s_j0, s_pb, sm);
             break;
         case kTaskMatvec: task_matvec<LT>(W, sm); break;
+        case kTaskPivotLevel:
+            task_pivot_level<LT>(W, s_j0, s_pb, W.ctl->pad0, W.ctl->pad1, smem);
+            break;
         case kTaskRates: task_rates(m, s_x, W.pw, W.qr); break;
         case kTaskSolve: {
             const Vecs v = W.ctl->vecs;
@@ -758,65 +1187,37 @@ __device__ bool wide_pivot_block(const WideWs<LT> &W, int j0, int pb, LT *scratc
     return cta_block_inverse<LT>(scratch, kWPB, pb, W.Dinv, scratch + kWPB * kWPB);
 }
 
-// Leader: partial-pivoting choice of the panel's pivot rows among the rows
-// not yet used, on a copy of the panel (the LU panel factorisation restricted
-// to the candidate rows).  Ties go to the smaller row, NaN never wins.  False
-// if a column has no nonzero candidate.
+// Leader: the panel's pivot rows among the rows not used yet (the
+// tournament above when they outnumber tour_max), into piv[j0..] with
+// used[] set.  0: done; 1: a column has no nonzero candidate (singular);
+// 2: a wait ran out of time.
 template <typename LT>
-__device__ bool wide_select_pivots(const WideWs<LT> &W, int j0, int pb, double *red, int *ired,
-                                   LT *prow) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int N = W.N, ld = W.ld;
-    for (int i = tid; i < N; i += kThreads) {
-        if (W.used[i]) continue;
-        const LT *src = W.A + (int64_t)i * ld + j0;
-        for (int k = 0; k < pb; k++) W.PN[(int64_t)k * N + i] = src[k];
+__device__ int wide_select_pivots(const WideWs<LT> &W, int j0, int pb, unsigned char *smem,
+                                  uint64_t limit, int *sflag) {
+    __shared__ int sel[kWPB];
+    const int N = W.N;
+    int C = cta_compact(nullptr, W.used, N, W.cand);
+    int src = 0;
+    while (C > tour_max((int)sizeof(LT))) {
+        if (threadIdx.x == 0) {
+            W.ctl->pad0 = C;
+            W.ctl->pad1 = src;
+        }
+        wide_fork<LT>(W, kTaskPivotLevel, j0, pb, 0.0, nullptr);
+        task_pivot_level<LT>(W, j0, pb, C, src, smem);
+        if (!wide_join<LT>(W, limit, sflag)) return 2;
+        const int ng = (C + kTourGroup - 1) / kTourGroup;
+        C = cta_compact(W.cand + (int64_t)(src ^ 1) * N, nullptr, ng * kWPB,
+                        W.cand + (int64_t)src * N);
+    }
+    const int n = cta_select<LT>(W, W.cand + (int64_t)src * N, C, j0, pb, smem, sel);
+    if (n < pb) return 1;
+    if (threadIdx.x < pb) {
+        W.piv[j0 + threadIdx.x] = sel[threadIdx.x];
+        W.used[sel[threadIdx.x]] = 1;
     }
     __syncthreads();
-    for (int k = 0; k < pb; k++) {
-        PivT<LT> best{LT(-1), 1 << 30};
-        for (int i = tid; i < N; i += kThreads) {
-            if (W.used[i]) continue;
-            const LT v = fabs(W.PN[(int64_t)k * N + i]);
-            if (!isnan(v)) best = piv_better(best, PivT<LT>{v, i});
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            PivT<LT> other{__shfl_xor_sync(0xffffffffu, best.v, o),
-                           __shfl_xor_sync(0xffffffffu, best.i, o)};
-            best = piv_better(best, other);
-        }
-        LT *redv = reinterpret_cast<LT *>(red);
-        if (lane == 0) {
-            redv[warp] = best.v;
-            ired[warp] = best.i;
-        }
-        __syncthreads();
-        PivT<LT> all{LT(-1), 1 << 30};
-        if (lane < kWarps) all = PivT<LT>{redv[lane], ired[lane]};
-        for (int o = kWarps / 2; o > 0; o >>= 1) {
-            PivT<LT> other{__shfl_xor_sync(0xffffffffu, all.v, o),
-                           __shfl_xor_sync(0xffffffffu, all.i, o)};
-            all = piv_better(all, other);
-        }
-        const int p = __shfl_sync(0xffffffffu, all.i, 0);
-        const LT pv = __shfl_sync(0xffffffffu, all.v, 0);
-        if (p >= N || !(pv > LT(0))) return false;  // uniform
-        if (tid < kWPB) prow[tid] = (tid < pb) ? W.PN[(int64_t)tid * N + p] : LT(0);
-        __syncthreads();
-        if (tid == 0) {
-            W.piv[j0 + k] = p;
-            W.used[p] = 1;
-        }
-        const LT rd = LT(1) / prow[k];
-        for (int i = tid; i < N; i += kThreads) {
-            if (W.used[i] || i == p) continue;
-            const LT l = W.PN[(int64_t)k * N + i] * rd;
-            for (int c = k + 1; c < pb; c++)
-                W.PN[(int64_t)c * N + i] = lt_fma(-l, prow[c], W.PN[(int64_t)c * N + i]);
-        }
-        __syncthreads();
-    }
-    return true;
+    return 0;
 }
 
 // Leader: assemble M = I - h*J(x) on all CTAs and invert it in place.
@@ -851,38 +1252,74 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
         }
         __syncthreads();
         bool ok = true;
-        for (int j0 = 0; j0 < N; j0 += kWPB) {
-            const int pb = min(kWPB, N - j0);
-            if (!use_old && !wide_select_pivots<LT>(W, j0, pb, red, ired, sD)) {
-                if (tid == 0) W.flags[0] = 0;
-                __syncthreads();
-                return 1;
-            }
-            __syncthreads();
-            tick(0);
-            if (j0 > 0 && tid < kWPB) W.pos[W.piv[j0 - kWPB + tid]] = -1;
-            __syncthreads();
-            if (tid < pb) W.pos[W.piv[j0 + tid]] = tid;
-            if (!wide_pivot_block<LT>(W, j0, pb, sm)) {
-                ok = false;
-                break;
-            }
-            tick(0);
-            wide_fork<LT>(W, kTaskPanel, j0, pb, h, x);
-            task_panel<LT>(W, j0, pb, sD);
-            if (!wide_join<LT>(W, limit, sflag)) return 2;
-            tick(1);
-            wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
-            bool tc_done = false;
-            if constexpr (std::is_same<LT, float>::value) {
-                if (W.tc_on) {
-                    task_update_tc(W, j0, pb, sm);
-                    tc_done = true;
+        for (int s0 = 0; s0 < N && ok; s0 += kWSP) {
+            const int sw = min(kWSP, N - s0);
+            // the panels of super-panel S, each updating S's column tile only
+            for (int j0 = s0; j0 < s0 + sw; j0 += kWPB) {
+                const int pb = min(kWPB, N - j0);
+                if (!use_old) {
+                    const int rc = wide_select_pivots<LT>(W, j0, pb, smem, limit, sflag);
+                    if (rc == 2) return 2;
+                    if (rc == 1) {
+                        if (tid == 0) W.flags[0] = 0;
+                        __syncthreads();
+                        return 1;
+                    }
                 }
+                __syncthreads();
+                tick(0);
+                if (j0 > s0 && tid < kWPB) W.pos[W.piv[j0 - kWPB + tid]] = -1;
+                __syncthreads();
+                if (tid < pb) W.pos[W.piv[j0 + tid]] = tid;
+                if (!wide_pivot_block<LT>(W, j0, pb, sm)) {
+                    ok = false;
+                    break;
+                }
+                tick(0);
+                if (tid == 0) W.ctl->pad0 = s0;
+                wide_fork<LT>(W, kTaskPanel, j0, pb, h, x);
+                task_panel<LT>(W, j0, pb, sD, s0);
+                if (!wide_join<LT>(W, limit, sflag)) return 2;
+                tick(1);
+                if (tid == 0) W.ctl->pad0 = s0;
+                wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
+                bool tc_done = false;
+                if constexpr (std::is_same<LT, float>::value) {
+                    if (W.tc_on) {
+                        task_update_tc(W, j0, pb, sm, s0);
+                        tc_done = true;
+                    }
+                }
+                if (!tc_done) task_update<LT>(W, j0, pb, sm, s0);
+                if (!wide_join<LT>(W, limit, sflag)) return 2;
+                tick(2);
             }
-            if (!tc_done) task_update<LT>(W, j0, pb, sm);
-            if (!wide_join<LT>(W, limit, sflag)) return 2;
-            tick(2);
+            if (!ok) break;
+            // the last panel's pivots leave pos, S's pivots enter it
+            const int jl = s0 + ((sw - 1) / kWPB) * kWPB;
+            if (tid < s0 + sw - jl) W.pos[W.piv[jl + tid]] = -1;
+            __syncthreads();
+            if (sw < N) {
+                // one rank-sw update of every other column tile
+                if (tid < sw) W.pos[W.piv[s0 + tid]] = tid;
+                wide_fork<LT>(W, kTaskPanelS, s0, sw, h, x);
+                task_panel_s<LT>(W, s0, sw, sm);
+                if (!wide_join<LT>(W, limit, sflag)) return 2;
+                tick(1);
+                wide_fork<LT>(W, kTaskUpdateS, s0, sw, h, x);
+                bool tc_done = false;
+                if constexpr (std::is_same<LT, float>::value) {
+                    if (W.tc_on) {
+                        task_update_s_tc(W, s0, sw, sm);
+                        tc_done = true;
+                    }
+                }
+                if (!tc_done) task_update_s<LT>(W, s0, sw, sm);
+                if (!wide_join<LT>(W, limit, sflag)) return 2;
+                tick(2);
+                if (tid < sw) W.pos[W.piv[s0 + tid]] = -1;
+                __syncthreads();
+            }
         }
         if (ok) {
             if (tid == 0) W.flags[0] = 1;
