@@ -54,8 +54,11 @@ extern "C" {
                                 kernels.cuh:302-457, with step and order
                                 selection); N <= 512.  precision FP64: FP64
                                 LU; MIXED: an FP32 Gauss-Jordan inverse refined
-                                in FP64 as the Newton solve, FP64 factors for
-                                an instance after 4 Newton failures in a row */
+                                in FP64 as the Newton solve; a step that
+                                fails on FP32 factors is retried on FP64
+                                factors, and an instance keeps FP64 factors
+                                after 4 such failures without an FP32
+                                success in between */
 
 /* precision of the Newton matrix factorisation */
 #define LASSIE_PREC_FP64 0  /* FP64 LU: the plain FP64 GPU form */
@@ -93,8 +96,9 @@ typedef struct {
                              (the refinement still converges to the FP64 solve of
                              the current matrix); 0 factors at every step */
     int32_t tensor_cores; /* wide engine (networks above 512 species), mixed
-                             form: LASSIE_TC_TF32 runs the rank-32 updates of
-                             the factorisation on the tensor cores (tcgen05,
+                             form: LASSIE_TC_TF32 runs the rank-32 panel and
+                             rank-128 super-panel updates of the Gauss-Jordan
+                             factorisation on the tensor cores (tcgen05,
                              TF32 products of split operands, close to FP32),
                              LASSIE_TC_BF16 with BF16 operands and FP32
                              accumulation (factors good to about 2^-9; the FP64

@@ -12,9 +12,12 @@
 // The Newton matrix M = I - h*J is inverted in place by blocked Gauss-Jordan
 // elimination with partial pivoting (row pivots, kWPB-column panels): per
 // panel, the pivot block D (rows p_j0.., columns J) is inverted by the leader,
-// then all CTAs form PR = D^-1 * M[P_J, :] and apply the rank-kWPB update
+// which also forms PR = D^-1 * M[P_J, C], and all CTAs apply
 //     M[i, C] -= M[i, J] * PR[:, C]   (i not a pivot row, C not in J)
 //     M[i, J]  = -M[i, J] * D^-1,   M[P_J, C] = PR,   M[P_J, J] = D^-1.
+// The panels of one kWSP-column super-panel S restrict C to S's columns;
+// the other columns then take the same step for all of S at once (rank
+// kWSP, see the super-panel section below).
 // The result X satisfies inv(M)[j][p_k] = X[p_j][k], so a solve is
 //     x[j] = (X * r[p])[p_j]:   one dense matrix-vector product,
 // where the LU's two triangular solves would be 2N/32 dependent block steps.
@@ -32,7 +35,7 @@ constexpr int kWT = 128;   // rank-update tile: kWT rows x kWT columns per CTA p
 constexpr int kWSP = 128;
 static_assert(kWSP == kWT && kWSP % kWPB == 0, "a super-panel is one column tile");
 
-enum WideTask : int { kTaskExit = 0, kTaskAssemble = 1, kTaskPanel = 2, kTaskUpdate = 3,
+enum WideTask : int { kTaskExit = 0, kTaskAssemble = 1, kTaskUpdate = 3,
                       kTaskMatvec = 4, kTaskRates = 5, kTaskRkf = 6, kTaskRkfFinal = 7,
                       kTaskSolve = 8, kTaskSolveUpdate = 9, kTaskJv = 10, kTaskResidual = 11,
                       kTaskNewtonRhs = 12, kTaskPivotLevel = 13, kTaskPanelS = 14,
@@ -72,7 +75,6 @@ struct WideWs {
     int *cand;        // [2][N] candidate rows of the pivot search (two lists, alternating)
     LT *Dinv;         // [kWPB][kWPB]
     LT *PR;           // [kWPB][ld]
-    LT *AJ;           // [N][kWPB] panel columns before the update
     LT *AJS;          // [N][kWSP] super-panel columns before its panels
     LT *PRS;          // [kWSP][ld] DS^-1 * M[P_S, :] (DS: the super-panel's pivot block)
     LT *vin, *vout;   // [N] matrix-vector product input (gathered) and output
@@ -87,7 +89,7 @@ struct WideWs {
 };
 
 struct WideLayout {
-    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJ, AJS, PRS, vin, vout, flags, part,
+    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJS, PRS, vin, vout, flags, part,
         total;
     __host__ __device__ static int64_t al(int64_t v) { return (v + 255) & ~int64_t(255); }
     __host__ __device__ WideLayout(int N, int R, int nnz_a, int lt) {
@@ -104,7 +106,6 @@ struct WideLayout {
         PN = o;    o = al(o + int64_t(kWPB) * N * lt);
         Dinv = o;  o = al(o + int64_t(kWPB) * kWPB * lt);
         PR = o;    o = al(o + int64_t(kWPB) * ld * lt);
-        AJ = o;    o = al(o + int64_t(N) * kWPB * lt);
         AJS = o;   o = al(o + int64_t(N) * kWSP * lt);
         PRS = o;   o = al(o + int64_t(kWSP) * ld * lt);
         vin = o;   o = al(o + int64_t(N) * lt);
@@ -131,7 +132,6 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
     W.cand = reinterpret_cast<int *>(base + L.PN);
     W.Dinv = reinterpret_cast<LT *>(base + L.Dinv);
     W.PR = reinterpret_cast<LT *>(base + L.PR);
-    W.AJ = reinterpret_cast<LT *>(base + L.AJ);
     W.AJS = reinterpret_cast<LT *>(base + L.AJS);
     W.PRS = reinterpret_cast<LT *>(base + L.PRS);
     W.vin = reinterpret_cast<LT *>(base + L.vin);
@@ -195,17 +195,23 @@ __device__ bool wide_wait(const unsigned *p, unsigned target, WideCtl *ctl, uint
     unsigned spins = 0;
     const uint64_t t0 = global_ns();
     while (ld_acquire(p) < target) {
-        if (ld_acquire_i(&ctl->abort)) return false;
-        if ((++spins & 255) == 0) {
+        if ((++spins & 63) == 0) {
+            if (ld_acquire_i(&ctl->abort)) return false;
             const uint64_t now = global_ns();
             if ((limit && now > limit) || now - t0 > kWideStallNs) {
                 atomicExch(&ctl->abort, 1);
                 return false;
             }
         }
-        __nanosleep(256);
+        __nanosleep(32);
     }
     return true;
+}
+
+// *p += 1 with release semantics at GPU scope: the CTA's writes before the
+// caller's last barrier are visible to whoever acquires the new value.
+__device__ __forceinline__ void red_release_add1(unsigned *p) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(p) : "memory");
 }
 
 // ---------------------------------------------------------------- tasks
@@ -266,19 +272,15 @@ __device__ void task_assemble(const WideWs<LT> &W, const Net &m, const double *x
     }
 }
 
-// PR = D^-1 * M[P_J, C] for the columns C of the super-panel's tile (s0 ..)
-// and the snapshot AJ = M[:, J], spread over every thread of the grid: PR by
-// (group of 4 pivot rows, column), AJ by (row, 4 panel columns).  The
-// super-panel's first panel also takes the snapshot AJS = M[:, S].
+// Leader: PR = D^-1 * M[P_J, C] for the columns C of the super-panel's tile
+// (s0 ..) outside J, by (group of 4 pivot rows, column); D^-1 staged in sD.
 template <typename LT>
-__device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD, int s0) {
-    const int tid = threadIdx.x;
+__device__ void leader_panel_pr(const WideWs<LT> &W, int j0, int pb, int s0, LT *sD) {
+    const int tid = threadIdx.x, ld = W.ld;
     for (int q = tid; q < kWPB * kWPB; q += kThreads) sD[q] = W.Dinv[q];
     __syncthreads();
-    const int N = W.N, ld = W.ld;
     const int cw = min(s0 + kWSP, ld) - s0;
-    const int gt = blockIdx.x * kThreads + tid, nt = gridDim.x * kThreads;
-    for (int q = gt; q < (kWPB / 4) * cw; q += nt) {
+    for (int q = tid; q < (kWPB / 4) * cw; q += kThreads) {
         const int g = q / cw, c = s0 + (q - g * cw);
         if (c >= j0 && c < j0 + kWPB) continue;
         LT a[kWPB];
@@ -293,32 +295,27 @@ __device__ void task_panel(const WideWs<LT> &W, int j0, int pb, LT *sD, int s0) 
             W.PR[(int64_t)r * ld + c] = acc;
         }
     }
-    for (int q = gt; q < N * (kWPB / 4); q += nt) {
-        const int i = q / (kWPB / 4), k4 = (q - i * (kWPB / 4)) * 4;
-        const LT *src = W.A + (int64_t)i * ld + j0 + k4;
+    __syncthreads();
+}
+
+// Before the first panel of super-panel S updates a row tile, the tile's
+// CTA keeps AJS = M[rows, S] (the super-panel's rank-kWSP update needs the
+// columns of S as they were before S).
+template <typename LT>
+__device__ void snapshot_ajs(const WideWs<LT> &W, int r0, int s0) {
+    const int N = W.N, ld = W.ld, sw = min(kWSP, N - s0);
+    for (int q = threadIdx.x; q < kWT * (kWSP / 4); q += kThreads) {
+        const int r = q / (kWSP / 4), k4 = (q - r * (kWSP / 4)) * 4;
+        if (r0 + r >= N) continue;
+        const LT *src = W.A + (int64_t)(r0 + r) * ld + s0 + k4;
         LT v[4];
-        if (k4 + 4 <= pb) {
+        if (k4 + 4 <= sw) {
             load4(src, v);
         } else {
 #pragma unroll
-            for (int b = 0; b < 4; b++) v[b] = (k4 + b < pb) ? src[b] : LT(0);
+            for (int b = 0; b < 4; b++) v[b] = (k4 + b < sw) ? src[b] : LT(0);
         }
-        store4(W.AJ + (int64_t)i * kWPB + k4, v);
-    }
-    if (j0 == s0) {
-        const int sw = min(kWSP, N - s0);
-        for (int q = gt; q < N * (kWSP / 4); q += nt) {
-            const int i = q / (kWSP / 4), k4 = (q - i * (kWSP / 4)) * 4;
-            const LT *src = W.A + (int64_t)i * ld + s0 + k4;
-            LT v[4];
-            if (k4 + 4 <= sw) {
-                load4(src, v);
-            } else {
-#pragma unroll
-                for (int b = 0; b < 4; b++) v[b] = (k4 + b < sw) ? src[b] : LT(0);
-            }
-            store4(W.AJS + (int64_t)i * kWSP + k4, v);
-        }
+        store4(W.AJS + (int64_t)(r0 + r) * kWSP + k4, v);
     }
 }
 
@@ -337,9 +334,11 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s
     for (int t = blockIdx.x; t < nrt; t += gridDim.x) {
         const int r0 = t * kWT, c0 = s0;  // the super-panel's column tile
         __syncthreads();
+        if (j0 == s0) snapshot_ajs<LT>(W, r0, s0);
+        // the panel columns of this tile's rows (only this CTA writes them)
         for (int q = tid; q < kWT * kWPB; q += kThreads) {
             const int r = q / kWPB, k = q - r * kWPB;
-            sAJ[k * AS + r] = (r0 + r < N) ? W.AJ[(int64_t)(r0 + r) * kWPB + k] : LT(0);
+            sAJ[k * AS + r] = (r0 + r < N && k < pb) ? W.A[(int64_t)(r0 + r) * ld + j0 + k] : LT(0);
         }
         for (int q = tid; q < kWPB * kWT; q += kThreads) {
             const int k = q / kWT, cc = q - k * kWT;
@@ -389,9 +388,10 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s
 }
 
 // task_update on the tensor cores (FP32 form): per 128 x 128 tile the
-// panel columns (A = AJ rows) and B = [PR | D^-1] are split into TF32 high
-// and low parts in the canonical K-major layout, tc_tile_product forms
-// AJ * B in tensor memory, and each thread finishes 32 entries of its row:
+// panel columns of the tile's rows (A = M[rows, J]) and B = [PR | D^-1] are
+// split into TF32 high and low parts in the canonical K-major layout,
+// tc_tile_product forms A * B in tensor memory, and each thread finishes 32
+// entries of its row:
 // pivot rows take B, columns in J start from 0, the rest subtract from M.
 // False if a tensor-core wait ran out (the control block's abort flag is
 // then set).
@@ -409,12 +409,26 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
     for (int t = blockIdx.x; t < nrt && ok; t += gridDim.x) {
         const int r0 = t * kTcM, c0 = s0;  // the super-panel's column tile
         __syncthreads();
+        if (j0 == s0) snapshot_ajs<float>(W, r0, s0);
+        // A: the panel columns of this tile's rows (only this CTA writes them)
+        auto panel4 = [&](int r, int k4, float *v) {
+#pragma unroll
+            for (int b = 0; b < 4; b++) v[b] = 0.f;
+            if (r0 + r >= N) return;
+            const float *src = W.A + (int64_t)(r0 + r) * ld + j0 + k4;
+            if (k4 + 4 <= pb) {
+                load4(src, v);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 4; b++) v[b] = (k4 + b < pb) ? src[b] : 0.f;
+            }
+        };
         if (bf16) {
             // A: 128 rows x 32, B: kTcN columns x 32, 4 elements per thread
             for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
                 const int r = q >> 3, k4 = (q & 7) * 4;
-                float v[4] = {0.f, 0.f, 0.f, 0.f};
-                if (r0 + r < N) load4(W.AJ + (int64_t)(r0 + r) * kWPB + k4, v);
+                float v[4];
+                panel4(r, k4, v);
                 uint2 pk;
                 pk.x = (uint32_t)bf16_bits(v[0]) | ((uint32_t)bf16_bits(v[1]) << 16);
                 pk.y = (uint32_t)bf16_bits(v[2]) | ((uint32_t)bf16_bits(v[3]) << 16);
@@ -443,8 +457,8 @@ __device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *sm
         } else {
         for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
             const int r = q >> 3, k4 = (q & 7) * 4;
-            float v[4] = {0.f, 0.f, 0.f, 0.f};
-            if (r0 + r < N) load4(W.AJ + (int64_t)(r0 + r) * kWPB + k4, v);
+            float v[4];
+            panel4(r, k4, v);
             float h[4], l[4];
 #pragma unroll
             for (int b = 0; b < 4; b++) {
@@ -1053,12 +1067,10 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
     __shared__ double s_h;
     __shared__ const double *s_x;
     LT *sm = reinterpret_cast<LT *>(smem);
-    LT *sD = sm + wide_smem_bytes(W.N, (int)sizeof(LT)) / (int)sizeof(LT) - kWPB * kWPB;
     unsigned gen = 0;
     for (;;) {
         if (threadIdx.x == 0) {
             s_ok = wide_wait(&W.ctl->gen, gen + 1, W.ctl, limit);
-            __threadfence();
             if (s_ok) {
                 s_task = W.ctl->task;
                 s_j0 = W.ctl->j0;
@@ -1072,7 +1084,6 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
         gen++;
         switch (s_task) {
         case kTaskAssemble: task_assemble<LT>(W, m, s_x, s_h, mdiag); break;
-        case kTaskPanel: task_panel<LT>(W, s_j0, s_pb, sD, W.ctl->pad0); break;
         case kTaskUpdate:
             if constexpr (std::is_same<LT, float>::value) {
                 if (W.tc_on) {
@@ -1138,8 +1149,7 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
-            atomicAdd(&W.ctl->done, 1u);
+            red_release_add1(&W.ctl->done);
         }
     }
 }
@@ -1157,8 +1167,7 @@ __device__ void wide_fork(const WideWs<LT> &W, int task, int j0, int pb, double 
         c->h = h;
         c->x = x;
         c->done = 0;
-        __threadfence();
-        atomicAdd(&c->gen, 1u);
+        red_release_add1(&c->gen);
     }
 }
 
@@ -1168,7 +1177,6 @@ __device__ bool wide_join(const WideWs<LT> &W, uint64_t limit, int *sflag) {
     __syncthreads();
     if (threadIdx.x == 0) {
         *sflag = wide_wait(&W.ctl->done, gridDim.x - 1, W.ctl, limit) ? 1 : 0;
-        __threadfence();
     }
     __syncthreads();
     return *sflag != 0;
@@ -1275,12 +1283,8 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
                     ok = false;
                     break;
                 }
+                leader_panel_pr<LT>(W, j0, pb, s0, sD);
                 tick(0);
-                if (tid == 0) W.ctl->pad0 = s0;
-                wide_fork<LT>(W, kTaskPanel, j0, pb, h, x);
-                task_panel<LT>(W, j0, pb, sD, s0);
-                if (!wide_join<LT>(W, limit, sflag)) return 2;
-                tick(1);
                 if (tid == 0) W.ctl->pad0 = s0;
                 wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
                 bool tc_done = false;

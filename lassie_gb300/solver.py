@@ -59,7 +59,7 @@ class NativeModel:
 
 
 ROOTS = {"pow": nat.ROOT_POW, "sqrt": nat.ROOT_SQRT}
-# rank-32 updates of the wide engine's factorisation: FP32 pipes ("off"),
+# rank updates of the wide engine's factorisation: FP32 pipes ("off"),
 # tensor cores with split TF32 operands ("tf32", the default, or True), or
 # BF16 operands with FP32 accumulation ("bf16")
 TENSOR_CORES = {False: 0, True: 1, "off": 0, "tf32": 1, "bf16": 2}
