@@ -4,6 +4,8 @@ solutions, against a tight-tolerance LSODA solution (scipy), and against
 scipy's own BDF (the published algorithm it restates) for accuracy."""
 import math
 
+import os
+
 import numpy as np
 import pytest
 
@@ -55,7 +57,12 @@ def test_closed_forms():
     assert np.allclose(out[:, 0], m.x0[0] + m.k[0] * m.t, rtol=1e-12, atol=1e-12)
 
 
-@pytest.mark.parametrize("name", ["c1", "c5", "sized-100", "c2-short"])
+SLOW = pytest.mark.skipif(not os.environ.get("LASSIE_SLOW_TESTS"),
+                          reason="five minutes of scipy on 512 species; LASSIE_SLOW_TESTS=1 runs it")
+
+
+@pytest.mark.parametrize("name", ["c1", "c5", "sized-100",
+                                  pytest.param("c2-short", marks=SLOW)])
 def test_accuracy_like_scipy_bdf(name):
     """Global error against LSODA at rtol 1e-12 is of the size scipy's BDF
     reaches at the same tolerances (both control the local error only).  On

@@ -165,13 +165,17 @@ def test_float_oracle_against_the_reference_float_mode(name):
     the reference's -p float outputs (--use_fast_math division and pow):
     within the float tolerance before the first sample at which the float
     oracle's own spread (quarter root or Newton corrections moved by one
-    float ulp) leaves it, and within twice the spread's excess after it."""
+    float ulp) leaves it, and within twice the spread's excess after it
+    (the spread is computed only when the reference leaves the tolerance
+    somewhere)."""
     d = np.load(os.path.join(FLOAT_DIR, name + ".npz"))
     m = Model(left=d["left"], right=d["right"], k=d["k"], x0=d["x0"], t=d["t"])
     if d["feed"].size:
         m.feed = d["feed"]
     base, st, rc = O.solve(m, precision="float")
     assert rc == 0
+    if np.all(fexcess(d["ref"], base) <= 0):
+        return  # within the float tolerance at every sample: no spread needed
     first, worst = base.shape[0], 0.0
     for ctx in ([O.root_perturbation(2.0 ** -23, s) for s in range(1, 6)]
                 + [O.solve_perturbation(2.0 ** -23, s) for s in range(1, 6)]):
