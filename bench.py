@@ -136,6 +136,39 @@ def load_traffic(alg_flops):
     return None if per_flop is None else per_flop * alg_flops
 
 
+def spread_classes(mixed, fp64, mixed_stats, cap):
+    """Instances of the FP64-vs-mixed sample by the oracle's own spread
+    (tests/oracle_fixtures/c4_spread.npz, the same 152 instances on t in
+    [0, 2]): within rtol 1e-6 / atol 1e-9 of the FP64 form (which equals the
+    oracle bit for bit) before the spread's first divergence and within twice
+    its excess after it -- the FP64 solvers' spread first, else the normwise
+    one -- or outside both.  None without the fixture or for another sample."""
+    p = os.path.join(ROOT, "tests", "oracle_fixtures", "c4_spread.npz")
+    if not os.path.exists(p):
+        return None
+    f = np.load(p)
+    if len(f["index"]) != len(mixed) or int(f["cap"]) != cap:
+        return None
+    out = {"fp64_solvers": 0, "normwise_solvers": 0, "outside": 0, "capped_in_oracle": 0}
+    for j, (a, b, st) in enumerate(zip(mixed, fp64, mixed_stats)):
+        if int(f["status"][j]) != 0:
+            out["capped_in_oracle"] += 1
+            continue
+        e = np.max(np.abs(a - b) - 1e-9 - 1e-6 * np.abs(b), axis=1)
+
+        def within(first, worst):
+            return st["status"] == 0 and np.all(e[:first] <= 0) and e.max() <= 2 * worst
+
+        if within(int(f["first_divergence"][j]), float(f["worst_excess"][j])):
+            out["fp64_solvers"] += 1
+        elif ("first_divergence_normwise" in f.files and
+              within(int(f["first_divergence_normwise"][j]), float(f["worst_excess_normwise"][j]))):
+            out["normwise_solvers"] += 1
+        else:
+            out["outside"] += 1
+    return out
+
+
 def pipe_work(stats, models):
     """Work of the mixed batched integrator on the pipes that bound it.
     FP32 (the FMA pipes): the Gauss-Jordan inverses, 2 N^3 per factorisation,
@@ -767,10 +800,13 @@ def main():
 
     if rank == 0 and world == 1 and not args.no_extras:
         # plain FP64 GPU form vs the mixed form on the same sample
+        # (sqrt(sqrt()) quarter root, as the oracle, so that the oracle's
+        # spread stored for this sample applies)
         sample = [synth.shorten(m, 2.0, 5) for m in models[::13][:152]]
         res = {}
         for eng in ("fp64", "mixed"):
-            b = solver.Batch(sample, engine=eng, max_steps=args.max_steps // 10, deadline_s=900)
+            b = solver.Batch(sample, engine=eng, max_steps=args.max_steps // 10, deadline_s=900,
+                             root="sqrt")
             b.run(stream.cuda_stream)
             b.sync()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -797,7 +833,9 @@ def main():
             "max_rel_err_vs_fp64": worst, "points_outside_rtol1e-6_atol1e-9": nbad,
             "instances_same_step_sequence": len(same),
             "max_rel_err_same_step_sequence": w_same,
-            "points_outside_same_step_sequence": n_same}
+            "points_outside_same_step_sequence": n_same,
+            "oracle_spread": spread_classes(res["mixed"][1], res["fp64"][1], res["mixed"][2],
+                                            args.max_steps // 10)}
         line["parity_vs_fp64_form"] = parity_table()
         line["adjoint"] = adjoint_measure()
         line["rhs_hbm"] = rhs_bandwidth(torch, stream)
