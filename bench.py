@@ -488,9 +488,14 @@ def bdf_measure(torch, stream, models, max_steps, engine):
     from lassie_gb300 import solver
     b = solver.Batch(models, engine=engine, max_steps=max_steps, deadline_s=900,
                      bdf={"rtol": 1e-6, "atol": 1e-9})
-    b.run(stream.cuda_stream)  # warm-up
-    b.sync()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        b.run(stream.cuda_stream)  # warm-up, creation order (largest network first)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms_creation = e0.elapsed_time(e1)
+    b.order_by_cost()  # longest first by the warm-up's per-instance times
     with torch.cuda.stream(stream):
         e0.record(stream)
         b.run(stream.cuda_stream)
@@ -505,7 +510,9 @@ def bdf_measure(torch, stream, models, max_steps, engine):
             "mean_steps": sum(s["be_steps"] for s in ok) / max(1, len(ok)),
             "mean_factorisations": sum(s["lu_factorisations"] for s in ok) / max(1, len(ok)),
             "mean_newton_iters": sum(s["newton_iters"] for s in ok) / max(1, len(ok)),
-            "controller": "BDF orders 1-5, rtol 1e-6, atol 1e-9", "engine": engine}
+            "controller": "BDF orders 1-5, rtol 1e-6, atol 1e-9", "engine": engine,
+            "queue_order": "longest first by the warm-up run's per-instance times",
+            "ms_creation_order": ms_creation}
 
 
 def parity_table():
@@ -716,10 +723,19 @@ def main():
         torch.cuda.synchronize()
 
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for w in range(args.warmup):
             flush.zero_()
+            if w == args.warmup - 1:
+                w0.record(stream)
             batch.run(stream.cuda_stream)
+            if w == args.warmup - 1:
+                w1.record(stream)
         torch.cuda.synchronize()
+        ms_creation_order = w0.elapsed_time(w1) if args.warmup > 0 else None
+        # the timed runs take the instances longest first, by the last
+        # warm-up run's per-instance times (no result changes)
+        batch.order_by_cost()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(args.steps)]
         with ClockSampler(local) as clocks:
@@ -791,6 +807,10 @@ def main():
                     "tile_rows": {str(r): batch.tile_rows().count(r) for r in (8, 4, 2)},
                     "parallelism": f"instances sharded over {world} GPU(s) "
                                    f"({args.scaling} scaling)"},
+            "queue_order": {"timed_steps": "longest first by the last warm-up run's per-instance "
+                                           "integration times (lassie_batch_order_by_cost)",
+                            "warmup_order": "largest network first (creation order)",
+                            "ms_last_warmup_step": ms_creation_order},
             "failed_instances": len(bad),
             "e2e": {"value": e2e_val, "unit": "sims/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -166,6 +166,9 @@ typedef struct {
     int64_t rhs_evals;
     int32_t order_final;
     int32_t pad2;
+    /* SM clock cycles of the instance's whole integration (thread 0 of its
+       CTA); lassie_batch_order_by_cost orders later runs by it */
+    int64_t cycles_total;
 } lassie_stats;
 
 /* One instance of a batch: a network, its parameterisation and its outputs.
@@ -235,6 +238,15 @@ int lassie_batch_read(lassie_batch *batch, const lassie_instance *inst,
                       lassie_stats *stats);
 /* kernel launches one lassie_batch_run issues (for launch accounting) */
 int lassie_batch_launches(const lassie_batch *batch);
+/* Orders the batch's later runs by the last run's per-instance integration
+   times (lassie_stats.cycles_total), longest first, so that the persistent
+   work queue ends with short instances (replaces the launch heuristic of
+   Simulation.cuh:583-600 for repeated runs; the reference runs one model per
+   process).  Results of every instance do not depend on the order.  A batch
+   that has not run keeps its creation order (largest network first).  Waits
+   for the batch's stream; refused while that stream is being captured.
+   A captured run replays with the new order. */
+int lassie_batch_order_by_cost(lassie_batch *batch);
 /* bytes lassie_solve_batch moves host->device (inputs) and device->host
    (trajectories and stats) for this batch */
 int lassie_batch_bytes(const lassie_batch *batch, int64_t *h2d, int64_t *d2h);

@@ -34,6 +34,7 @@ EXPORTS = (
     "lassie_model_create_dense", "lassie_model_create_csr", "lassie_model_destroy",
     "lassie_model_info", "lassie_solve", "lassie_solve_batch", "lassie_batch_create",
     "lassie_batch_run", "lassie_batch_sync", "lassie_batch_read", "lassie_batch_launches",
+    "lassie_batch_order_by_cost",
     "lassie_batch_bytes", "lassie_batch_destroy", "lassie_rhs_device", "lassie_rhs", "lassie_newton_matrix",
     "lassie_newton_matrix_device", "lassie_jacobian_nnz", "lassie_jacobian_pattern",
     "lassie_lu_solve", "lassie_adjoint_batch", "lassie_solve_noalloc", "lassie_batch_tile_rows", "lassie_tc_selftest", "lassie_tc_selftest_bf16",
@@ -64,7 +65,8 @@ class Stats(C.Structure):
                 ("t_final", C.c_double),
                 ("dt_be_final", C.c_double), ("status", C.c_int32), ("pad", C.c_int32),
                 ("jac_evals", C.c_int64), ("rhs_evals", C.c_int64),
-                ("order_final", C.c_int32), ("pad2", C.c_int32)]
+                ("order_final", C.c_int32), ("pad2", C.c_int32),
+                ("cycles_total", C.c_int64)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if not f.startswith("pad")}
@@ -126,6 +128,7 @@ def load():
         L.lassie_batch_sync.argtypes = [vp]
         L.lassie_batch_read.argtypes = [vp, vp, vp]
         L.lassie_batch_launches.argtypes = [vp]
+        L.lassie_batch_order_by_cost.argtypes = [vp]
         L.lassie_batch_bytes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64)]
         L.lassie_batch_tile_rows.argtypes = [vp, vp]
         L.lassie_batch_destroy.argtypes = [vp]

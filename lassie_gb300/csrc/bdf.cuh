@@ -65,26 +65,33 @@ __device__ __forceinline__ double bdf_rms(const double *v, const double *scale, 
 
 // D[0..q] <- RU^T D[0..q], RU = R(factor) R(1), R(f)[i][j] = prod_{r=1..i}
 // (r - 1 - f j) / r for j >= 1, R[0][j] = 1, R[i>0][0] = 0.
+// The (q+1) x (q+1) matrix RU is formed once, by thread 0 (FP64 is slow on
+// this GPU: 512 threads forming it redundantly cost tens of microseconds),
+// and read by every thread from shared memory.
 __device__ __noinline__ void bdf_change_d(double *Dd, int vstride, int N, int q, double factor) {
-    double R[kBdfMaxOrder + 1][kBdfMaxOrder + 1], U[kBdfMaxOrder + 1][kBdfMaxOrder + 1];
-    double RU[kBdfMaxOrder + 1][kBdfMaxOrder + 1];
+    __shared__ double RU[kBdfMaxOrder + 1][kBdfMaxOrder + 1];
+    if (threadIdx.x == 0) {
+        double R[kBdfMaxOrder + 1][kBdfMaxOrder + 1], U[kBdfMaxOrder + 1][kBdfMaxOrder + 1];
 #pragma unroll 1
-    for (int pass = 0; pass < 2; pass++) {
-        const double f = pass == 0 ? factor : 1.0;
-        double (*M)[kBdfMaxOrder + 1] = pass == 0 ? R : U;
-        for (int j = 0; j <= q; j++) M[0][j] = 1.0;
-        for (int i = 1; i <= q; i++)
+        for (int pass = 0; pass < 2; pass++) {
+            const double f = pass == 0 ? factor : 1.0;
+            double (*M)[kBdfMaxOrder + 1] = pass == 0 ? R : U;
+            for (int j = 0; j <= q; j++) M[0][j] = 1.0;
+            for (int i = 1; i <= q; i++)
+                for (int j = 0; j <= q; j++) {
+                    const double mij =
+                        j == 0 ? 0.0 : ((double)(i - 1) - f * (double)j) / (double)i;
+                    M[i][j] = M[i - 1][j] * mij;
+                }
+        }
+        for (int i = 0; i <= q; i++)
             for (int j = 0; j <= q; j++) {
-                const double mij = j == 0 ? 0.0 : ((double)(i - 1) - f * (double)j) / (double)i;
-                M[i][j] = M[i - 1][j] * mij;
+                double a = 0.0;
+                for (int l = 0; l <= q; l++) a = a + R[i][l] * U[l][j];
+                RU[i][j] = a;
             }
     }
-    for (int i = 0; i <= q; i++)
-        for (int j = 0; j <= q; j++) {
-            double a = 0.0;
-            for (int l = 0; l <= q; l++) a = a + R[i][l] * U[l][j];
-            RU[i][j] = a;
-        }
+    __syncthreads();
     for (int s = threadIdx.x; s < N; s += kThreads) {
         double nv[kBdfMaxOrder + 1];
         for (int j = 0; j <= q; j++) {
@@ -102,6 +109,8 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                               int *ired, InstDesc &D, InstResult &st, uint64_t deadline) {
     constexpr bool kMixed = std::is_same<LT, float>::value;
     constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN;
+    __shared__ double s_bcast[1];  // a scalar formed by thread 0 for all
+    __shared__ int s_ibcast;
     const int tid = threadIdx.x;
     if (tid == 0) {
         D = P.inst[id];
@@ -169,6 +178,7 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     const int ld = round_up4(N);
     long long cyc[3] = {0, 0, 0};
     long long c_mark = 0;
+    const long long c_start = clock64();
 
     double gamma[kBdfMaxOrder + 2], econst[kBdfMaxOrder + 2];
     gamma[0] = 0.0;
@@ -468,9 +478,14 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                 if (err_norm > 1.0) {
                     // Newton converged: the factors stay until the next
                     // refactoring (modified Newton with the previous c)
-                    if (tid == 0) st.rkf_retries++;
-                    double fct = safety * pow(err_norm, -1.0 / (double)(q + 1));
-                    fct = bdf_quantize(fmax(kBdfMinFactor, fct));
+                    if (tid == 0) {
+                        st.rkf_retries++;
+                        // one thread forms the factor (FP64 pow), all read it
+                        double f0 = safety * pow(err_norm, -1.0 / (double)(q + 1));
+                        s_bcast[0] = bdf_quantize(fmax(kBdfMinFactor, f0));
+                    }
+                    __syncthreads();
+                    const double fct = s_bcast[0];
                     bdf_change_d(Dd, vstride, N, q, fct);
                     h = h * fct;
                     n_equal = 0;
@@ -527,20 +542,30 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
                     __syncthreads();
                     e_p = bdf_rms(aux, scale, N, red);
                 }
-                const double en[3] = {e_m, err_norm, e_p};
-                double fq[3];
-                for (int i = 0; i < 3; i++) {
-                    fq[i] = en[i] == 0.0 ? INFINITY
-                                         : (isinf(en[i]) ? 0.0
-                                                         : pow(en[i], -1.0 / (double)(q + i)));
-                    fq[i] = bdf_quantize(fmin(kBdfMaxFactor, safety * fq[i]));
+                // one thread forms the candidate factors (FP64 pow), all read
+                // the choice
+                if (tid == 0) {
+                    const double en[3] = {e_m, err_norm, e_p};
+                    double fq[3];
+                    for (int i = 0; i < 3; i++) {
+                        fq[i] = en[i] == 0.0 ? INFINITY
+                                             : (isinf(en[i]) ? 0.0
+                                                             : pow(en[i], -1.0 / (double)(q + i)));
+                        fq[i] = bdf_quantize(fmin(kBdfMaxFactor, safety * fq[i]));
+                    }
+                    int best = 0;
+                    for (int i = 1; i < 3; i++)
+                        if (fq[i] > fq[best]) best = i;
+                    s_bcast[0] = fq[best];
+                    s_ibcast = best;
                 }
-                int best = 0;
-                for (int i = 1; i < 3; i++)
-                    if (fq[i] > fq[best]) best = i;
+                __syncthreads();
+                const int best = s_ibcast;
+                const double fbest = s_bcast[0];
+                __syncthreads();
                 q += best - 1;
-                h = h * fq[best];
-                bdf_change_d(Dd, vstride, N, q, fq[best]);
+                h = h * fbest;
+                bdf_change_d(Dd, vstride, N, q, fbest);
                 n_equal = 0;
                 lu_valid = false;
             }
@@ -549,6 +574,7 @@ __device__ __noinline__ void bdf_integrate(const LaunchParams &P, int id, unsign
     __syncthreads();
     if (tid == 0) {
         st.outer_iters = attempts;
+        st.cycles_total = clock64() - c_start;
         st.t_final = tc;
         st.dt_be_final = h;
         st.jac_evals = jac_evals;

@@ -756,6 +756,33 @@ extern "C" int lassie_batch_run(lassie_batch *b, void *stream) {
 
 extern "C" int lassie_batch_launches(const lassie_batch *b) { return (b && b->n > 0) ? 1 : 0; }
 
+// Longest-processing-time order for the persistent work queue: the last
+// run's whole-integration cycles per instance, longest first (ties keep the
+// current order, largest network first at creation).  Each CTA integrates
+// its instance alone, so the order changes no result.
+extern "C" int lassie_batch_order_by_cost(lassie_batch *b) {
+    if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
+    if (b->n <= 1 || b->wide) return LASSIE_OK;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CU(cudaStreamIsCapturing(b->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+        return set_error(LASSIE_ERR_ARGS, "lassie_batch_order_by_cost: stream is being captured");
+    std::vector<InstResult> hres(b->n);
+    CU(cudaMemcpyAsync(hres.data(), b->d_res.p, hres.size() * sizeof(InstResult),
+                       cudaMemcpyDeviceToHost, b->stream));
+    CU(cudaStreamSynchronize(b->stream));
+    bool measured = false;
+    for (const InstResult &r : hres) measured = measured || r.cycles_total > 0;
+    if (!measured) return LASSIE_OK;  // no run yet
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) {
+        return hres[a].cycles_total > hres[c].cycles_total;
+    });
+    CU(cudaMemcpyAsync(b->d_order.p, b->order.data(), b->order.size() * 4, cudaMemcpyHostToDevice,
+                       b->stream));
+    CU(cudaStreamSynchronize(b->stream));
+    return LASSIE_OK;
+}
+
 extern "C" int lassie_batch_bytes(const lassie_batch *b, int64_t *h2d, int64_t *d2h) {
     if (!b) return set_error(LASSIE_ERR_ARGS, "null batch");
     if (h2d)

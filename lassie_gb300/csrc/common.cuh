@@ -46,6 +46,7 @@ struct InstResult {
     int32_t status, pad;
     int64_t jac_evals, rhs_evals;  // BDF controller
     int32_t order_final, pad2;
+    int64_t cycles_total;  // the instance's whole integration
 };
 static_assert(sizeof(InstResult) == sizeof(lassie_stats), "stats layout");
 

@@ -1426,6 +1426,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
     constexpr int PB = LuShape<LT>::PB, TN = LuShape<LT>::TN;
     constexpr bool kMixed = std::is_same<LT, float>::value;
     const int tid = threadIdx.x;
+    const long long c_start = clock64();
     if (tid == 0) {
         D = P.inst[id];
         st = InstResult{};
@@ -1979,6 +1980,7 @@ __device__ void integrate(const LaunchParams &P, int id, unsigned char *smem, do
         st.t_final = t;
         st.dt_be_final = newDt;
         st.status = status;
+        st.cycles_total = clock64() - c_start;
         P.res[id] = st;
     }
     __syncthreads();

@@ -235,6 +235,7 @@ constexpr int kFVecs = 16;
 __device__ void fm_integrate(const LaunchParams &P, int id, unsigned char *smem, double *redd,
                              float *redf, int *redi, InstDesc &D, InstResult &st, uint64_t deadline) {
     const int tid = threadIdx.x;
+    const long long c_start = clock64();
     if (tid == 0) {
         D = P.inst[id];
         st = InstResult{};
@@ -500,6 +501,7 @@ __device__ void fm_integrate(const LaunchParams &P, int id, unsigned char *smem,
         st.t_final = t;
         st.dt_be_final = newDtBDF;
         st.status = status;
+        st.cycles_total = clock64() - c_start;
         P.res[id] = st;
     }
     __syncthreads();

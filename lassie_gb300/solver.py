@@ -197,6 +197,13 @@ class Batch:
     def launches(self) -> int:
         return int(nat.load().lassie_batch_launches(self.handle))
 
+    def order_by_cost(self) -> None:
+        """Later runs take the instances longest first, by the last run's
+        per-instance integration times (``lassie_batch_order_by_cost``); no
+        result changes."""
+        nat.check(nat.load().lassie_batch_order_by_cost(self.handle),
+                  "lassie_batch_order_by_cost")
+
     def transfer_bytes(self) -> Tuple[int, int]:
         h2d, d2h = C.c_int64(), C.c_int64()
         nat.check(nat.load().lassie_batch_bytes(self.handle, C.byref(h2d), C.byref(d2h)),
