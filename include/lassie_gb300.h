@@ -96,14 +96,16 @@ typedef struct {
                              (the refinement still converges to the FP64 solve of
                              the current matrix); 0 factors at every step */
     int32_t tensor_cores; /* wide engine (networks above 512 species), mixed
-                             form: LASSIE_TC_TF32 runs the rank-32 panel and
-                             rank-128 super-panel updates of the Gauss-Jordan
+                             form: LASSIE_TC_TF32 runs the rank-128
+                             super-panel updates of the Gauss-Jordan
                              factorisation on the tensor cores (tcgen05,
                              TF32 products of split operands, close to FP32),
                              LASSIE_TC_BF16 with BF16 operands and FP32
                              accumulation (factors good to about 2^-9; the FP64
                              refinement takes more sweeps), LASSIE_TC_OFF on
-                             the FP32 pipes; default LASSIE_TC_TF32 */
+                             the FP32 pipes; default LASSIE_TC_TF32.  The
+                             rank-32 updates within a super-panel run on the
+                             FP32 pipes in every setting */
     int32_t controller;   /* LASSIE_CTRL_* (default LASSIE_CTRL_COMPAT) */
     /* LASSIE_CTRL_BDF only: */
     double rtol;          /* relative tolerance (1e-6) */
@@ -270,8 +272,8 @@ int lassie_adjoint_batch(const lassie_instance *inst, int32_t n, const double *c
                          double *loss, double *const *grad_logk, double *const *grad_x0,
                          lassie_stats *stats);
 
-/* Self-test of the tensor-core (tcgen05) tile product used by the wide
-   engine's rank-32 updates (no reference counterpart): on device buffers,
+/* Self-test of the tensor-core (tcgen05) tile product, one K = 32 chunk of
+   the wide engine's rank-128 updates (no reference counterpart): on device buffers,
    D[128 x 128] = A[128 x 32] * B[32 x 128], row-major FP32, computed as three
    TF32 products of the operands split into TF32 high and low parts; status[0]
    becomes 1, or 2 if the tensor core did not complete.  Launches one CTA on

@@ -302,9 +302,9 @@ __device__ void leader_panel_pr(const WideWs<LT> &W, int j0, int pb, int s0, LT 
 // CTA keeps AJS = M[rows, S] (the super-panel's rank-kWSP update needs the
 // columns of S as they were before S).
 template <typename LT>
-__device__ void snapshot_ajs(const WideWs<LT> &W, int r0, int s0) {
+__device__ void snapshot_ajs(const WideWs<LT> &W, int r0, int s0, int rows = kWT) {
     const int N = W.N, ld = W.ld, sw = min(kWSP, N - s0);
-    for (int q = threadIdx.x; q < kWT * (kWSP / 4); q += kThreads) {
+    for (int q = threadIdx.x; q < rows * (kWSP / 4); q += kThreads) {
         const int r = q / (kWSP / 4), k4 = (q - r * (kWSP / 4)) * 4;
         if (r0 + r >= N) continue;
         const LT *src = W.A + (int64_t)(r0 + r) * ld + s0 + k4;
@@ -319,26 +319,30 @@ __device__ void snapshot_ajs(const WideWs<LT> &W, int r0, int s0) {
     }
 }
 
-// The rank-kWPB update of every row in the super-panel's column tile, in
-// kWT x kWT tiles; thread (ty, tx) owns rows ty*8.. and columns tx*4.. of a
-// tile.  Columns in J start from 0 and use D^-1 in place of PR; the current
-// panel's pivot rows take their new values (PR, D^-1) directly.
+// The panel's rank-kWPB update of the super-panel's column tile in tiles of
+// kNarrowRows rows, on the FP32 (or FP64) pipes: the strip is N x 128, so
+// 128-row tiles would keep only N / 128 CTAs busy.  Thread (ty, tx) owns
+// rows 2*ty, 2*ty+1 and columns tx*4.. of a tile.  Columns in J start from 0
+// and use D^-1 in place of PR; the panel's pivot rows take their new values
+// (PR, D^-1) directly.
+constexpr int kNarrowRows = 32;
 template <typename LT>
-__device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s0) {
-    constexpr int AS = kWT + 4;           // sAJ row stride (16-byte rows)
-    LT *sAJ = smem;                       // [kWPB][AS]: panel columns, column-major
-    LT *sB = smem + kWPB * AS;            // [kWPB][kWT]
+__device__ void task_update_narrow(const WideWs<LT> &W, int j0, int pb, LT *smem, int s0) {
+    static_assert(kNarrowRows == 2 * kWarps && kWT == 4 * 32, "2 rows x 4 columns a thread");
+    LT *sAJ = smem;                       // [kWPB][kNarrowRows]: panel columns, K-major
+    LT *sB = smem + kWPB * kNarrowRows;   // [kWPB][kWT]
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const int N = W.N, ld = W.ld;
-    const int nrt = (N + kWT - 1) / kWT;
+    const int nrt = (N + kNarrowRows - 1) / kNarrowRows;
     for (int t = blockIdx.x; t < nrt; t += gridDim.x) {
-        const int r0 = t * kWT, c0 = s0;  // the super-panel's column tile
+        const int r0 = t * kNarrowRows, c0 = s0;
         __syncthreads();
-        if (j0 == s0) snapshot_ajs<LT>(W, r0, s0);
+        if (j0 == s0) snapshot_ajs<LT>(W, r0, s0, kNarrowRows);
         // the panel columns of this tile's rows (only this CTA writes them)
-        for (int q = tid; q < kWT * kWPB; q += kThreads) {
+        for (int q = tid; q < kNarrowRows * kWPB; q += kThreads) {
             const int r = q / kWPB, k = q - r * kWPB;
-            sAJ[k * AS + r] = (r0 + r < N && k < pb) ? W.A[(int64_t)(r0 + r) * ld + j0 + k] : LT(0);
+            sAJ[k * kNarrowRows + r] =
+                (r0 + r < N && k < pb) ? W.A[(int64_t)(r0 + r) * ld + j0 + k] : LT(0);
         }
         for (int q = tid; q < kWPB * kWT; q += kThreads) {
             const int k = q / kWT, cc = q - k * kWT;
@@ -354,10 +358,10 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s
         const int col = c0 + tx * 4;
         if (col >= ld) continue;
         const bool inJ = col >= j0 && col < j0 + kWPB;
-        const int rl0 = ty * 8;
-        LT acc[8][4];
+        const int rl0 = ty * 2;
+        LT acc[2][4];
 #pragma unroll
-        for (int a = 0; a < 8; a++) {
+        for (int a = 0; a < 2; a++) {
             const int row = r0 + rl0 + a;
             if (row < N && !inJ) {
                 load4(W.A + (int64_t)row * ld + col, acc[a]);
@@ -366,18 +370,19 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s
                 for (int b = 0; b < 4; b++) acc[a][b] = LT(0);
             }
         }
-#pragma unroll 4
+#pragma unroll 8
         for (int k = 0; k < kWPB; k++) {
-            LT av[8], bv[4];
-            load8(sAJ + k * AS + rl0, av);
+            LT bv[4];
             load4(sB + k * kWT + tx * 4, bv);
+            const LT a0 = sAJ[k * kNarrowRows + rl0], a1 = sAJ[k * kNarrowRows + rl0 + 1];
 #pragma unroll
-            for (int a = 0; a < 8; a++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[a][b] = lt_fma(-av[a], bv[b], acc[a][b]);
+            for (int b = 0; b < 4; b++) {
+                acc[0][b] = lt_fma(-a0, bv[b], acc[0][b]);
+                acc[1][b] = lt_fma(-a1, bv[b], acc[1][b]);
+            }
         }
 #pragma unroll
-        for (int a = 0; a < 8; a++) {
+        for (int a = 0; a < 2; a++) {
             const int row = r0 + rl0 + a;
             if (row >= N) break;
             const int pr = W.pos[row];
@@ -385,154 +390,6 @@ __device__ void task_update(const WideWs<LT> &W, int j0, int pb, LT *smem, int s
             store4(W.A + (int64_t)row * ld + col, acc[a]);
         }
     }
-}
-
-// task_update on the tensor cores (FP32 form): per 128 x 128 tile the
-// panel columns of the tile's rows (A = M[rows, J]) and B = [PR | D^-1] are
-// split into TF32 high and low parts in the canonical K-major layout,
-// tc_tile_product forms A * B in tensor memory, and each thread finishes 32
-// entries of its row:
-// pivot rows take B, columns in J start from 0, the rest subtract from M.
-// False if a tensor-core wait ran out (the control block's abort flag is
-// then set).
-// W.tc_on == 2: the BF16 form (operands rounded to BF16, one kind::f16 MMA
-// per 16-wide K step, FP32 accumulation).
-__device__ bool task_update_tc(const WideWs<float> &W, int j0, int pb, float *smem, int s0) {
-    float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
-    uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
-    const bool bf16 = W.tc_on == 2;
-    const int tid = threadIdx.x;
-    const int N = W.N, ld = W.ld;
-    const int nrt = (N + kTcM - 1) / kTcM;
-    uint32_t phase = *W.tc_phase;
-    bool ok = true;
-    for (int t = blockIdx.x; t < nrt && ok; t += gridDim.x) {
-        const int r0 = t * kTcM, c0 = s0;  // the super-panel's column tile
-        __syncthreads();
-        if (j0 == s0) snapshot_ajs<float>(W, r0, s0);
-        // A: the panel columns of this tile's rows (only this CTA writes them)
-        auto panel4 = [&](int r, int k4, float *v) {
-#pragma unroll
-            for (int b = 0; b < 4; b++) v[b] = 0.f;
-            if (r0 + r >= N) return;
-            const float *src = W.A + (int64_t)(r0 + r) * ld + j0 + k4;
-            if (k4 + 4 <= pb) {
-                load4(src, v);
-            } else {
-#pragma unroll
-                for (int b = 0; b < 4; b++) v[b] = (k4 + b < pb) ? src[b] : 0.f;
-            }
-        };
-        if (bf16) {
-            // A: 128 rows x 32, B: kTcN columns x 32, 4 elements per thread
-            for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
-                const int r = q >> 3, k4 = (q & 7) * 4;
-                float v[4];
-                panel4(r, k4, v);
-                uint2 pk;
-                pk.x = (uint32_t)bf16_bits(v[0]) | ((uint32_t)bf16_bits(v[1]) << 16);
-                pk.y = (uint32_t)bf16_bits(v[2]) | ((uint32_t)bf16_bits(v[3]) << 16);
-                *reinterpret_cast<uint2 *>(sA16 + tc_off16(r, k4) / 2) = pk;
-            }
-            for (int q = tid; q < kTcN * (kTcK / 4); q += kThreads) {
-                const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
-                const int c = c0 + n;
-                const bool inJ = c >= j0 && c < j0 + kWPB;
-                uint16_t h[4];
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    const int k = k4 + b;
-                    float x = 0.f;
-                    if (k < pb && c < ld) {
-                        if (inJ) x = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : 0.f;
-                        else x = W.PR[(int64_t)k * ld + c];
-                    }
-                    h[b] = bf16_bits(x);
-                }
-                uint2 pk;
-                pk.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
-                pk.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
-                *reinterpret_cast<uint2 *>(sB16 + tc_off16(n, k4) / 2) = pk;
-            }
-        } else {
-        for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
-            const int r = q >> 3, k4 = (q & 7) * 4;
-            float v[4];
-            panel4(r, k4, v);
-            float h[4], l[4];
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                h[b] = tf32_hi(v[b]);
-                l[b] = v[b] - h[b];
-            }
-            const int o = tc_off(r, k4) / 4;
-            store4(sAh + o, h);
-            store4(sAl + o, l);
-        }
-        for (int q = tid; q < kTcN * (kTcK / 4); q += kThreads) {
-            const int n = q & (kTcN - 1), k4 = (q / kTcN) * 4;
-            const int c = c0 + n;
-            const bool inJ = c >= j0 && c < j0 + kWPB;
-            float h[4], l[4];
-#pragma unroll
-            for (int b = 0; b < 4; b++) {
-                const int k = k4 + b;
-                float x = 0.f;
-                if (k < pb && c < ld) {
-                    if (inJ) x = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : 0.f;
-                    else x = W.PR[(int64_t)k * ld + c];
-                }
-                h[b] = tf32_hi(x);
-                l[b] = x - h[b];
-            }
-            const int o = tc_off(n, k4) / 4;
-            store4(sBh + o, h);
-            store4(sBl + o, l);
-        }
-        }
-        tc_proxy_fence();
-        __syncthreads();
-        float out[32];
-        ok = bf16 ? tc_tile_product_bf16(sA16, sB16, W.tc_bar, W.tc_tmem, phase, out)
-                  : tc_tile_product(sAh, sAl, sBh, sBl, W.tc_bar, W.tc_tmem, phase, out);
-        if (!ok) break;
-        const int w = tid >> 5;
-        const int row = r0 + (w & 3) * 32 + (tid & 31), cb = c0 + (w >> 2) * 32;
-        if (row < N && cb < ld) {
-            const int pr = W.pos[row];
-            float *dst = W.A + (int64_t)row * ld;
-#pragma unroll
-            for (int g = 0; g < 8; g++) {
-                const int c = cb + 4 * g;
-                if (c >= ld) break;
-                const bool inJ = c >= j0 && c < j0 + kWPB;
-                float v[4];
-                if (pr >= 0) {
-#pragma unroll
-                    for (int b = 0; b < 4; b++)
-                        v[b] = inJ ? ((c + b - j0 < pb) ? W.Dinv[pr * kWPB + (c + b - j0)] : 0.f)
-                                   : W.PR[(int64_t)pr * ld + c + b];
-                } else {
-                    if (inJ) {
-#pragma unroll
-                        for (int b = 0; b < 4; b++) v[b] = 0.f;
-                    } else {
-                        load4(dst + c, v);
-                    }
-#pragma unroll
-                    for (int b = 0; b < 4; b++) v[b] -= out[4 * g + b];
-                }
-                store4(dst + c, v);
-            }
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        *W.tc_phase = phase;
-        if (!ok) atomicExch(&W.ctl->abort, 1);
-    }
-    __syncthreads();
-    return ok;
 }
 
 // ---------------------------------------------------------------- super-panel
@@ -588,7 +445,8 @@ __device__ void task_panel_s(const WideWs<LT> &W, int s0, int sw, LT *smem) {
 }
 
 // The rank-kWSP update of every column tile but S's, on the FP32 (or FP64)
-// pipes: task_update's tiles with K in chunks of kWPB.
+// pipes: 128 x 128 tiles, thread (ty, tx) owning rows ty*8.. and columns
+// tx*4.., K in chunks of kWPB staged in shared memory.
 template <typename LT>
 __device__ void task_update_s(const WideWs<LT> &W, int s0, int sw, LT *smem) {
     constexpr int AS = kWT + 4;
@@ -650,9 +508,12 @@ __device__ void task_update_s(const WideWs<LT> &W, int s0, int sw, LT *smem) {
 }
 
 // task_update_s on the tensor cores: per 128 x 128 tile, K chunks of kTcK
-// staged as task_update_tc stages its operands (A from AJS, B from PRS),
-// accumulated in tensor memory, read back once.  False if a tensor-core wait
-// ran out (the control block's abort flag is then set).
+// with A = AJS rows and B = PRS columns split into TF32 high and low parts
+// (W.tc_on == 2: rounded to BF16) in the canonical K-major layout,
+// accumulated in tensor memory, read back once; each thread finishes 32
+// entries of its row (pivot rows of S take PRS, the rest subtract).  False
+// if a tensor-core wait ran out (the control block's abort flag is then
+// set).
 __device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *smem) {
     float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
     uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
@@ -1084,15 +945,7 @@ __device__ void wide_worker(const WideWs<LT> &W, const Net &m, double *mdiag, un
         gen++;
         switch (s_task) {
         case kTaskAssemble: task_assemble<LT>(W, m, s_x, s_h, mdiag); break;
-        case kTaskUpdate:
-            if constexpr (std::is_same<LT, float>::value) {
-                if (W.tc_on) {
-                    task_update_tc(W, s_j0, s_pb, sm, W.ctl->pad0);
-                    break;
-                }
-            }
-            task_update<LT>(W, s_j0, s_pb, sm, W.ctl->pad0);
-            break;
+        case kTaskUpdate: task_update_narrow<LT>(W, s_j0, s_pb, sm, W.ctl->pad0); break;
         case kTaskPanelS: task_panel_s<LT>(W, s_j0, s_pb, sm); break;
         case kTaskUpdateS:
             if constexpr (std::is_same<LT, float>::value) {
@@ -1287,14 +1140,7 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
                 tick(0);
                 if (tid == 0) W.ctl->pad0 = s0;
                 wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
-                bool tc_done = false;
-                if constexpr (std::is_same<LT, float>::value) {
-                    if (W.tc_on) {
-                        task_update_tc(W, j0, pb, sm, s0);
-                        tc_done = true;
-                    }
-                }
-                if (!tc_done) task_update<LT>(W, j0, pb, sm, s0);
+                task_update_narrow<LT>(W, j0, pb, sm, s0);
                 if (!wide_join<LT>(W, limit, sflag)) return 2;
                 tick(2);
             }
