@@ -7,10 +7,10 @@ the oracle, so the trajectories are stored:
     minutes on one core);
   * c3_t05: the same network on t in [0, 0.5] (11 samples, about fifty
     backward-Euler steps, tens of minutes);
-  * c2_t01: the stiff 512-species network on t in [0, 0.1] (6 samples; the
-    step stays near 4.5e-6, so about 22 000 backward-Euler steps with a
-    512 x 512 LU each -- its whole horizon t in [0, 100] would take the
-    oracle days on one core);
+  * c2_t01: the stiff 512-species network on t in [0, 0.1] (6 samples;
+    three negative-species reverts take the backward-Euler step to 1e-5, so
+    8 893 steps with a 512 x 512 LU each, fifteen minutes -- its whole
+    horizon t in [0, 100] would take the oracle days on one core);
   * c5_full: the 256-species adjoint network (base rate constants) over its
     whole horizon, 40 samples in (0, 10].
 

@@ -5,9 +5,9 @@
   (40 samples, 1000 backward-Euler steps): the FP64 form bit for bit with
   the oracle's step counts; the mixed form within the oracle's spread (this
   network's RKF45 steps after backward-Euler stretches depend on last bits);
-* the stiff 512-species network on t in [0, 0.1] (about 22 000
-  backward-Euler steps at its step of 4.5e-6; its whole horizon would take
-  the oracle days): the FP64 form bit for bit, the mixed form within
+* the stiff 512-species network on t in [0, 0.1] (8 893 backward-Euler
+  steps after three reverts take the step to 1e-5; its whole horizon would
+  take the oracle days): the FP64 form bit for bit, the mixed form within
   rtol 1e-6 / atol 1e-9 with the oracle's step counts;
 * the 4096-species network on t in [0, 0.5] (11 samples) on the wide
   engine: within rtol 1e-6 / atol 1e-9 with the oracle's backward-Euler
