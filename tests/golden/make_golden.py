@@ -7,7 +7,8 @@ reference binary needs a CUDA GPU, so this runs on the GPU machine:
 
     python tests/golden/make_golden.py <out_dir> [--float]
 
-(--float: the reference's -p float runs, stored under tests/golden/float/).
+(--float: the reference's -p float runs, stored under tests/golden/float/;
+--long: two longer horizons, stored under tests/golden/long/).
 
 Each fixture holds the dense stoichiometries, rate constants, initial state,
 sampling times, the reference's trajectory (``ref``), its number of loop
@@ -34,6 +35,15 @@ from lassie_gb300.model import write_folder  # noqa: E402
 REF = os.path.join(ROOT, "oracle", "_ref", "lassie_ref_f64")
 
 
+def long_cases():
+    """Longer horizons, stored under tests/golden/long/ (--long): the same
+    networks and samples as tests/oracle_fixtures/c2_t01.npz and
+    c3_t05.npz, so that the stored oracle trajectories are checked against
+    the reference without running either."""
+    yield "c2_t01", synth.shorten(synth.make_c2(), 0.1, 6)
+    yield "c3_t05", synth.shorten(synth.make_c3(), 0.5, 11)
+
+
 def cases():
     yield "c1", synth.make_c1()
     for kind in ("decay", "conversion", "dimer", "bimolecular", "source", "reversible"):
@@ -56,12 +66,13 @@ def read_solution(path: str, ncols: int) -> np.ndarray:
     return np.asarray(rows)
 
 
-def main(out_dir: str, precision: str = "double") -> int:
-    """precision "float": the reference's -p float runs (Simulation<float>)."""
+def main(out_dir: str, precision: str = "double", long: bool = False) -> int:
+    """precision "float": the reference's -p float runs (Simulation<float>);
+    long: the longer-horizon cases instead of the standard set."""
     os.makedirs(out_dir, exist_ok=True)
     status = 0
     extra = ["-p", "float"] if precision == "float" else []
-    for name, m in cases():
+    for name, m in (long_cases() if long else cases()):
         with tempfile.TemporaryDirectory() as tmp:
             inp, outp = os.path.join(tmp, "in"), os.path.join(tmp, "out")
             write_folder(m, inp)
@@ -91,7 +102,9 @@ def main(out_dir: str, precision: str = "double") -> int:
 
 
 if __name__ == "__main__":
-    args = [a for a in sys.argv[1:] if a != "--float"]
+    args = [a for a in sys.argv[1:] if a not in ("--float", "--long")]
     prec = "float" if "--float" in sys.argv[1:] else "double"
-    default = os.path.join(ROOT, "tests", "golden", "float" if prec == "float" else "")
-    sys.exit(main(args[0] if args else default, prec))
+    long = "--long" in sys.argv[1:]
+    sub = "float" if prec == "float" else ("long" if long else "")
+    default = os.path.join(ROOT, "tests", "golden", sub)
+    sys.exit(main(args[0] if args else default, prec, long))

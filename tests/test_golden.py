@@ -188,3 +188,30 @@ def test_float_oracle_against_the_reference_float_mode(name):
     e = fexcess(d["ref"], base)
     assert np.all(e[:first] <= 0), (first, e)
     assert e.max() <= 2 * worst, (float(e.max()), worst)
+
+
+# ------------------------------------------------ longer horizons
+LONG_DIR = os.path.join(HERE, "long")
+FIXTURES = os.path.join(os.path.dirname(HERE), "oracle_fixtures")
+
+
+def long_cases():
+    return sorted(os.path.basename(f)[:-4] for f in glob.glob(os.path.join(LONG_DIR, "*.npz")))
+
+
+@pytest.mark.parametrize("name", long_cases())
+def test_stored_oracle_trajectory_matches_the_reference(name):
+    """The reference binary's run (tests/golden/long/, make_golden.py --long)
+    against the oracle's stored trajectory of the same network and samples
+    (tests/oracle_fixtures/, make_oracle_fixtures.py): C2 over 8 893
+    backward-Euler steps and C3 over 50 with 4096 x 4096 factorisations,
+    within rtol 1e-6 / atol 1e-9 at every sample.  Nothing is integrated
+    here: both runs take minutes to an hour."""
+    d = np.load(os.path.join(LONG_DIR, name + ".npz"))
+    f = np.load(os.path.join(FIXTURES, name + ".npz"))
+    assert int(f["status"]) == 0
+    assert np.array_equal(d["ref_t"], f["t"]) and np.array_equal(d["t"], f["t"])
+    ref, out = d["ref"], f["out"]
+    assert ref.shape == out.shape
+    assert np.all(np.abs(out - ref) <= ATOL + RTOL * np.abs(ref)), \
+        float(np.max(np.abs(out - ref) / np.maximum(np.abs(ref), ATOL)))
