@@ -330,6 +330,52 @@ def lsoda_baseline(n_total, stride=128, threads=None):
             "cpu_seconds_per_instance": sum(t for t, _ in res) / len(res)}
 
 
+def _lsoda_c3_child(t_reached, cap_s):
+    """Child process of lsoda_c3: odeint interval by interval over the C3
+    sample times, publishing the time reached after each interval."""
+    import warnings
+    from scipy.integrate import odeint
+    from lassie_gb300 import synth
+    from oracle import oracle as O
+    m = synth.make_c3()
+    om = O.OracleModel(m.left, m.right)
+    x = m.x0.copy()
+    t0 = time.perf_counter()
+    for i in range(1, len(m.t)):
+        if time.perf_counter() - t0 > cap_s:
+            return
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            ys = odeint(lambda y, t: om.rhs(m.k, y), x, [m.t[i - 1], m.t[i]],
+                        Dfun=lambda y, t: om.jacobian_exact(m.k, y), rtol=1e-6, atol=1e-12,
+                        mxstep=10000)
+        x = ys[-1]
+        t_reached.value = float(m.t[i])
+
+
+def lsoda_c3(cap_s=120.0):
+    """The CPU baseline's C3 figure: scipy LSODA (odeint, analytic dense
+    4096 x 4096 Jacobian, rtol 1e-6, atol 1e-12) on one core, stopped at a
+    wall-clock cap (a spawned child, ended by its own PID when an interval
+    outlasts the cap).  Reports how far it got."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    reached = ctx.Value("d", 0.0)
+    p = ctx.Process(target=_lsoda_c3_child, args=(reached, cap_s))
+    t0 = time.perf_counter()
+    p.start()
+    p.join(cap_s + 30.0)
+    if p.is_alive():
+        p.terminate()
+        p.join()
+    wall = time.perf_counter() - t0
+    t_end = 50.0
+    return {"kind": "scipy LSODA (odeint, analytic dense Jacobian, rtol 1e-6, atol 1e-12), "
+                    "one core", "cap_s": cap_s, "t_reached": reached.value, "t_end": t_end,
+            "capped": reached.value < t_end, "seconds": wall,
+            "sims_per_s_extrapolated": (reached.value / t_end) / wall if reached.value > 0 else 0.0}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -646,6 +692,8 @@ def run_c3(args):
                          "kernel_ms": k_ms, "algorithmic_flops_per_launch": flops,
                          "peak_kind": f"{peak_kind} bf16 sustained"},
             "clocks": clocks.summary()}
+    if not args.no_extras:
+        line["cpu_lsoda"] = lsoda_c3()
     print(json.dumps(line), flush=True)
     return 0
 
