@@ -12,7 +12,8 @@
 // The Newton matrix M = I - h*J is inverted in place by blocked Gauss-Jordan
 // elimination with partial pivoting (row pivots, kWPB-column panels): per
 // panel, the pivot block D (rows p_j0.., columns J) is inverted by the leader,
-// which also forms PR = D^-1 * M[P_J, C], and all CTAs apply
+// and all CTAs form PR = D^-1 * M[P_J, C] from the leader's copy of the pivot
+// rows and apply
 //     M[i, C] -= M[i, J] * PR[:, C]   (i not a pivot row, C not in J)
 //     M[i, J]  = -M[i, J] * D^-1,   M[P_J, C] = PR,   M[P_J, J] = D^-1.
 // The panels of one kWSP-column super-panel S restrict C to S's columns;
@@ -74,7 +75,7 @@ struct WideWs {
     LT *PN;           // [kWPB][N] scratch; its first 2N ints are the pivot candidate lists
     int *cand;        // [2][N] candidate rows of the pivot search (two lists, alternating)
     LT *Dinv;         // [kWPB][kWPB]
-    LT *PR;           // [kWPB][ld]
+    LT *SNAP;         // [kWPB][kWSP] the panel's pivot rows in the super-panel's tile
     LT *AJS;          // [N][kWSP] super-panel columns before its panels
     LT *PRS;          // [kWSP][ld] DS^-1 * M[P_S, :] (DS: the super-panel's pivot block)
     LT *vin, *vout;   // [N] matrix-vector product input (gathered) and output
@@ -89,7 +90,7 @@ struct WideWs {
 };
 
 struct WideLayout {
-    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, PR, AJS, PRS, vin, vout, flags, part,
+    int64_t ctl, vec, pw, qr, A, piv, pos, used, PN, Dinv, SNAP, AJS, PRS, vin, vout, flags, part,
         total;
     __host__ __device__ static int64_t al(int64_t v) { return (v + 255) & ~int64_t(255); }
     __host__ __device__ WideLayout(int N, int R, int nnz_a, int lt) {
@@ -105,7 +106,7 @@ struct WideLayout {
         used = o;  o = al(o + int64_t(N) * 4);
         PN = o;    o = al(o + int64_t(kWPB) * N * lt);
         Dinv = o;  o = al(o + int64_t(kWPB) * kWPB * lt);
-        PR = o;    o = al(o + int64_t(kWPB) * ld * lt);
+        SNAP = o;  o = al(o + int64_t(kWPB) * kWSP * lt);
         AJS = o;   o = al(o + int64_t(N) * kWSP * lt);
         PRS = o;   o = al(o + int64_t(kWSP) * ld * lt);
         vin = o;   o = al(o + int64_t(N) * lt);
@@ -131,7 +132,7 @@ __device__ WideWs<LT> wide_ws(unsigned char *base, int N, int R, int nnz_a) {
     W.PN = reinterpret_cast<LT *>(base + L.PN);
     W.cand = reinterpret_cast<int *>(base + L.PN);
     W.Dinv = reinterpret_cast<LT *>(base + L.Dinv);
-    W.PR = reinterpret_cast<LT *>(base + L.PR);
+    W.SNAP = reinterpret_cast<LT *>(base + L.SNAP);
     W.AJS = reinterpret_cast<LT *>(base + L.AJS);
     W.PRS = reinterpret_cast<LT *>(base + L.PRS);
     W.vin = reinterpret_cast<LT *>(base + L.vin);
@@ -272,28 +273,15 @@ __device__ void task_assemble(const WideWs<LT> &W, const Net &m, const double *x
     }
 }
 
-// Leader: PR = D^-1 * M[P_J, C] for the columns C of the super-panel's tile
-// (s0 ..) outside J, by (group of 4 pivot rows, column); D^-1 staged in sD.
+// Leader: SNAP = M[P_J, C] for the columns C of the super-panel's tile, the
+// panel's pivot rows before the panel's update (the update's CTAs form
+// PR = D^-1 * SNAP from it; the CTAs that own pivot rows overwrite them).
 template <typename LT>
-__device__ void leader_panel_pr(const WideWs<LT> &W, int j0, int pb, int s0, LT *sD) {
-    const int tid = threadIdx.x, ld = W.ld;
-    for (int q = tid; q < kWPB * kWPB; q += kThreads) sD[q] = W.Dinv[q];
-    __syncthreads();
-    const int cw = min(s0 + kWSP, ld) - s0;
-    for (int q = tid; q < (kWPB / 4) * cw; q += kThreads) {
-        const int g = q / cw, c = s0 + (q - g * cw);
-        if (c >= j0 && c < j0 + kWPB) continue;
-        LT a[kWPB];
-#pragma unroll
-        for (int k = 0; k < kWPB; k++) a[k] = (k < pb) ? W.A[(int64_t)W.piv[j0 + k] * ld + c] : LT(0);
-#pragma unroll
-        for (int rr = 0; rr < 4; rr++) {
-            const int r = g * 4 + rr;
-            LT acc = LT(0);
-#pragma unroll
-            for (int k = 0; k < kWPB; k++) acc = lt_fma(sD[r * kWPB + k], a[k], acc);
-            W.PR[(int64_t)r * ld + c] = acc;
-        }
+__device__ void leader_snapshot(const WideWs<LT> &W, int j0, int pb, int s0) {
+    const int ld = W.ld;
+    for (int q = threadIdx.x; q < kWPB * kWSP; q += kThreads) {
+        const int k = q / kWSP, c = s0 + (q - k * kWSP);
+        W.SNAP[q] = (k < pb && c < ld) ? W.A[(int64_t)W.piv[j0 + k] * ld + c] : LT(0);
     }
     __syncthreads();
 }
@@ -330,10 +318,38 @@ template <typename LT>
 __device__ void task_update_narrow(const WideWs<LT> &W, int j0, int pb, LT *smem, int s0) {
     static_assert(kNarrowRows == 2 * kWarps && kWT == 4 * 32, "2 rows x 4 columns a thread");
     LT *sAJ = smem;                       // [kWPB][kNarrowRows]: panel columns, K-major
-    LT *sB = smem + kWPB * kNarrowRows;   // [kWPB][kWT]
+    LT *sB = smem + kWPB * kNarrowRows;   // [kWPB][kWT]: [PR | D^-1] over the tile's columns
+    LT *sD = sB + kWPB * kWT;             // [kWPB][kWPB]: D^-1
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const int N = W.N, ld = W.ld;
     const int nrt = (N + kNarrowRows - 1) / kNarrowRows;
+    if ((int)blockIdx.x < nrt) {
+        // B = [PR | D^-1] with PR = D^-1 * SNAP, formed by every CTA with
+        // tiles (the same products in the same order in each)
+        for (int q = tid; q < kWPB * kWPB; q += kThreads) sD[q] = W.Dinv[q];
+        __syncthreads();
+        for (int q = tid; q < (kWPB / 4) * kWT; q += kThreads) {
+            const int g = q / kWT, cc = q - g * kWT, c = s0 + cc;
+            const bool inJ = c >= j0 && c < j0 + kWPB;
+            LT a[kWPB];
+#pragma unroll
+            for (int k = 0; k < kWPB; k++) a[k] = W.SNAP[k * kWSP + cc];
+#pragma unroll
+            for (int rr = 0; rr < 4; rr++) {
+                const int r = g * 4 + rr;
+                LT v = LT(0);
+                if (r < pb && c < ld) {
+                    if (inJ) {
+                        v = (c - j0 < pb) ? sD[r * kWPB + (c - j0)] : LT(0);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < kWPB; k++) v = lt_fma(sD[r * kWPB + k], a[k], v);
+                    }
+                }
+                sB[r * kWT + cc] = v;
+            }
+        }
+    }
     for (int t = blockIdx.x; t < nrt; t += gridDim.x) {
         const int r0 = t * kNarrowRows, c0 = s0;
         __syncthreads();
@@ -343,16 +359,6 @@ __device__ void task_update_narrow(const WideWs<LT> &W, int j0, int pb, LT *smem
             const int r = q / kWPB, k = q - r * kWPB;
             sAJ[k * kNarrowRows + r] =
                 (r0 + r < N && k < pb) ? W.A[(int64_t)(r0 + r) * ld + j0 + k] : LT(0);
-        }
-        for (int q = tid; q < kWPB * kWT; q += kThreads) {
-            const int k = q / kWT, cc = q - k * kWT;
-            const int c = c0 + cc;
-            LT v = LT(0);
-            if (k < pb && c < ld) {
-                if (c >= j0 && c < j0 + kWPB) v = (c - j0 < pb) ? W.Dinv[k * kWPB + (c - j0)] : LT(0);
-                else v = W.PR[(int64_t)k * ld + c];
-            }
-            sB[q] = v;
         }
         __syncthreads();
         const int col = c0 + tx * 4;
@@ -1094,7 +1100,6 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
                            int *ired, uint64_t limit, int *sflag, long long *cyc) {
     const int tid = threadIdx.x, N = W.N;
     LT *sm = reinterpret_cast<LT *>(smem);
-    LT *sD = sm + wide_smem_bytes(N, (int)sizeof(LT)) / (int)sizeof(LT) - kWPB * kWPB;
     bool use_old = !fresh && ld_acquire_i(W.flags) != 0;
     long long c0 = clock64(), c1;
     auto tick = [&](int slot) {
@@ -1136,7 +1141,7 @@ __device__ int wide_factor(const WideWs<LT> &W, const Net &m, const double *x, d
                     ok = false;
                     break;
                 }
-                leader_panel_pr<LT>(W, j0, pb, s0, sD);
+                leader_snapshot<LT>(W, j0, pb, s0);
                 tick(0);
                 if (tid == 0) W.ctl->pad0 = s0;
                 wide_fork<LT>(W, kTaskUpdate, j0, pb, h, x);
