@@ -162,7 +162,8 @@ __host__ __device__ constexpr int64_t tour_smem_bytes(int lt) {
 // largest, plus the pivot-block inverse.
 __host__ __device__ inline int64_t wide_smem_bytes(int N, int lt) {
     int64_t tiles = (int64_t(kWPB) * (kWT + 4) + int64_t(kWPB) * kWT) * lt;
-    if (lt == 4 && tiles < 4 * kWT * kWPB * 4) tiles = 4 * kWT * kWPB * 4;  // tensor-core operands
+    // tensor-core operands: two split-TF32 sets (staging overlaps the MMAs)
+    if (lt == 4 && tiles < 2 * 4 * kWT * kWPB * 4) tiles = 2 * 4 * kWT * kWPB * 4;
     const int64_t vin = int64_t((N + 3) & ~3) * lt;
     int64_t big = tiles > vin ? tiles : vin;
     if (big < tour_smem_bytes(lt)) big = tour_smem_bytes(lt);
@@ -521,8 +522,8 @@ __device__ void task_update_s(const WideWs<LT> &W, int s0, int sw, LT *smem) {
 // if a tensor-core wait ran out (the control block's abort flag is then
 // set).
 __device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *smem) {
-    float *sAh = smem, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK, *sBl = sBh + kTcN * kTcK;
-    uint16_t *sA16 = reinterpret_cast<uint16_t *>(smem), *sB16 = sA16 + kTcM * kTcK;
+    // two operand buffers: chunk k+1 is staged while the MMAs of chunk k run
+    constexpr int kSet = 2 * kTcM * kTcK + 2 * kTcN * kTcK;  // floats of one split set
     const bool bf16 = W.tc_on == 2;
     const int tid = threadIdx.x;
     const int N = W.N, ld = W.ld;
@@ -532,8 +533,11 @@ __device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *
     for (int t = blockIdx.x; nct > 1 && t < nrt * (nct - 1) && ok; t += gridDim.x) {
         const int ct = t % (nct - 1);
         const int r0 = (t / (nct - 1)) * kTcM, c0 = (ct < st ? ct : ct + 1) * kTcN;
-        for (int k0 = 0; k0 < sw && ok; k0 += kTcK) {
+        // chunk k0 of A = AJS rows and B = PRS columns into buffer set `b`
+        auto stage = [&](int k0, int b) {
+            float *base = smem + b * kSet;
             if (bf16) {
+                uint16_t *sA16 = reinterpret_cast<uint16_t *>(base), *sB16 = sA16 + kTcM * kTcK;
                 for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
                     const int r = q >> 3, k4 = (q & 7) * 4;
                     float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -548,23 +552,25 @@ __device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *
                     const int c = c0 + n;
                     uint16_t h[4];
 #pragma unroll
-                    for (int b = 0; b < 4; b++)
-                        h[b] = bf16_bits(c < ld ? W.PRS[(int64_t)(k0 + k4 + b) * ld + c] : 0.f);
+                    for (int e = 0; e < 4; e++)
+                        h[e] = bf16_bits(c < ld ? W.PRS[(int64_t)(k0 + k4 + e) * ld + c] : 0.f);
                     uint2 pk;
                     pk.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
                     pk.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
                     *reinterpret_cast<uint2 *>(sB16 + tc_off16(n, k4) / 2) = pk;
                 }
             } else {
+                float *sAh = base, *sAl = sAh + kTcM * kTcK, *sBh = sAl + kTcM * kTcK,
+                      *sBl = sBh + kTcN * kTcK;
                 for (int q = tid; q < kTcM * (kTcK / 4); q += kThreads) {
                     const int r = q >> 3, k4 = (q & 7) * 4;
                     float v[4] = {0.f, 0.f, 0.f, 0.f};
                     if (r0 + r < N) load4(W.AJS + (int64_t)(r0 + r) * kWSP + k0 + k4, v);
                     float h[4], l[4];
 #pragma unroll
-                    for (int b = 0; b < 4; b++) {
-                        h[b] = tf32_hi(v[b]);
-                        l[b] = v[b] - h[b];
+                    for (int e = 0; e < 4; e++) {
+                        h[e] = tf32_hi(v[e]);
+                        l[e] = v[e] - h[e];
                     }
                     const int o = tc_off(r, k4) / 4;
                     store4(sAh + o, h);
@@ -575,10 +581,10 @@ __device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *
                     const int c = c0 + n;
                     float h[4], l[4];
 #pragma unroll
-                    for (int b = 0; b < 4; b++) {
-                        const float x = c < ld ? W.PRS[(int64_t)(k0 + k4 + b) * ld + c] : 0.f;
-                        h[b] = tf32_hi(x);
-                        l[b] = x - h[b];
+                    for (int e = 0; e < 4; e++) {
+                        const float x = c < ld ? W.PRS[(int64_t)(k0 + k4 + e) * ld + c] : 0.f;
+                        h[e] = tf32_hi(x);
+                        l[e] = x - h[e];
                     }
                     const int o = tc_off(n, k4) / 4;
                     store4(sBh + o, h);
@@ -587,9 +593,26 @@ __device__ bool task_update_s_tc(const WideWs<float> &W, int s0, int sw, float *
             }
             tc_proxy_fence();
             __syncthreads();
-            ok = bf16 ? tc_chunk_mma_bf16(sA16, sB16, W.tc_bar, W.tc_tmem, phase, k0 > 0)
-                      : tc_chunk_mma(sAh, sAl, sBh, sBl, W.tc_bar, W.tc_tmem, phase, k0 > 0);
+        };
+        auto issue = [&](int b, bool acc) {
+            float *base = smem + b * kSet;
+            if (bf16) {
+                const uint16_t *sA16 = reinterpret_cast<const uint16_t *>(base);
+                tc_chunk_issue_bf16(sA16, sA16 + kTcM * kTcK, W.tc_bar, W.tc_tmem, acc);
+            } else {
+                tc_chunk_issue(base, base + kTcM * kTcK, base + 2 * kTcM * kTcK,
+                               base + 2 * kTcM * kTcK + kTcN * kTcK, W.tc_bar, W.tc_tmem, acc);
+            }
+        };
+        stage(0, 0);
+        issue(0, false);
+        int kc = 1;
+        for (int k0 = kTcK; k0 < sw && ok; k0 += kTcK, kc++) {
+            stage(k0, kc & 1);                     // while chunk kc-1 multiplies
+            ok = tc_chunk_wait(W.tc_bar, phase);  // chunk kc-1 done: its buffer is free
+            if (ok) issue(kc & 1, true);
         }
+        if (ok) ok = tc_chunk_wait(W.tc_bar, phase);
         if (!ok) break;
         float out[32];
         tc_tile_read(W.tc_tmem, out);
