@@ -129,3 +129,18 @@ def test_wide_c3_full_horizon_conserves_total_amount(gpu, tensor_cores):
     total = out.sum(axis=1)
     assert np.all(np.abs(total - m.x0.sum()) <= 1e-10 * m.x0.sum()), \
         float(np.max(np.abs(total - m.x0.sum())))
+
+
+def test_wide_two_level_tournament(gpu):
+    """4200 species: the first panel's 4200 candidate rows make 33 groups of
+    128 and 1056 survivors, more than one CTA holds (1024), so the FP32 pivot
+    search takes a second tournament level (the FP64 form, 512 a CTA, takes
+    three).  The FP64 form (Gauss-Jordan in FP64, no refinement) and the
+    mixed form agree within rtol 1e-6 / atol 1e-9 with the same step
+    counts."""
+    m = synth.shorten(synth.make_sized(4200, 0), 0.02, 3)
+    o64, s64 = solver.simulate(m, engine="fp64", deadline_s=900, root="sqrt")
+    omx, smx = solver.simulate(m, engine="mixed", deadline_s=900, root="sqrt")
+    assert s64["status"] == 0 == smx["status"]
+    assert within(omx, o64), float(np.max(np.abs(omx - o64) - RTOL * np.abs(o64)))
+    assert (s64["be_steps"], s64["rkf_accepts"]) == (smx["be_steps"], smx["rkf_accepts"])
