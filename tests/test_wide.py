@@ -142,5 +142,8 @@ def test_wide_two_level_tournament(gpu):
     o64, s64 = solver.simulate(m, engine="fp64", deadline_s=900, root="sqrt")
     omx, smx = solver.simulate(m, engine="mixed", deadline_s=900, root="sqrt")
     assert s64["status"] == 0 == smx["status"]
+    assert s64["lu_factorisations"] >= 1 and smx["lu_factorisations"] >= 1
     assert within(omx, o64), float(np.max(np.abs(omx - o64) - RTOL * np.abs(o64)))
     assert (s64["be_steps"], s64["rkf_accepts"]) == (smx["be_steps"], smx["rkf_accepts"])
+    print(f"4200 species: {s64['be_steps']} backward-Euler steps, "
+          f"{s64['lu_factorisations']} FP64 and {smx['lu_factorisations']} FP32 inversions")
