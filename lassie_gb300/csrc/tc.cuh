@@ -230,68 +230,15 @@ __device__ __forceinline__ bool tc_tile_product(const float *sAh, const float *s
 }
 
 // Deeper products D = sum over K chunks of A_c * B_c (K = 32 per chunk), the
-// accumulator staying in tensor memory: the caller stages each chunk's split
-// operands as for tc_tile_product, makes them visible to the tensor core,
-// and calls tc_chunk_mma (first chunk: accumulate = false), which issues the
-// chunk's MMAs, waits for them (bounded) and flips phase; the chunk's
-// shared-memory operands may then be overwritten.  tc_tile_read reads the
-// product back (same thread-to-entry map as tc_tile_product).  Both return
-// (uniformly) false when a wait ran out.
-__device__ __forceinline__ bool tc_chunk_mma(const float *sAh, const float *sAl,
-                                             const float *sBh, const float *sBl, uint64_t *bar,
-                                             uint32_t tmem, uint32_t &phase, bool accumulate) {
-    if (threadIdx.x == 0) {
-        tc_fence_after();
-        const uint32_t idesc = tc_idesc_tf32(kTcN);
-        const uint32_t sbo = (kTcK / 4) * 128;
-        uint32_t acc = accumulate ? 1u : 0u;
-#pragma unroll
-        for (int ks = 0; ks < kTcK / 8; ks++) {
-            const uint32_t koff = ks * 2 * 128;
-            const uint64_t ah = tc_desc(smem_u32(sAh) + koff, 128, sbo);
-            const uint64_t al = tc_desc(smem_u32(sAl) + koff, 128, sbo);
-            const uint64_t bh = tc_desc(smem_u32(sBh) + koff, 128, sbo);
-            const uint64_t bl = tc_desc(smem_u32(sBl) + koff, 128, sbo);
-            tc_mma_tf32(tmem, ah, bh, idesc, acc);
-            acc = 1;
-            tc_mma_tf32(tmem, ah, bl, idesc, 1);
-            tc_mma_tf32(tmem, al, bh, idesc, 1);
-        }
-        tc_commit(bar);
-    }
-    const bool ok = tc_mbar_wait(bar, phase);
-    tc_fence_after();
-    phase ^= 1u;
-    return __syncthreads_and(ok) != 0;
-}
-
-__device__ __forceinline__ bool tc_chunk_mma_bf16(const uint16_t *sA, const uint16_t *sB,
-                                                  uint64_t *bar, uint32_t tmem, uint32_t &phase,
-                                                  bool accumulate) {
-    if (threadIdx.x == 0) {
-        tc_fence_after();
-        const uint32_t idesc = tc_idesc_bf16(kTcN);
-        const uint32_t sbo = (kTcK / 8) * 128;
-#pragma unroll
-        for (int ks = 0; ks < kTcK / 16; ks++) {
-            const uint32_t koff = ks * 2 * 128;
-            const uint64_t a = tc_desc(smem_u32(sA) + koff, 128, sbo);
-            const uint64_t b = tc_desc(smem_u32(sB) + koff, 128, sbo);
-            tc_mma_f16(tmem, a, b, idesc, (accumulate || ks > 0) ? 1u : 0u);
-        }
-        tc_commit(bar);
-    }
-    const bool ok = tc_mbar_wait(bar, phase);
-    tc_fence_after();
-    phase ^= 1u;
-    return __syncthreads_and(ok) != 0;
-}
-
-// The two halves of tc_chunk_mma, for a caller that stages the next chunk
-// into another buffer while the tensor core works on this one: thread 0
-// issues the chunk's MMAs and commits them (tc_chunk_issue*), every thread
-// later waits for that commit (tc_chunk_wait: bounded, flips phase,
-// uniformly false if the wait ran out).
+// accumulator staying in tensor memory.  The caller stages each chunk's
+// operands as for tc_tile_product and makes them visible to the tensor core;
+// thread 0 issues the chunk's MMAs and commits them (tc_chunk_issue*, first
+// chunk: accumulate = false); every thread later waits for that commit
+// (tc_chunk_wait: bounded, flips phase, uniformly false if the wait ran out),
+// after which the chunk's shared-memory operands may be overwritten -- so a
+// caller with two operand buffers stages the next chunk while the tensor
+// core works on this one.  tc_tile_read reads the product back (same
+// thread-to-entry map as tc_tile_product).
 __device__ __forceinline__ void tc_chunk_issue(const float *sAh, const float *sAl,
                                                const float *sBh, const float *sBl, uint64_t *bar,
                                                uint32_t tmem, bool accumulate) {
