@@ -10,8 +10,8 @@
   take the oracle days): the FP64 form bit for bit, the mixed form within
   rtol 1e-6 / atol 1e-9 with the oracle's step counts;
 * the 4096-species network on t in [0, 0.5] (11 samples) on the wide
-  engine: within rtol 1e-6 / atol 1e-9 with the oracle's backward-Euler
-  steps.
+  engine, with each of its rank-update modes: within rtol 1e-6 / atol 1e-9
+  with the oracle's backward-Euler steps.
 """
 import os
 
@@ -69,11 +69,15 @@ def test_c2_to_a_tenth_time_unit(gpu):
     assert sx["be_steps"] == int(d["be_steps"])
 
 
-def test_c3_to_half_time_unit(gpu):
+@pytest.mark.parametrize("mode", ["tf32", "bf16", "off"])
+def test_c3_to_half_time_unit(gpu, mode):
+    """Rank updates on the tensor cores with split-TF32 (the default) or BF16
+    operands, or on the FP32 pipes: the same trajectory and steps."""
     d = fixture("c3_t05")
     m = synth.shorten(synth.make_c3(), 0.5, 11)
     assert np.array_equal(m.t, d["t"])
-    out, st = solver.simulate(m, engine="mixed", root="sqrt", deadline_s=1200)
+    out, st = solver.simulate(m, engine="mixed", root="sqrt", deadline_s=1200, tensor_cores=mode,
+                              refine_max=32 if mode == "bf16" else 0)
     assert st["status"] == 0 == int(d["status"])
     assert np.all(excess(out, d["out"]) <= 0), float(excess(out, d["out"]).max())
     assert st["be_steps"] == int(d["be_steps"])
